@@ -1,0 +1,181 @@
+/*
+ * otfem_gpu.h -- C ABI of libotfem_gpu.so, the GB300 (sm_103a) implementation
+ * of OpenTissue's stiffness-warped tetrahedral FEM time step.
+ *
+ * Every function returns an int status: 0 = OK, > 0 = warning (the step ran;
+ * e.g. the CG hit its iteration cap), < 0 = error.  otfem_last_error() gives
+ * a thread-local message for the last non-zero status.  A handle is bound to
+ * one CUDA stream and one device; calls on one handle are not thread-safe,
+ * distinct handles are independent.  Pointers marked "host" are host memory,
+ * pointers marked "device" are device memory on the handle's device.  Node
+ * vectors are packed xyz doubles (3 per node); 3x3 matrices are row-major.
+ *
+ * Reference citations are relative to the OpenTissue source tree.
+ */
+#ifndef OTFEM_GPU_H
+#define OTFEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OTFEM_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define OTFEM_API __attribute__((visibility("default")))
+#else
+#define OTFEM_API
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  OTFEM_OK = 0,
+  OTFEM_WARN_NOT_CONVERGED = 1,  /* relative-residual CG stopped at max_iterations */
+  OTFEM_ERR_INVALID_ARGUMENT = -1,
+  OTFEM_ERR_BAD_MESH = -2,       /* index out of range, repeated node, non-positive volume */
+  OTFEM_ERR_NOT_INITIALIZED = -3,/* otfem_init not called yet */
+  OTFEM_ERR_CUDA = -4,           /* a CUDA runtime call failed */
+  OTFEM_ERR_NONFINITE = -5,      /* NaN/Inf in a CG scalar */
+  OTFEM_ERR_TIMEOUT = -6,        /* a bounded device-side wait gave up */
+  OTFEM_ERR_OUT_OF_MEMORY = -7,
+  OTFEM_ERR_UNSUPPORTED = -8
+};
+
+/* ---- node fields for otfem_set_nodes / otfem_get_nodes ------------------ */
+enum {
+  OTFEM_COORD = 0,       /* m_coord        (fem_node_traits.h:44) set/get */
+  OTFEM_MODEL_COORD = 1, /* m_model_coord  (fem_node_traits.h:43) set/get */
+  OTFEM_VELOCITY = 2,    /* m_velocity     (fem_node_traits.h:46) set/get */
+  OTFEM_F_EXTERNAL = 3,  /* m_f_external   (fem_node_traits.h:48) set/get */
+  OTFEM_MASS = 4,        /* m_mass, 1 double per node (fem_node_traits.h:47) get */
+  OTFEM_F0 = 5,          /* m_f0           (fem_node_traits.h:39) get */
+  OTFEM_B = 6            /* m_b            (fem_node_traits.h:40) get */
+};
+
+/* ---- solver selection --------------------------------------------------- */
+enum {
+  /* The reference's own step (fem_simulate.h:94-112): FP64 assembled K and A
+   * rows, reference operation order, CG with min/max iterations, the absolute
+   * clamps tiny = 1e-10 and the d1 < 0.001 break (fem_conjugate_gradients.h). */
+  OTFEM_SOLVER_REFERENCE = 0,
+  /* Matrix-free step: FP64 orientation and right-hand side, FP32 stiffness
+   * apply, FP64 CG vectors, dot products and alpha/beta, residual replaced
+   * by b - A v every refresh_period iterations, stop at ||r|| <= rtol*||b||.
+   * One persistent CG kernel per step, replayed from a CUDA graph. */
+  OTFEM_SOLVER_MIXED = 1,
+  /* Matrix-free step with the FP64 stiffness apply (accuracy reference for the
+   * mixed solver; FP64 throughput on GB300 is far below FP32). */
+  OTFEM_SOLVER_FP64 = 2
+};
+
+enum {
+  OTFEM_WARM_START_PREVIOUS = 0, /* CG starts from the previous velocity (reference) */
+  OTFEM_WARM_START_LEARNED = 1   /* CG starts from v + MLP-predicted dv */
+};
+
+typedef struct otfem_solver_params {
+  int solver;               /* OTFEM_SOLVER_* */
+  double mass_damping;      /* Rayleigh mass coefficient; reference 2.0 (fem_simulate.h:104) */
+  int min_iterations;       /* reference solver: 20 (fem_simulate.h:108) */
+  int max_iterations;       /* reference: 20 (fem_simulate.h:109); matrix-free: cap */
+  double rtol;              /* matrix-free: stop at ||r|| <= rtol*||b|| (free rows) */
+  int refresh_period;       /* matrix-free: recompute r = b - A v every N iterations (16) */
+  int sequential_dots;      /* reference solver: 1 = sum dot products in node order on one
+                               thread (bit-identical to the reference), 0 = parallel tree */
+  int warm_start;           /* OTFEM_WARM_START_* */
+  int graph;                /* 1 = replay the step from a CUDA graph (default) */
+} otfem_solver_params;
+
+typedef struct otfem_step_stats {
+  int iterations;           /* CG iterations taken this step */
+  int status;               /* same code the call returned */
+  double rel_residual;      /* ||b - A v|| / ||b|| over free rows at exit (matrix-free) */
+  double initial_rel_residual; /* same for the initial guess */
+  double bnorm;             /* ||b|| over free rows */
+} otfem_step_stats;
+
+typedef struct otfem_mesh_desc {
+  int32_t num_nodes;
+  int32_t num_tets;
+  const int32_t* tets;         /* host, 4*num_tets node indices i,j,k,m (t4mesh_t4tetrahedron.h:39) */
+  const double* coord;         /* host, 3*num_nodes, m_coord */
+  const double* model_coord;   /* host, 3*num_nodes, m_model_coord (NULL: = coord) */
+  const uint8_t* fixed;        /* host, num_nodes, m_fixed (NULL: none fixed) */
+} otfem_mesh_desc;
+
+typedef struct otfem_context* otfem_handle;
+
+/* Defaults: reference solver, mass damping 2, 20/20 iterations, rtol 1e-6,
+ * refresh 16, parallel dots, previous-velocity warm start, graph on. */
+OTFEM_API void otfem_default_params(otfem_solver_params* p);
+
+OTFEM_API const char* otfem_last_error(void);
+OTFEM_API int otfem_abi_version(void);
+
+/* Creates the device-resident mesh (replaces building fem::Mesh, fem_mesh.h:21-34,
+ * over t4mesh::T4Mesh, t4mesh.h:48-55).  stream: a cudaStream_t (NULL = the
+ * legacy default stream).  Builds the node->tet incidence and the K_row
+ * sparsity pattern on the GPU.  The fixed flags must be final before otfem_init
+ * (compute_mass reads them, fem_compute_mass.h:154-160). */
+OTFEM_API int otfem_create(const otfem_mesh_desc* desc, void* stream, otfem_handle* out);
+OTFEM_API int otfem_destroy(otfem_handle h);
+OTFEM_API int otfem_num_nodes(otfem_handle h, int32_t* n);
+OTFEM_API int otfem_num_tets(otfem_handle h, int32_t* t);
+
+/* fem::init (fem_init.h:45-65): uniform material, element stiffness, lumped
+ * mass, plasticity state. */
+OTFEM_API int otfem_init(otfem_handle h, double young, double poisson, double density, double c_yield,
+               double c_creep, double c_max);
+
+/* Node field transfer (direct member access on the reference's nodes). */
+OTFEM_API int otfem_set_nodes(otfem_handle h, int field, const double* host_src, int64_t count);
+OTFEM_API int otfem_get_nodes(otfem_handle h, int field, double* host_dst, int64_t count);
+OTFEM_API int otfem_set_nodes_device(otfem_handle h, int field, const double* device_src, int64_t count);
+OTFEM_API int otfem_get_nodes_device(otfem_handle h, int field, double* device_dst, int64_t count);
+OTFEM_API int otfem_set_fixed(otfem_handle h, const uint8_t* host_fixed, int64_t count);
+
+/* fem::simulate (fem_simulate.h:49-113) with the reference's fixed solver
+ * settings.  Asynchronous on the handle's stream. */
+OTFEM_API int otfem_simulate(otfem_handle h, double time_step, int use_stiffness_warping);
+/* The same step with explicit solver parameters; stats (optional, host) are
+ * filled after a stream synchronisation. */
+OTFEM_API int otfem_simulate_ex(otfem_handle h, double time_step, int use_stiffness_warping,
+                      const otfem_solver_params* params, otfem_step_stats* stats);
+/* Reads the statistics of the last step (synchronises the stream). */
+OTFEM_API int otfem_last_stats(otfem_handle h, otfem_step_stats* stats);
+OTFEM_API int otfem_synchronize(otfem_handle h);
+
+/* fem::update_original_coord (fem_update_original_coord.h:28-33). */
+OTFEM_API int otfem_update_original_coord(otfem_handle h);
+
+/* fem::export_K (fem_export_k.h:23-68) as CSR of 3x3 blocks.  Rows of fixed
+ * nodes hold one identity block; columns of fixed nodes are omitted.  Before
+ * the first reference-solver step no K is assembled (empty free rows), as in
+ * the reference.  Call with NULL arrays to get the block count. */
+OTFEM_API int otfem_export_k_csr(otfem_handle h, int64_t* nnz_blocks, int32_t* row_ptr, int32_t* col_idx,
+                       double* values);
+/* The K_row key sets of all nodes (fem_node_traits.h:30-36), built on the GPU
+ * at otfem_create: CSR with ascending columns.  NULL arrays: count only. */
+OTFEM_API int otfem_k_pattern(otfem_handle h, int64_t* nnz_blocks, int32_t* row_ptr, int32_t* col_idx);
+/* The assembled K_row values (9 doubles per pattern block) of the last
+ * reference-solver step. */
+OTFEM_API int otfem_k_values(otfem_handle h, double* host_values);
+
+/* Per-tet state: m_Re (9 doubles, row-major), m_plastic (6), m_V (1). */
+OTFEM_API int otfem_get_orientations(otfem_handle h, double* host_re);
+OTFEM_API int otfem_get_plastic(otfem_handle h, double* host_plastic);
+OTFEM_API int otfem_get_volumes(otfem_handle h, double* host_volume);
+
+/* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* Number of kernels this handle has enqueued so far (graph replays included). */
+OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);
+/* Launch shape of the persistent CG kernel (grid CTAs, threads per CTA). */
+OTFEM_API int otfem_solver_shape(otfem_handle h, int32_t* grid, int32_t* block);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,145 @@
+"""ctypes declarations of the C ABI in include/otfem_gpu.h.
+
+Loads the in-tree libotfem_gpu.so (opentissue_gb300/_build/).  There is no
+fallback: if the library is missing or cannot be loaded, ``lib()`` raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libotfem_gpu.so")
+
+# status codes
+OK = 0
+WARN_NOT_CONVERGED = 1
+ERR_INVALID_ARGUMENT = -1
+ERR_BAD_MESH = -2
+ERR_NOT_INITIALIZED = -3
+ERR_CUDA = -4
+ERR_NONFINITE = -5
+ERR_TIMEOUT = -6
+ERR_OUT_OF_MEMORY = -7
+ERR_UNSUPPORTED = -8
+
+# node fields
+COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B = range(7)
+# solvers
+SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
+WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
+
+
+class SolverParams(ctypes.Structure):
+    _fields_ = [
+        ("solver", ctypes.c_int),
+        ("mass_damping", ctypes.c_double),
+        ("min_iterations", ctypes.c_int),
+        ("max_iterations", ctypes.c_int),
+        ("rtol", ctypes.c_double),
+        ("refresh_period", ctypes.c_int),
+        ("sequential_dots", ctypes.c_int),
+        ("warm_start", ctypes.c_int),
+        ("graph", ctypes.c_int),
+    ]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int),
+        ("status", ctypes.c_int),
+        ("rel_residual", ctypes.c_double),
+        ("initial_rel_residual", ctypes.c_double),
+        ("bnorm", ctypes.c_double),
+    ]
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("num_nodes", ctypes.c_int32),
+        ("num_tets", ctypes.c_int32),
+        ("tets", ctypes.POINTER(ctypes.c_int32)),
+        ("coord", ctypes.POINTER(ctypes.c_double)),
+        ("model_coord", ctypes.POINTER(ctypes.c_double)),
+        ("fixed", ctypes.POINTER(ctypes.c_uint8)),
+    ]
+
+
+class OtfemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"otfem error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_h = ctypes.c_void_p
+
+# every exported symbol with (restype, argtypes); test_abi checks this list
+# against include/otfem_gpu.h
+SIGNATURES = {
+    "otfem_default_params": (None, [ctypes.POINTER(SolverParams)]),
+    "otfem_last_error": (ctypes.c_char_p, []),
+    "otfem_abi_version": (ctypes.c_int, []),
+    "otfem_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.c_void_p, ctypes.POINTER(_h)]),
+    "otfem_destroy": (ctypes.c_int, [_h]),
+    "otfem_num_nodes": (ctypes.c_int, [_h, _i32p]),
+    "otfem_num_tets": (ctypes.c_int, [_h, _i32p]),
+    "otfem_init": (ctypes.c_int, [_h] + [ctypes.c_double] * 6),
+    "otfem_set_nodes": (ctypes.c_int, [_h, ctypes.c_int, _dp, ctypes.c_int64]),
+    "otfem_get_nodes": (ctypes.c_int, [_h, ctypes.c_int, _dp, ctypes.c_int64]),
+    "otfem_set_nodes_device": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64]),
+    "otfem_get_nodes_device": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64]),
+    "otfem_set_fixed": (ctypes.c_int, [_h, _u8p, ctypes.c_int64]),
+    "otfem_simulate": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int]),
+    "otfem_simulate_ex": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverParams),
+                                         ctypes.POINTER(StepStats)]),
+    "otfem_last_stats": (ctypes.c_int, [_h, ctypes.POINTER(StepStats)]),
+    "otfem_synchronize": (ctypes.c_int, [_h]),
+    "otfem_update_original_coord": (ctypes.c_int, [_h]),
+    "otfem_export_k_csr": (ctypes.c_int, [_h, _i64p, _i32p, _i32p, _dp]),
+    "otfem_k_pattern": (ctypes.c_int, [_h, _i64p, _i32p, _i32p]),
+    "otfem_k_values": (ctypes.c_int, [_h, _dp]),
+    "otfem_get_orientations": (ctypes.c_int, [_h, _dp]),
+    "otfem_get_plastic": (ctypes.c_int, [_h, _dp]),
+    "otfem_get_volumes": (ctypes.c_int, [_h, _dp]),
+    "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),
+    "otfem_solver_shape": (ctypes.c_int, [_h, _i32p, _i32p]),
+}
+
+
+def lib(path=None):
+    """Loads libotfem_gpu.so and declares every exported function."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libotfem_gpu.so is not built ({p}); run __graft_entry__.build()")
+    handle = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = handle
+    return handle
+
+
+def last_error():
+    return lib().otfem_last_error().decode(errors="replace")
+
+
+def check(rc, allow_warning=True):
+    if rc < 0 or (rc > 0 and not allow_warning):
+        raise OtfemError(rc, last_error())
+    return rc
+
+
+def default_params(**overrides):
+    p = SolverParams()
+    lib().otfem_default_params(ctypes.byref(p))
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p

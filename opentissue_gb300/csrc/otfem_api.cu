@@ -1,0 +1,514 @@
+// otfem_api.cu -- the C ABI of libotfem_gpu.so (include/otfem_gpu.h): context
+// lifetime, host<->device transfers, and the step orchestration, replayed
+// from a CUDA graph per (solver, dt, warp, parameters) key.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "otfem_internal.h"
+
+using otfem::Context;
+
+struct otfem_context {
+  Context c;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(OTFEM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define OT_CUDA(call)                                                  \
+  do {                                                                 \
+    cudaError_t e_ = (call);                                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);                \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count > 0 ? count : 1));
+}
+
+void free_all(Context& c) {
+  void* ptrs[] = {c.tets, c.x, c.x0, c.v, c.fext, c.mass, c.f0, c.b, c.fixed, c.prev, c.update,
+                  c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
+                  c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.inc_ptr,
+                  c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.q_d,
+                  c.p_d4, c.v_d4, c.partials, c.sync, c.stats};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c.stats_host) cudaFreeHost(c.stats_host);
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+}
+
+double* node_field(Context& c, int field) {
+  switch (field) {
+    case OTFEM_COORD: return c.x;
+    case OTFEM_MODEL_COORD: return c.x0;
+    case OTFEM_VELOCITY: return c.v;
+    case OTFEM_F_EXTERNAL: return c.fext;
+    case OTFEM_MASS: return c.mass;
+    case OTFEM_F0: return c.f0;
+    case OTFEM_B: return c.last_solver == OTFEM_SOLVER_REFERENCE ? c.b : c.bvec;
+    default: return nullptr;
+  }
+}
+
+int64_t field_count(Context& c, int field) { return field == OTFEM_MASS ? int64_t(c.N) : 3 * int64_t(c.N); }
+
+int check_params(const otfem_solver_params& p) {
+  if (p.solver < OTFEM_SOLVER_REFERENCE || p.solver > OTFEM_SOLVER_FP64)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown solver");
+  if (p.max_iterations < 0 || p.min_iterations < 0)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "iteration counts must be non-negative");
+  if (p.solver != OTFEM_SOLVER_REFERENCE && !(p.rtol >= 0.0))
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
+  if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
+  if (p.warm_start == OTFEM_WARM_START_LEARNED)
+    return fail(OTFEM_ERR_UNSUPPORTED, "learned warm start needs an attached warm-start network");
+  return OTFEM_OK;
+}
+
+// Enqueues one step on c.stream (no host synchronisation).
+cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_params& p) {
+  cudaError_t e;
+  if (p.solver == OTFEM_SOLVER_REFERENCE) {
+    // fem_simulate.h:94-112
+    if ((e = otfem::launch_orientation(c, warp)) != cudaSuccess) return e;
+    if ((e = otfem::launch_assembly(c)) != cudaSuccess) return e;
+    if ((e = otfem::launch_plasticity(c, dt)) != cudaSuccess) return e;
+    if ((e = otfem::launch_dynamics_assembly(c, p.mass_damping, dt)) != cudaSuccess) return e;
+    if ((e = otfem::launch_reference_cg(c, p.min_iterations, p.max_iterations, p.sequential_dots != 0)) !=
+        cudaSuccess)
+      return e;
+    if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
+  } else {
+    if ((e = otfem::launch_mixed_step(c, dt, warp, p)) != cudaSuccess) return e;
+  }
+  return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
+}
+
+std::string step_key(double dt, bool warp, const otfem_solver_params& p) {
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d", p.solver, dt, int(warp), p.mass_damping,
+           p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots, p.warm_start);
+  return buf;
+}
+
+int kernels_per_step(const Context& c, const otfem_solver_params& p) {
+  if (p.solver == OTFEM_SOLVER_REFERENCE) return 1 + 2 + 2 + 1 + (1 + 5 * p.max_iterations + 1) + 1;
+  return 2 + (c.plastic_active ? 2 : 0);
+}
+
+}  // namespace
+
+extern "C" {
+
+void otfem_default_params(otfem_solver_params* p) {
+  if (!p) return;
+  p->solver = OTFEM_SOLVER_REFERENCE;
+  p->mass_damping = 2.0;
+  p->min_iterations = 20;
+  p->max_iterations = 20;
+  p->rtol = 1e-6;
+  p->refresh_period = 16;
+  p->sequential_dots = 0;
+  p->warm_start = OTFEM_WARM_START_PREVIOUS;
+  p->graph = 1;
+}
+
+const char* otfem_last_error(void) { return g_last_error.c_str(); }
+int otfem_abi_version(void) { return OTFEM_ABI_VERSION; }
+
+int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
+  if (!d || !out) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (d->num_nodes < 0 || d->num_tets < 0) return fail(OTFEM_ERR_INVALID_ARGUMENT, "negative size");
+  if ((d->num_tets > 0 && !d->tets) || (d->num_nodes > 0 && !d->coord))
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "missing tets or coord");
+  if (int64_t(d->num_tets) * 16 > 0x7fffffffLL) return fail(OTFEM_ERR_INVALID_ARGUMENT, "too many tets");
+  // t4mesh_t4mesh.h:139-144 and :232 (verify_nodes): indices in range and distinct
+  for (int64_t t = 0; t < d->num_tets; ++t) {
+    const int32_t* n = d->tets + 4 * t;
+    for (int a = 0; a < 4; ++a) {
+      if (n[a] < 0 || n[a] >= d->num_nodes)
+        return fail(OTFEM_ERR_BAD_MESH, "tet " + std::to_string(t) + " has a node index out of range");
+      for (int b = 0; b < a; ++b)
+        if (n[a] == n[b]) return fail(OTFEM_ERR_BAD_MESH, "tet " + std::to_string(t) + " repeats a node");
+    }
+  }
+  otfem_context* h = new (std::nothrow) otfem_context;
+  if (!h) return fail(OTFEM_ERR_OUT_OF_MEMORY, "host allocation failed");
+  Context& c = h->c;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  c.N = d->num_nodes;
+  c.T = d->num_tets;
+  const size_t N = size_t(c.N), T = size_t(c.T);
+  int rc = OTFEM_OK;
+  auto bail = [&](cudaError_t e, const char* what) {
+    rc = cuda_fail(e, what);
+    free_all(c);
+    delete h;
+    return rc;
+  };
+  cudaError_t e;
+#define OT_ALLOC(ptr, n) \
+  if ((e = dalloc(&(ptr), (n))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr);
+  if ((e = cudaGetDevice(&c.device)) != cudaSuccess) return bail(e, "cudaGetDevice");
+  if ((e = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device)) != cudaSuccess)
+    return bail(e, "cudaDeviceGetAttribute");
+  OT_ALLOC(c.tets, T);
+  OT_ALLOC(c.x, 3 * N);
+  OT_ALLOC(c.x0, 3 * N);
+  OT_ALLOC(c.v, 3 * N);
+  OT_ALLOC(c.fext, 3 * N);
+  OT_ALLOC(c.mass, N);
+  OT_ALLOC(c.f0, 3 * N);
+  OT_ALLOC(c.b, 3 * N);
+  OT_ALLOC(c.fixed, N);
+  OT_ALLOC(c.prev, 3 * N);
+  OT_ALLOC(c.update, 3 * N);
+  OT_ALLOC(c.residual, 3 * N);
+  OT_ALLOC(c.node_dots, 2 * N);
+  OT_ALLOC(c.scal, 8);
+  OT_ALLOC(c.Ke, 144 * T);
+  OT_ALLOC(c.Re, 9 * T);
+  OT_ALLOC(c.V, T);
+  OT_ALLOC(c.E, 9 * T);
+  OT_ALLOC(c.Bv, 12 * T);
+  OT_ALLOC(c.D, 3 * T);
+  OT_ALLOC(c.plastic, 6 * T);
+  OT_ALLOC(c.young, T);
+  OT_ALLOC(c.poisson, T);
+  OT_ALLOC(c.density, T);
+  OT_ALLOC(c.yield, T);
+  OT_ALLOC(c.creep, T);
+  OT_ALLOC(c.cmax, T);
+  OT_ALLOC(c.tet_force, 12 * T);
+  OT_ALLOC(c.re_f, 9 * T);
+  OT_ALLOC(c.b_f, 9 * T);
+  OT_ALLOC(c.c_f, 3 * T);
+  OT_ALLOC(c.re_d, 9 * T);
+  OT_ALLOC(c.b_d, 9 * T);
+  OT_ALLOC(c.c_d, 3 * T);
+  OT_ALLOC(c.diag, N);
+  OT_ALLOC(c.r, 3 * N);
+  OT_ALLOC(c.p, 3 * N);
+  OT_ALLOC(c.bvec, 3 * N);
+  OT_ALLOC(c.p_f, N);
+  OT_ALLOC(c.v_f, N);
+  OT_ALLOC(c.q_f, N);
+  OT_ALLOC(c.q_d, N);
+  OT_ALLOC(c.p_d4, N);
+  OT_ALLOC(c.v_d4, N);
+  OT_ALLOC(c.sync, 1);
+  OT_ALLOC(c.stats, 1);
+  if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
+    return bail(e, "cudaMallocHost");
+  memset(c.stats_host, 0, sizeof(otfem::DeviceStats));
+  otfem::mixed_grid_shape(c, &c.mf_grid, &c.mf_block);
+  OT_ALLOC(c.partials, size_t(otfem::kMaxPartials) * c.mf_grid);
+
+  // zero-initialised node members (math_vector3.h:63-66) and uploads
+  const size_t bytes3 = sizeof(double) * 3 * N;
+  if ((e = cudaMemsetAsync(c.v, 0, bytes3, c.stream)) != cudaSuccess) return bail(e, "memset");
+  cudaMemsetAsync(c.fext, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.f0, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.b, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.prev, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.update, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.residual, 0, bytes3, c.stream);
+  cudaMemsetAsync(c.mass, 0, sizeof(double) * N, c.stream);
+  cudaMemsetAsync(c.fixed, 0, N > 0 ? N : 1, c.stream);
+  cudaMemsetAsync(c.plastic, 0, sizeof(double) * 6 * T, c.stream);
+  cudaMemsetAsync(c.sync, 0, sizeof(otfem::DeviceSync), c.stream);
+  cudaMemsetAsync(c.stats, 0, sizeof(otfem::DeviceStats), c.stream);
+  if (T && (e = cudaMemcpyAsync(c.tets, d->tets, sizeof(int4) * T, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+    return bail(e, "upload tets");
+  if (N) {
+    if ((e = cudaMemcpyAsync(c.x, d->coord, bytes3, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+      return bail(e, "upload coord");
+    const double* mc = d->model_coord ? d->model_coord : d->coord;
+    if ((e = cudaMemcpyAsync(c.x0, mc, bytes3, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+      return bail(e, "upload model coord");
+    if (d->fixed && (e = cudaMemcpyAsync(c.fixed, d->fixed, N, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+      return bail(e, "upload fixed");
+  }
+  if ((e = otfem::build_incidence(c)) != cudaSuccess) return bail(e, "build_incidence");
+  if ((e = otfem::build_pattern(c)) != cudaSuccess) return bail(e, "build_pattern");
+  OT_ALLOC(c.K, 9 * size_t(c.nnz));
+  OT_ALLOC(c.A, 9 * size_t(c.nnz));
+  cudaMemsetAsync(c.K, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream);
+  cudaMemsetAsync(c.A, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream);
+  if ((e = cudaStreamSynchronize(c.stream)) != cudaSuccess) return bail(e, "create sync");
+#undef OT_ALLOC
+  *out = h;
+  return OTFEM_OK;
+}
+
+int otfem_destroy(otfem_handle h) {
+  if (!h) return OTFEM_OK;
+  cudaStreamSynchronize(h->c.stream);
+  free_all(h->c);
+  delete h;
+  return OTFEM_OK;
+}
+
+int otfem_num_nodes(otfem_handle h, int32_t* n) {
+  if (!h || !n) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *n = h->c.N;
+  return OTFEM_OK;
+}
+
+int otfem_num_tets(otfem_handle h, int32_t* t) {
+  if (!h || !t) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *t = h->c.T;
+  return OTFEM_OK;
+}
+
+int otfem_init(otfem_handle h, double young, double poisson, double density, double c_yield,
+               double c_creep, double c_max) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  // fem_uniform_young.h:32, fem_uniform_poisson.h:33-34, fem_uniform_density.h:27,
+  // fem_initialize_plastic.h:42-44 (debug asserts in the reference)
+  if (!(young >= 0.0) || !(poisson >= 0.0 && poisson <= 0.5) || !(density > 0.0) || !(c_yield >= 0.0) ||
+      !(c_creep >= 0.0) || !(c_max >= 0.0))
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "material parameter out of range");
+  cudaError_t e;
+  if ((e = otfem::launch_init_elements(c, young, poisson, density, c_yield, c_creep, c_max)) != cudaSuccess)
+    return cuda_fail(e, "init elements");
+  if ((e = otfem::mixed_prepare(c)) != cudaSuccess) return cuda_fail(e, "prepare");
+  // clear_stiffness_assembly (fem_init.h:60)
+  OT_CUDA(cudaMemsetAsync(c.f0, 0, sizeof(double) * 3 * size_t(c.N), c.stream));
+  if (c.k_assembled) OT_CUDA(cudaMemsetAsync(c.K, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream));
+  std::vector<double> vol(size_t(c.T));
+  if (c.T) OT_CUDA(cudaMemcpyAsync(vol.data(), c.V, sizeof(double) * c.T, cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  c.plastic_active = c_creep > 0.0 && c_max > 0.0;
+  c.initialized = true;
+  if (c.graph) {
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+    c.graph_key.clear();
+  }
+  // fem_initialize_stiffness_elements.h:48
+  for (int t = 0; t < c.T; ++t)
+    if (!(vol[t] > 0.0))
+      return fail(OTFEM_ERR_BAD_MESH, "tet " + std::to_string(t) + " has non-positive volume");
+  return OTFEM_OK;
+}
+
+static int transfer(otfem_handle h, int field, double* ptr, int64_t count, bool to_device, cudaMemcpyKind kind) {
+  if (!h || (!ptr && count)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  double* d = node_field(c, field);
+  if (!d) return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown field");
+  if (to_device && field > OTFEM_F_EXTERNAL) return fail(OTFEM_ERR_INVALID_ARGUMENT, "field is read-only");
+  if (count != field_count(c, field)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "count does not match the field size");
+  if (!count) return OTFEM_OK;
+  size_t bytes = sizeof(double) * size_t(count);
+  if (to_device) {
+    OT_CUDA(cudaMemcpyAsync(d, ptr, bytes, kind, c.stream));
+  } else {
+    OT_CUDA(cudaMemcpyAsync(ptr, d, bytes, kind, c.stream));
+    if (kind == cudaMemcpyDeviceToHost) OT_CUDA(cudaStreamSynchronize(c.stream));
+  }
+  return OTFEM_OK;
+}
+
+int otfem_set_nodes(otfem_handle h, int field, const double* src, int64_t count) {
+  return transfer(h, field, const_cast<double*>(src), count, true, cudaMemcpyHostToDevice);
+}
+int otfem_get_nodes(otfem_handle h, int field, double* dst, int64_t count) {
+  return transfer(h, field, dst, count, false, cudaMemcpyDeviceToHost);
+}
+int otfem_set_nodes_device(otfem_handle h, int field, const double* src, int64_t count) {
+  return transfer(h, field, const_cast<double*>(src), count, true, cudaMemcpyDeviceToDevice);
+}
+int otfem_get_nodes_device(otfem_handle h, int field, double* dst, int64_t count) {
+  return transfer(h, field, dst, count, false, cudaMemcpyDeviceToDevice);
+}
+
+int otfem_set_fixed(otfem_handle h, const uint8_t* fixed, int64_t count) {
+  if (!h || (!fixed && count)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  if (count != h->c.N) return fail(OTFEM_ERR_INVALID_ARGUMENT, "count does not match the node count");
+  if (count) OT_CUDA(cudaMemcpyAsync(h->c.fixed, fixed, size_t(count), cudaMemcpyHostToDevice, h->c.stream));
+  return OTFEM_OK;
+}
+
+int otfem_simulate_ex(otfem_handle h, double dt, int warp, const otfem_solver_params* params,
+                      otfem_step_stats* stats) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (!(dt > 0.0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "time step must be positive");
+  otfem_solver_params p;
+  if (params) p = *params;
+  else otfem_default_params(&p);
+  int rc = check_params(p);
+  if (rc != OTFEM_OK) return rc;
+  bool use_warp = warp != 0;
+  cudaError_t e;
+  if (p.graph) {
+    std::string key = step_key(dt, use_warp, p);
+    if (!c.graph || key != c.graph_key) {
+      if (c.graph) {
+        cudaGraphExecDestroy(c.graph);
+        c.graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      OT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ee = enqueue_step(c, dt, use_warp, p);
+      cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
+      if (ee != cudaSuccess) return cuda_fail(ee, "capture step");
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&c.graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      c.graph_key = key;
+    }
+    OT_CUDA(cudaGraphLaunch(c.graph, c.stream));
+  } else {
+    if ((e = enqueue_step(c, dt, use_warp, p)) != cudaSuccess) return cuda_fail(e, "enqueue step");
+  }
+  if (p.solver == OTFEM_SOLVER_REFERENCE) c.k_assembled = true;
+  c.last_solver = p.solver;
+  c.launches += kernels_per_step(c, p);
+  if (stats) return otfem_last_stats(h, stats);
+  return OTFEM_OK;
+}
+
+int otfem_simulate(otfem_handle h, double dt, int warp) { return otfem_simulate_ex(h, dt, warp, nullptr, nullptr); }
+
+int otfem_last_stats(otfem_handle h, otfem_step_stats* s) {
+  if (!h || !s) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  const otfem::DeviceStats& d = *c.stats_host;
+  s->iterations = d.iterations;
+  s->status = d.status;
+  s->bnorm = d.bb > 0 ? sqrt(d.bb) : 0.0;
+  double ref = d.bb > 0 ? d.bb : 1.0;
+  s->rel_residual = sqrt(d.rr / ref);
+  s->initial_rel_residual = sqrt(d.rr0 / ref);
+  if (d.status < 0) {
+    const char* what = d.status == OTFEM_ERR_TIMEOUT ? "a device-side wait timed out"
+                       : d.status == OTFEM_ERR_NONFINITE ? "non-finite or non-positive CG scalar"
+                                                          : "device error";
+    return fail(d.status, what);
+  }
+  if (d.status > 0) g_last_error = "CG reached max_iterations before rtol";
+  return d.status;
+}
+
+int otfem_synchronize(otfem_handle h) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  OT_CUDA(cudaStreamSynchronize(h->c.stream));
+  return OTFEM_OK;
+}
+
+int otfem_update_original_coord(otfem_handle h) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (c.N) OT_CUDA(cudaMemcpyAsync(c.x0, c.x, sizeof(double) * 3 * size_t(c.N), cudaMemcpyDeviceToDevice, c.stream));
+  return OTFEM_OK;
+}
+
+int otfem_export_k_csr(otfem_handle h, int64_t* nnz_blocks, int32_t* row_ptr, int32_t* col_idx, double* values) {
+  if (!h || !nnz_blocks) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  int* cnt = nullptr;
+  OT_CUDA(dalloc(&cnt, size_t(c.N) + 1));
+  cudaError_t e = otfem::launch_export_k_counts(c, cnt);
+  std::vector<int> hc(size_t(c.N) + 1, 0), hp(size_t(c.N) + 1, 0);
+  if (e == cudaSuccess && c.N) e = cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * c.N, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) {
+    cudaFree(cnt);
+    return cuda_fail(e, "export counts");
+  }
+  for (int i = 0; i < c.N; ++i) hp[i + 1] = hp[i] + hc[i];
+  *nnz_blocks = hp[c.N];
+  if (!row_ptr || !col_idx || !values) {
+    cudaFree(cnt);
+    return OTFEM_OK;
+  }
+  int* dcols = nullptr;
+  double* dvals = nullptr;
+  e = dalloc(&dcols, size_t(hp[c.N]));
+  if (e == cudaSuccess) e = dalloc(&dvals, 9 * size_t(hp[c.N]));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cnt, hp.data(), sizeof(int) * (c.N + 1), cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) e = otfem::launch_export_k(c, cnt, dcols, dvals);
+  if (e == cudaSuccess && hp[c.N])
+    e = cudaMemcpyAsync(col_idx, dcols, sizeof(int) * hp[c.N], cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess && hp[c.N])
+    e = cudaMemcpyAsync(values, dvals, sizeof(double) * 9 * size_t(hp[c.N]), cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  cudaFree(cnt);
+  if (dcols) cudaFree(dcols);
+  if (dvals) cudaFree(dvals);
+  if (e != cudaSuccess) return cuda_fail(e, "export fill");
+  memcpy(row_ptr, hp.data(), sizeof(int) * (size_t(c.N) + 1));
+  return OTFEM_OK;
+}
+
+int otfem_k_pattern(otfem_handle h, int64_t* nnz_blocks, int32_t* row_ptr, int32_t* col_idx) {
+  if (!h || !nnz_blocks) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  *nnz_blocks = c.nnz;
+  if (!row_ptr || !col_idx) return OTFEM_OK;
+  OT_CUDA(cudaMemcpyAsync(row_ptr, c.row_ptr, sizeof(int) * (size_t(c.N) + 1), cudaMemcpyDeviceToHost, c.stream));
+  if (c.nnz) OT_CUDA(cudaMemcpyAsync(col_idx, c.cols, sizeof(int) * size_t(c.nnz), cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  return OTFEM_OK;
+}
+
+int otfem_k_values(otfem_handle h, double* vals) {
+  if (!h || (!vals && h->c.nnz)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  if (c.nnz) OT_CUDA(cudaMemcpyAsync(vals, c.K, sizeof(double) * 9 * size_t(c.nnz), cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  return OTFEM_OK;
+}
+
+static int get_tet_array(otfem_handle h, const double* src, size_t per, double* dst) {
+  if (!h || (!dst && h->c.T)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  if (c.T) OT_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * per * size_t(c.T), cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  return OTFEM_OK;
+}
+
+int otfem_get_orientations(otfem_handle h, double* re) { return get_tet_array(h, h ? h->c.Re : nullptr, 9, re); }
+int otfem_get_plastic(otfem_handle h, double* pl) { return get_tet_array(h, h ? h->c.plastic : nullptr, 6, pl); }
+int otfem_get_volumes(otfem_handle h, double* vol) { return get_tet_array(h, h ? h->c.V : nullptr, 1, vol); }
+
+int otfem_launch_count(otfem_handle h, int64_t* n) {
+  if (!h || !n) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *n = h->c.launches;
+  return OTFEM_OK;
+}
+
+int otfem_solver_shape(otfem_handle h, int32_t* grid, int32_t* block) {
+  if (!h || !grid || !block) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *grid = h->c.mf_grid;
+  *block = h->c.mf_block;
+  return OTFEM_OK;
+}
+
+}  // extern "C"

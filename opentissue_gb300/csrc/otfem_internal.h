@@ -1,0 +1,118 @@
+// otfem_internal.h -- device-resident state of one FEM mesh and the host-side
+// launch wrappers shared by the translation units of libotfem_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/otfem_gpu.h"
+
+namespace otfem {
+
+// Per-CTA partial sums written before a grid barrier (one slot per scalar).
+constexpr int kMaxPartials = 8;
+
+// Counters for the bounded grid barrier and the device status word.
+struct DeviceSync {
+  unsigned int count;    // CTAs arrived at the current barrier
+  unsigned int gen;      // barrier generation
+  int status;            // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
+  int pad;
+};
+
+// Statistics written by the step kernels (device memory).
+struct DeviceStats {
+  int iterations;
+  int status;
+  double rr;       // squared residual norm at exit (free rows)
+  double rr0;      // squared residual of the initial guess
+  double bb;       // squared norm of b (free rows)
+};
+
+// Everything a mesh keeps on the device.  Node vectors are packed xyz
+// doubles; per-tet matrices row-major.  Arrays named *_f are FP32 copies used
+// by the matrix-free apply, stored structure-of-arrays (component c of tet t
+// at [c*T + t]) so that a warp's loads are coalesced.
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int N = 0, T = 0;
+  bool initialized = false;
+  bool k_assembled = false;
+  bool plastic_active = false;
+
+  // mesh and node fields (fem_node_traits.h:37-52)
+  int4* tets = nullptr;
+  double *x = nullptr, *x0 = nullptr, *v = nullptr, *fext = nullptr, *mass = nullptr;
+  double *f0 = nullptr, *b = nullptr;
+  unsigned char* fixed = nullptr;
+  // reference-solver CG vectors (persist between steps like the node members)
+  double *prev = nullptr, *update = nullptr, *residual = nullptr;
+  double* node_dots = nullptr;  // 2*N per-node dot products for the reductions
+  double* scal = nullptr;       // device scalars of the reference CG
+
+  // tet fields (fem_tetrahedron_traits.h:18-49)
+  double *Ke = nullptr, *Re = nullptr, *V = nullptr, *E = nullptr /*e10,e20,e30*/;
+  double *Bv = nullptr, *D = nullptr, *plastic = nullptr;
+  double *young = nullptr, *poisson = nullptr, *density = nullptr;
+  double *yield = nullptr, *creep = nullptr, *cmax = nullptr;
+  double* tet_force = nullptr;  // 12*T scratch: per-tet node forces
+
+  // node -> incident (tet, slot) lists, ascending tet index
+  int* inc_ptr = nullptr;  // N+1
+  int* inc_ent = nullptr;  // 4T entries tet*4+slot
+  // K_row pattern (ascending columns) and per-block contribution lists
+  int64_t nnz = 0;
+  int* row_ptr = nullptr;
+  int* cols = nullptr;
+  int* bc_ptr = nullptr;  // nnz+1
+  int* bc_ent = nullptr;  // 16T entries tet*16 + li*4 + lj, ascending tet
+  double *K = nullptr, *A = nullptr;
+
+  // matrix-free data
+  float *re_f = nullptr, *b_f = nullptr, *c_f = nullptr;  // 9T, 9T, 3T
+  double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
+  double* diag = nullptr;                                 // N: m(1+dt*alpha)
+  double *r = nullptr, *p = nullptr, *bvec = nullptr;    // 3N
+  float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N
+  double4* q_d = nullptr;                                  // N (FP64 apply accumulator)
+  double4 *p_d4 = nullptr, *v_d4 = nullptr;               // N (FP64 apply operands)
+  double* partials = nullptr;                              // kMaxPartials * max grid
+  DeviceSync* sync = nullptr;
+  DeviceStats* stats = nullptr;
+  DeviceStats* stats_host = nullptr;  // pinned
+  int mf_grid = 0, mf_block = 0;      // persistent CG launch shape
+  int last_solver = -1;
+  int64_t launches = 0;               // kernels enqueued by this handle
+
+  // cached step graph
+  cudaGraphExec_t graph = nullptr;
+  std::string graph_key;
+  int last_status = 0;
+};
+
+// ---- pattern / incidence (otfem_pattern.cu) ------------------------------
+cudaError_t build_incidence(Context& c);
+cudaError_t build_pattern(Context& c);
+
+// ---- reference-order FP64 kernels (otfem_exact.cu) ------------------------
+cudaError_t launch_init_elements(Context& c, double young, double poisson, double density,
+                                 double c_yield, double c_creep, double c_max);
+cudaError_t launch_orientation(Context& c, bool warp);
+cudaError_t launch_assembly(Context& c);
+cudaError_t launch_plasticity(Context& c, double dt);
+cudaError_t launch_dynamics_assembly(Context& c, double mass_damping, double dt);
+cudaError_t launch_reference_cg(Context& c, int min_it, int max_it, bool sequential);
+cudaError_t launch_position_update(Context& c, double dt);
+cudaError_t launch_export_k(Context& c, int* row_ptr_out, int* cols_out, double* vals_out);
+cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
+
+// ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
+cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
+cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solver_params& p);
+int mixed_grid_shape(Context& c, int* grid, int* block);
+
+}  // namespace otfem

@@ -1,0 +1,213 @@
+// otfem_pattern.cu -- builds on the GPU, once per mesh:
+//  * the node -> (tet, slot) incidence lists in ascending tet order (the
+//    per-node tet list of t4mesh_t4node.h:36, sorted);
+//  * the K_row sparsity pattern: for every node i the ascending set of nodes j
+//    that share a tet with i, which are exactly the keys that
+//    p_i->K(p_j->idx()) creates in stiffness_assembly
+//    (fem_stiffness_assembly.h:199-201; std::map keeps them sorted);
+//  * for every pattern block the ascending-tet list of (tet, local i, local j)
+//    contributions, used by the reference-order assembly gather.
+// All steps are deterministic: counts by atomics, then per-node sorting.
+#include "otfem_internal.h"
+
+namespace otfem {
+namespace {
+
+constexpr int kThreads = 256;
+inline int blocks_for(long n) { long b = (n + kThreads - 1) / kThreads; return b > 0 ? int(b) : 1; }
+
+__global__ void k_count_incidence(int T, const int4* __restrict__ tets, int* cnt) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  int4 n = tets[t];
+  atomicAdd(cnt + n.x, 1);
+  atomicAdd(cnt + n.y, 1);
+  atomicAdd(cnt + n.z, 1);
+  atomicAdd(cnt + n.w, 1);
+}
+
+// Exclusive scan of n ints into out[0..n] (out[n] = total) with one block:
+// each thread scans a contiguous chunk, chunk totals are scanned in shared
+// memory.  Used only at set-up.
+__global__ void k_scan_one_block(long n, const int* __restrict__ in, int* out) {
+  __shared__ long part[1024];
+  long chunk = (n + blockDim.x - 1) / blockDim.x;
+  long lo = threadIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
+  long s = 0;
+  for (long i = lo; i < hi; ++i) s += in[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long acc = 0;
+    for (int k = 0; k < (int)blockDim.x; ++k) {
+      long v = part[k];
+      part[k] = acc;
+      acc += v;
+    }
+    out[n] = (int)acc;
+  }
+  __syncthreads();
+  long acc = part[threadIdx.x];
+  for (long i = lo; i < hi; ++i) {
+    int v = in[i];
+    out[i] = (int)acc;
+    acc += v;
+  }
+}
+
+__global__ void k_fill_incidence(int T, const int4* __restrict__ tets, const int* __restrict__ ptr,
+                                 int* cursor, int* ent) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  int4 n = tets[t];
+  int nn[4] = {n.x, n.y, n.z, n.w};
+  for (int s = 0; s < 4; ++s) {
+    int pos = atomicAdd(cursor + nn[s], 1);
+    ent[ptr[nn[s]] + pos] = t * 4 + s;
+  }
+}
+
+__device__ void insertion_sort(int* a, int n) {
+  for (int i = 1; i < n; ++i) {
+    int v = a[i], j = i - 1;
+    while (j >= 0 && a[j] > v) {
+      a[j + 1] = a[j];
+      --j;
+    }
+    a[j + 1] = v;
+  }
+}
+
+__global__ void k_sort_incidence(int N, const int* __restrict__ ptr, int* ent) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  insertion_sort(ent + ptr[i], ptr[i + 1] - ptr[i]);
+}
+
+// Candidate neighbours of node i (the 4 nodes of each incident tet) sorted and
+// de-duplicated in place in scratch[4*ptr[i] ...]; cnt[i] = distinct count.
+__global__ void k_row_unique(int N, const int4* __restrict__ tets, const int* __restrict__ ptr,
+                             const int* __restrict__ ent, int* scratch, int* cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int* s = scratch + 4L * ptr[i];
+  int m = 0;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    int4 n = tets[ent[q] >> 2];
+    s[m++] = n.x;
+    s[m++] = n.y;
+    s[m++] = n.z;
+    s[m++] = n.w;
+  }
+  insertion_sort(s, m);
+  int u = 0;
+  for (int k = 0; k < m; ++k)
+    if (k == 0 || s[k] != s[k - 1]) s[u++] = s[k];
+  cnt[i] = u;
+}
+
+__global__ void k_row_fill(int N, const int* __restrict__ ptr, const int* __restrict__ scratch,
+                           const int* __restrict__ row_ptr, int* cols) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int* s = scratch + 4L * ptr[i];
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) cols[k] = s[k - row_ptr[i]];
+}
+
+__device__ int find_col(const int* cols, int lo, int hi, int j) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (cols[mid] < j) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Per row: walk incident tets in ascending order; every local pair (li, lj)
+// with tet[li] == i contributes once to block (i, tet[lj]).
+__global__ void k_bc_count(int N, const int4* __restrict__ tets, const int* __restrict__ ptr,
+                           const int* __restrict__ ent, const int* __restrict__ row_ptr,
+                           const int* __restrict__ cols, int* bc_cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    int4 n4 = tets[ent[q] >> 2];
+    int nn[4] = {n4.x, n4.y, n4.z, n4.w};
+    for (int lj = 0; lj < 4; ++lj) bc_cnt[find_col(cols, row_ptr[i], row_ptr[i + 1], nn[lj])] += 1;
+  }
+}
+
+__global__ void k_bc_fill(int N, const int4* __restrict__ tets, const int* __restrict__ ptr,
+                          const int* __restrict__ ent, const int* __restrict__ row_ptr,
+                          const int* __restrict__ cols, const int* __restrict__ bc_ptr, int* bc_cur,
+                          int* bc_ent) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    int t = ent[q] >> 2, li = ent[q] & 3;
+    int4 n4 = tets[t];
+    int nn[4] = {n4.x, n4.y, n4.z, n4.w};
+    for (int lj = 0; lj < 4; ++lj) {
+      int b = find_col(cols, row_ptr[i], row_ptr[i + 1], nn[lj]);
+      bc_ent[bc_ptr[b] + bc_cur[b]++] = t * 16 + li * 4 + lj;
+    }
+  }
+}
+
+#define OT_TRY(x)                       \
+  do {                                  \
+    cudaError_t e_ = (x);               \
+    if (e_ != cudaSuccess) return e_;   \
+  } while (0)
+
+}  // namespace
+
+cudaError_t build_incidence(Context& c) {
+  int* cnt = nullptr;
+  OT_TRY(cudaMallocAsync(&cnt, sizeof(int) * (c.N + 1), c.stream));
+  OT_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (c.N + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&c.inc_ptr, sizeof(int) * (c.N + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&c.inc_ent, sizeof(int) * (4L * c.T + 1), c.stream));
+  k_count_incidence<<<blocks_for(c.T), kThreads, 0, c.stream>>>(c.T, c.tets, cnt);
+  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.N, cnt, c.inc_ptr);
+  OT_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (c.N + 1), c.stream));
+  k_fill_incidence<<<blocks_for(c.T), kThreads, 0, c.stream>>>(c.T, c.tets, c.inc_ptr, cnt, c.inc_ent);
+  k_sort_incidence<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.inc_ptr, c.inc_ent);
+  OT_TRY(cudaGetLastError());
+  OT_TRY(cudaFreeAsync(cnt, c.stream));
+  return cudaSuccess;
+}
+
+cudaError_t build_pattern(Context& c) {
+  int *scratch = nullptr, *cnt = nullptr;
+  OT_TRY(cudaMallocAsync(&scratch, sizeof(int) * (16L * c.T + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&cnt, sizeof(int) * (c.N + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&c.row_ptr, sizeof(int) * (c.N + 1), c.stream));
+  k_row_unique<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, scratch, cnt);
+  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.N, cnt, c.row_ptr);
+  int nnz = 0;
+  OT_TRY(cudaMemcpyAsync(&nnz, c.row_ptr + c.N, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  OT_TRY(cudaStreamSynchronize(c.stream));
+  c.nnz = nnz;
+  OT_TRY(cudaMallocAsync(&c.cols, sizeof(int) * (c.nnz + 1), c.stream));
+  k_row_fill<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.inc_ptr, scratch, c.row_ptr, c.cols);
+  // block contribution lists
+  int *bc_cnt = nullptr;
+  OT_TRY(cudaMallocAsync(&bc_cnt, sizeof(int) * (c.nnz + 1), c.stream));
+  OT_TRY(cudaMemsetAsync(bc_cnt, 0, sizeof(int) * (c.nnz + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&c.bc_ptr, sizeof(int) * (c.nnz + 1), c.stream));
+  OT_TRY(cudaMallocAsync(&c.bc_ent, sizeof(int) * (16L * c.T + 1), c.stream));
+  k_bc_count<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, c.row_ptr,
+                                                         c.cols, bc_cnt);
+  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.nnz, bc_cnt, c.bc_ptr);
+  OT_TRY(cudaMemsetAsync(bc_cnt, 0, sizeof(int) * (c.nnz + 1), c.stream));
+  k_bc_fill<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, c.row_ptr,
+                                                        c.cols, c.bc_ptr, bc_cnt, c.bc_ent);
+  OT_TRY(cudaGetLastError());
+  OT_TRY(cudaFreeAsync(bc_cnt, c.stream));
+  OT_TRY(cudaFreeAsync(cnt, c.stream));
+  OT_TRY(cudaFreeAsync(scratch, c.stream));
+  return cudaSuccess;
+}
+
+}  // namespace otfem

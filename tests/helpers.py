@@ -1,0 +1,172 @@
+"""Shared test helpers: beam meshes, loads, and a thin C-ABI mesh wrapper."""
+import ctypes
+import hashlib
+import os
+
+import numpy as np
+
+from opentissue_gb300 import capi
+from opentissue_gb300.fem import generate_blocks
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+GRAVITY = -9.81
+MATERIAL = (5e5, 0.33, 1000.0, 1e30, 0.0, 0.0)
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def beam(I, J, K, jitter_seed=None, jitter=0.01, edge=0.1):
+    """Block beam with the x = 0 face (grid index i == 0) fixed."""
+    tets, coord = generate_blocks(I, J, K, edge, edge, edge)
+    if jitter_seed is not None:
+        rng = np.random.default_rng(jitter_seed)
+        coord = coord + rng.uniform(-jitter, jitter, coord.shape)
+    fixed = (np.arange(coord.shape[0]) < (J + 1) * (K + 1)).astype(np.uint8)
+    return tets, coord, fixed
+
+
+def gravity_force(mass, fixed):
+    f = np.zeros((mass.shape[0], 3))
+    free = fixed == 0
+    f[free, 1] = GRAVITY * mass[free]
+    return f
+
+
+def step_hash(x, v):
+    return hashlib.sha256(np.ascontiguousarray(x).tobytes() + np.ascontiguousarray(v).tobytes()).hexdigest()
+
+
+class GpuMesh:
+    """A mesh on the GPU driven directly through the C ABI."""
+
+    def __init__(self, tets, coord, fixed=None, model_coord=None, stream=None):
+        self.lib = capi.lib()
+        self.tets = np.ascontiguousarray(tets, np.int32)
+        self.coord = np.ascontiguousarray(coord, np.float64)
+        self.model = self.coord if model_coord is None else np.ascontiguousarray(model_coord, np.float64)
+        self.N, self.T = self.coord.shape[0], self.tets.shape[0]
+        self.fixed = np.zeros(self.N, np.uint8) if fixed is None else np.ascontiguousarray(fixed, np.uint8)
+        desc = capi.MeshDesc(self.N, self.T, self.tets.ctypes.data_as(_i32p), self.coord.ctypes.data_as(_dp),
+                             self.model.ctypes.data_as(_dp), self.fixed.ctypes.data_as(_u8p))
+        self.h = ctypes.c_void_p()
+        capi.check(self.lib.otfem_create(ctypes.byref(desc), stream, ctypes.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.lib.otfem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, material=MATERIAL):
+        capi.check(self.lib.otfem_init(self.h, *material))
+
+    def set(self, field, arr):
+        a = np.ascontiguousarray(arr, np.float64).reshape(-1)
+        capi.check(self.lib.otfem_set_nodes(self.h, field, a.ctypes.data_as(_dp), a.size))
+
+    def get(self, field):
+        out = np.zeros(self.N if field == capi.MASS else (self.N, 3))
+        capi.check(self.lib.otfem_get_nodes(self.h, field, out.ctypes.data_as(_dp), out.size))
+        return out
+
+    def step(self, dt=0.01, warp=True, params=None, check=True):
+        st = capi.StepStats()
+        p = params if params is not None else capi.default_params()
+        rc = self.lib.otfem_simulate_ex(self.h, dt, int(warp), ctypes.byref(p), ctypes.byref(st))
+        if check:
+            capi.check(rc)
+        return rc, st
+
+    def re(self):
+        out = np.zeros((self.T, 3, 3))
+        capi.check(self.lib.otfem_get_orientations(self.h, out.ctypes.data_as(_dp)))
+        return out
+
+    def plastic(self):
+        out = np.zeros((self.T, 6))
+        capi.check(self.lib.otfem_get_plastic(self.h, out.ctypes.data_as(_dp)))
+        return out
+
+    def k_pattern(self):
+        nnz = ctypes.c_int64()
+        capi.check(self.lib.otfem_k_pattern(self.h, ctypes.byref(nnz), None, None))
+        rp = np.zeros(self.N + 1, np.int32)
+        cols = np.zeros(max(nnz.value, 1), np.int32)
+        capi.check(self.lib.otfem_k_pattern(self.h, ctypes.byref(nnz), rp.ctypes.data_as(_i32p),
+                                            cols.ctypes.data_as(_i32p)))
+        return rp, cols[:nnz.value]
+
+    def k_values(self):
+        nnz = ctypes.c_int64()
+        capi.check(self.lib.otfem_k_pattern(self.h, ctypes.byref(nnz), None, None))
+        v = np.zeros((max(nnz.value, 1), 3, 3))
+        capi.check(self.lib.otfem_k_values(self.h, v.ctypes.data_as(_dp)))
+        return v[:nnz.value]
+
+    def export_k(self):
+        """export_K triplets in the reference's push order."""
+        nnz = ctypes.c_int64()
+        capi.check(self.lib.otfem_export_k_csr(self.h, ctypes.byref(nnz), None, None, None))
+        rp = np.zeros(self.N + 1, np.int32)
+        cols = np.zeros(max(nnz.value, 1), np.int32)
+        vals = np.zeros((max(nnz.value, 1), 3, 3))
+        capi.check(self.lib.otfem_export_k_csr(self.h, ctypes.byref(nnz), rp.ctypes.data_as(_i32p),
+                                               cols.ctypes.data_as(_i32p), vals.ctypes.data_as(_dp)))
+        rows, cs, vs = [], [], []
+        for i in range(self.N):
+            for r in range(3):
+                if self.fixed[i]:
+                    rows.append(3 * i + r)
+                    cs.append(3 * i + r)
+                    vs.append(1.0)
+                    continue
+                for q in range(rp[i], rp[i + 1]):
+                    for c in range(3):
+                        rows.append(3 * i + r)
+                        cs.append(3 * cols[q] + c)
+                        vs.append(vals[q, r, c])
+        return np.array(rows, np.int32), np.array(cs, np.int32), np.array(vs)
+
+
+def run_gpu(tets, coord, fixed, steps, params=None, material=MATERIAL, dt=0.01, warp=True, record=None):
+    """Runs `steps` gravity steps; returns (mesh, per-step list of (x, v, stats))."""
+    m = GpuMesh(tets, coord, fixed)
+    m.init(material)
+    mass = m.get(capi.MASS)
+    out = []
+    for s in range(1, steps + 1):
+        m.set(capi.F_EXTERNAL, gravity_force(mass, fixed))
+        _, st = m.step(dt, warp, params)
+        if record is None or s in record:
+            out.append((m.get(capi.COORD), m.get(capi.VELOCITY), st))
+        else:
+            out.append((None, None, st))
+    return m, out
+
+
+def run_oracle(po, tets, coord, fixed, steps, material=MATERIAL, dt=0.01, warp=True, converged=False,
+               rtol=1e-6):
+    m = po.OracleMesh(tets, coord, coord, fixed)
+    m.init(*material)
+    mass = m.get(po.MASS)
+    out = []
+    for _ in range(steps):
+        m.set(po.F_EXTERNAL, gravity_force(mass, fixed))
+        if converged:
+            it, rr = m.simulate_converged(dt, warp, 2.0, rtol, 100000)
+        else:
+            m.simulate(dt, warp)
+            it, rr = 20, None
+        out.append((m.get(po.COORD), m.get(po.VELOCITY), it, rr))
+    return m, out

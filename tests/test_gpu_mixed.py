@@ -1,0 +1,123 @@
+"""The matrix-free solver (FP32 element apply, FP64 CG) against the
+reference's relative-residual runs.  Tolerance from the target: position
+error below 1e-5 relative to the FP64 oracle, measured here against the
+largest displacement of the step (stricter than relative to the positions),
+true relative residual <= rtol = 1e-6."""
+import numpy as np
+import pytest
+
+from helpers import MATERIAL, GpuMesh, beam, golden, gravity_force, run_gpu, run_oracle
+from opentissue_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL = 1e-5
+
+
+def mixed(**kw):
+    base = dict(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6)
+    base.update(kw)
+    return capi.default_params(**base)
+
+
+def rel_pos_err(x, x_ref, x_init):
+    disp = np.abs(x_ref - x_init).max()
+    return np.abs(x - x_ref).max() / max(disp, 1e-300)
+
+
+def test_mixed_vs_reference_converged_golden(gpu):
+    g = golden("converged")
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 20, params=mixed())
+    for s in (1, 5, 20):
+        x, v, st = out[s - 1]
+        err = rel_pos_err(x, g[f"x_{s}"], g["coord"])
+        assert err < POS_TOL, (s, err)
+    for (_, _, st), it_ref in zip(out, g["iterations"]):
+        assert st.status == capi.OK
+        assert st.rel_residual <= 1e-6
+        assert abs(st.iterations - int(it_ref)) <= max(6, 0.2 * it_ref)
+
+
+def test_fp64_matrix_free_vs_reference(gpu):
+    g = golden("converged")
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 5, params=mixed(solver=capi.SOLVER_FP64))
+    x, v, st = out[4]
+    assert rel_pos_err(x, g["x_5"], g["coord"]) < 1e-7
+    assert st.rel_residual <= 1e-6
+
+
+def test_mixed_large_mesh_golden(gpu):
+    g = golden("large")
+    tets, coord, fixed = beam(int(g["I"]), int(g["J"]), int(g["K"]), jitter_seed=int(g["seed"]))
+    m, out = run_gpu(tets, coord, fixed, 3, params=mixed())
+    sample = g["sample"]
+    for s in (1, 2, 3):
+        x, v, st = out[s - 1]
+        err = rel_pos_err(x[sample], g[f"x_{s}"], coord[sample])
+        assert err < POS_TOL, (s, err)
+        assert st.rel_residual <= 1e-6 and st.status == capi.OK
+
+
+def test_mixed_plasticity_vs_oracle(gpu, oracle):
+    tets, coord, fixed = beam(10, 4, 4, jitter_seed=4)
+    mat = (5e5, 0.33, 1000.0, 1e-4, 50.0, 1e-2)
+    _, out = run_gpu(tets, coord, fixed, 15, params=mixed(rtol=1e-9), material=mat)
+    _, ref = run_oracle(oracle, tets, coord, fixed, 15, material=mat, converged=True, rtol=1e-9)
+    for s in (1, 15):
+        assert rel_pos_err(out[s - 1][0], ref[s - 1][0], coord) < POS_TOL
+
+
+def test_rigid_translation_is_force_free(gpu):
+    tets, coord, _ = beam(6, 3, 3, jitter_seed=2)
+    fixed = np.zeros(coord.shape[0], np.uint8)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    v0 = np.tile([0.3, -0.2, 0.1], (coord.shape[0], 1))
+    m.set(capi.VELOCITY, v0)
+    m.set(capi.F_EXTERNAL, np.zeros_like(v0))
+    _, st = m.step(0.01, True, mixed())
+    v = m.get(capi.VELOCITY)
+    assert np.abs(v - v0).max() < 1e-6
+    assert np.abs(m.get(capi.COORD) - (coord + 0.01 * v)).max() < 1e-12
+
+
+def test_nonfinite_force_reports_error_and_context_recovers(gpu):
+    tets, coord, fixed = beam(4, 2, 2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    f = gravity_force(m.get(capi.MASS), fixed)
+    bad = f.copy()
+    bad[-1, 0] = np.nan
+    m.set(capi.F_EXTERNAL, bad)
+    rc, st = m.step(0.01, True, mixed(), check=False)
+    assert rc == capi.ERR_NONFINITE
+    # the context stays usable: reset the state and step again
+    m.set(capi.COORD, coord)
+    m.set(capi.VELOCITY, np.zeros_like(coord))
+    m.set(capi.F_EXTERNAL, f)
+    rc, st = m.step(0.01, True, mixed())
+    assert rc == capi.OK and st.rel_residual <= 1e-6
+
+
+def test_iteration_cap_is_a_warning(gpu):
+    tets, coord, fixed = beam(8, 3, 3, jitter_seed=1)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
+    rc, st = m.step(0.01, True, mixed(max_iterations=3), check=False)
+    assert rc == capi.WARN_NOT_CONVERGED and st.iterations == 3
+
+
+def test_mixed_deterministic_setup_state(gpu):
+    # orientations of the matrix-free path follow the reference Gram-Schmidt
+    tets, coord, fixed = beam(5, 3, 3, jitter_seed=8)
+    a = GpuMesh(tets, coord, fixed)
+    a.init()
+    b = GpuMesh(tets, coord, fixed)
+    b.init()
+    f = gravity_force(a.get(capi.MASS), fixed)
+    for m in (a, b):
+        m.set(capi.F_EXTERNAL, f)
+    a.step(0.01, True, mixed())
+    b.step(0.01, True, capi.default_params(**{"sequential_dots": 0}))
+    assert np.abs(a.re() - b.re()).max() < 1e-14

@@ -1,0 +1,136 @@
+"""The reference solver (OTFEM_SOLVER_REFERENCE) on the GPU against the
+reference's own outputs (golden fixtures) and the C oracle: bit-identical
+with sequential dot products, within 1e-10 with the parallel tree."""
+import numpy as np
+import pytest
+
+from helpers import MATERIAL, GpuMesh, beam, golden, gravity_force, run_gpu, run_oracle, step_hash
+from opentissue_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+SEQ = dict(sequential_dots=1)
+
+
+def _params(**kw):
+    return capi.default_params(**kw)
+
+
+def test_k_pattern_built_on_gpu_equals_reference_keys(gpu):
+    g = golden("config1")
+    m = GpuMesh(g["tets"], g["coord"], g["fixed"])
+    rp, cols = m.k_pattern()
+    assert np.array_equal(rp, g["k_row_ptr"]) and np.array_equal(cols, g["k_cols"])
+    g2 = golden("converged")  # jittered 16x6x6: same topology rules, bigger
+    m2 = GpuMesh(g2["tets"], g2["coord"], g2["fixed"])
+    rp2, cols2 = m2.k_pattern()
+    assert np.array_equal(rp2, g2["k_row_ptr"]) and np.array_equal(cols2, g2["k_cols"])
+
+
+def test_config1_bitwise_100_steps(gpu):
+    g = golden("config1")
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 100, params=_params(**SEQ))
+    hashes = [step_hash(x, v) for x, v, _ in out]
+    assert hashes == list(g["hashes"])
+    assert all(st.iterations == 20 for _, _, st in out)
+
+
+def test_config1_tree_reductions_close(gpu):
+    g = golden("config1")
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 100, params=_params(), record=(1, 10, 50, 100))
+    for s in (1, 10, 50, 100):
+        x, v, _ = out[s - 1]
+        assert np.abs(x - g[f"x_{s}"]).max() <= 1e-10
+        assert np.abs(v - g[f"v_{s}"]).max() <= 1e-8
+
+
+def test_step1_state_bitwise(gpu):
+    g = golden("config1")
+    m = GpuMesh(g["tets"], g["coord"], g["fixed"])
+    m.init()
+    assert np.array_equal(m.get(capi.MASS), g["mass"])
+    r, c, v = m.export_k()  # before any step only fixed rows export (empty K_row maps)
+    assert len(v) == 3 * int(g["fixed"].sum()) and np.all(v == 1.0)
+    m.set(capi.F_EXTERNAL, gravity_force(g["mass"], g["fixed"]))
+    m.step(0.01, True, _params(**SEQ))
+    assert np.array_equal(m.re(), g["re_1"])
+    assert np.array_equal(m.k_values(), g["k_values_1"])
+    assert np.array_equal(m.get(capi.F0), g["f0_1"])
+    assert np.array_equal(m.get(capi.B), g["b_1"])
+    r, c, v = m.export_k()
+    assert np.array_equal(r, g["export_rows_1"]) and np.array_equal(c, g["export_cols_1"])
+    assert np.array_equal(v, g["export_vals_1"])
+
+
+def test_plasticity_bitwise(gpu):
+    g = golden("plastic")
+    mat = (5e5, 0.33, 1000.0, 1e-4, 50.0, 1e-2)
+    m, out = run_gpu(g["tets"], g["coord"], g["fixed"], 30, params=_params(**SEQ), material=mat)
+    assert [step_hash(x, v) for x, v, _ in out] == list(g["hashes"])
+    assert np.array_equal(m.plastic(), g["plastic_final"])
+
+
+def test_no_warping_bitwise(gpu):
+    g = golden("nowarp")
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 10, params=_params(**SEQ), warp=False)
+    assert [step_hash(x, v) for x, v, _ in out] == list(g["hashes"])
+
+
+def test_graph_replay_equals_direct_launch(gpu):
+    tets, coord, fixed = beam(6, 3, 3, jitter_seed=3)
+    _, a = run_gpu(tets, coord, fixed, 5, params=_params(graph=1, **SEQ))
+    _, b = run_gpu(tets, coord, fixed, 5, params=_params(graph=0, **SEQ))
+    for (xa, va, _), (xb, vb, _) in zip(a, b):
+        assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+def test_update_original_coord_matches_oracle(gpu, oracle):
+    tets, coord, fixed = beam(5, 3, 2, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*MATERIAL)
+    mass = o.get(oracle.MASS)
+    for s in range(6):
+        f = gravity_force(mass, fixed)
+        m.set(capi.F_EXTERNAL, f)
+        o.set(oracle.F_EXTERNAL, f)
+        m.step(0.01, True, _params(**SEQ))
+        o.simulate(0.01, True)
+        if s == 2:
+            capi.check(m.lib.otfem_update_original_coord(m.h))
+            o.update_original_coord()
+    assert np.array_equal(m.get(capi.COORD), o.get(oracle.COORD))
+    assert np.array_equal(m.get(capi.MODEL_COORD), o.get(oracle.MODEL_COORD))
+
+
+@pytest.mark.parametrize("case", ["single_tet", "isolated_nodes", "all_fixed", "no_fixed_random"])
+def test_edge_meshes_bitwise(gpu, oracle, case):
+    rng = np.random.default_rng(5)
+    if case == "single_tet":
+        tets = np.array([[0, 1, 2, 3]], np.int32)
+        coord = np.array([[0, 0, 0], [0.1, 0, 0], [0, 0.1, 0], [0, 0, 0.1]], float)
+        fixed = np.array([1, 0, 0, 0], np.uint8)
+    elif case == "isolated_nodes":
+        tets, coord, fixed = beam(3, 2, 2)
+        coord = np.vstack([coord, rng.uniform(0, 1, (5, 3))])  # nodes in no tet
+        fixed = np.concatenate([fixed, np.zeros(5, np.uint8)])
+    elif case == "all_fixed":
+        tets, coord, fixed = beam(3, 2, 2)
+        fixed = np.ones(coord.shape[0], np.uint8)
+    else:
+        tets, coord, _ = beam(4, 3, 3, jitter_seed=9)
+        fixed = np.zeros(coord.shape[0], np.uint8)
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*MATERIAL)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    assert np.array_equal(m.get(capi.MASS), o.get(oracle.MASS))
+    for _ in range(4):
+        f = rng.normal(0, 5, (coord.shape[0], 3))
+        m.set(capi.F_EXTERNAL, f)
+        o.set(oracle.F_EXTERNAL, f)
+        m.step(0.01, True, _params(**SEQ))
+        o.simulate(0.01, True)
+    assert np.array_equal(m.get(capi.COORD), o.get(oracle.COORD))
+    assert np.array_equal(m.get(capi.VELOCITY), o.get(oracle.VELOCITY))
