@@ -95,6 +95,8 @@ typedef struct otfem_step_stats {
   double rel_residual;      /* ||b - A v|| / ||b|| over free rows at exit (matrix-free) */
   double initial_rel_residual; /* same for the initial guess */
   double bnorm;             /* ||b|| over free rows */
+  int applies;              /* element-apply sweeps of the step (initial residual,
+                               one per iteration, one per residual refresh) */
 } otfem_step_stats;
 
 typedef struct otfem_mesh_desc {
@@ -117,7 +119,7 @@ OTFEM_API int otfem_abi_version(void);
 
 /* Creates the device-resident mesh (replaces building fem::Mesh, fem_mesh.h:21-34,
  * over t4mesh::T4Mesh, t4mesh.h:48-55).  stream: a cudaStream_t (NULL = the
- * legacy default stream).  Builds the node->tet incidence and the K_row
+ * library creates and owns a stream).  Builds the node->tet incidence and the K_row
  * sparsity pattern on the GPU.  The fixed flags must be final before otfem_init
  * (compute_mass reads them, fem_compute_mass.h:154-160). */
 OTFEM_API int otfem_create(const otfem_mesh_desc* desc, void* stream, otfem_handle* out);
@@ -144,6 +146,13 @@ OTFEM_API int otfem_simulate(otfem_handle h, double time_step, int use_stiffness
  * filled after a stream synchronisation. */
 OTFEM_API int otfem_simulate_ex(otfem_handle h, double time_step, int use_stiffness_warping,
                       const otfem_solver_params* params, otfem_step_stats* stats);
+/* The two kernels of a matrix-free step enqueued separately (same result as
+ * otfem_simulate_ex when ORIENT is followed by SOLVE), so a caller can time
+ * them or insert work between them.  ORIENT: orientation, element forces and
+ * plasticity; SOLVE: right-hand side, CG and position update. */
+enum { OTFEM_PHASE_ORIENT = 1, OTFEM_PHASE_SOLVE = 2 };
+OTFEM_API int otfem_simulate_phase(otfem_handle h, double time_step, int use_stiffness_warping,
+                                   const otfem_solver_params* params, int phase);
 /* Reads the statistics of the last step (synchronises the stream). */
 OTFEM_API int otfem_last_stats(otfem_handle h, otfem_step_stats* stats);
 OTFEM_API int otfem_synchronize(otfem_handle h);
@@ -169,7 +178,22 @@ OTFEM_API int otfem_get_orientations(otfem_handle h, double* host_re);
 OTFEM_API int otfem_get_plastic(otfem_handle h, double* host_plastic);
 OTFEM_API int otfem_get_volumes(otfem_handle h, double* host_volume);
 
+/* ---- host staging (no counterpart in the reference) ---------------------- */
+/* Page-locked host memory for fast transfers (used by the drop-in headers). */
+OTFEM_API int otfem_host_alloc(size_t bytes, void** ptr);
+OTFEM_API int otfem_host_free(void* ptr);
+
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* y = A x for the matrix-free operator A = M(1 + dt*mass_damping) + dt^2 K'
+ * (solver OTFEM_SOLVER_MIXED: FP32 element apply, OTFEM_SOLVER_FP64: FP64),
+ * using the orientations of the last matrix-free step or ORIENT phase.
+ * x, y: host, 3 doubles per node; rows of fixed nodes are returned as 0. */
+OTFEM_API int otfem_apply_operator(otfem_handle h, int solver, double dt, double mass_damping, const double* x,
+                                   double* y);
+/* Convergence history of the last matrix-free step: per CG iteration the
+ * squared residual norm before the iteration, p.Ap, alpha and beta (4 doubles
+ * per row, at most 256 rows). */
+OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* Number of kernels this handle has enqueued so far (graph replays included). */
 OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);
 /* Launch shape of the persistent CG kernel (grid CTAs, threads per CTA). */

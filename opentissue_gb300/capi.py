@@ -26,6 +26,7 @@ COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B = range(7)
 # solvers
 SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
 WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
+PHASE_ORIENT, PHASE_SOLVE = 1, 2
 
 
 class SolverParams(ctypes.Structure):
@@ -49,6 +50,7 @@ class StepStats(ctypes.Structure):
         ("rel_residual", ctypes.c_double),
         ("initial_rel_residual", ctypes.c_double),
         ("bnorm", ctypes.c_double),
+        ("applies", ctypes.c_int),
     ]
 
 
@@ -95,6 +97,8 @@ SIGNATURES = {
     "otfem_simulate": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int]),
     "otfem_simulate_ex": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverParams),
                                          ctypes.POINTER(StepStats)]),
+    "otfem_simulate_phase": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverParams),
+                                            ctypes.c_int]),
     "otfem_last_stats": (ctypes.c_int, [_h, ctypes.POINTER(StepStats)]),
     "otfem_synchronize": (ctypes.c_int, [_h]),
     "otfem_update_original_coord": (ctypes.c_int, [_h]),
@@ -104,6 +108,10 @@ SIGNATURES = {
     "otfem_get_orientations": (ctypes.c_int, [_h, _dp]),
     "otfem_get_plastic": (ctypes.c_int, [_h, _dp]),
     "otfem_get_volumes": (ctypes.c_int, [_h, _dp]),
+    "otfem_apply_operator": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp]),
+    "otfem_solver_trace": (ctypes.c_int, [_h, _dp, ctypes.c_int32, _i32p]),
+    "otfem_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "otfem_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),
     "otfem_solver_shape": (ctypes.c_int, [_h, _i32p, _i32p]),
 }

@@ -47,11 +47,12 @@ void free_all(Context& c) {
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f,
                   c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.q_d,
-                  c.p_d4, c.v_d4, c.partials, c.sync, c.stats};
+                  c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c.stats_host) cudaFreeHost(c.stats_host);
   if (c.graph) cudaGraphExecDestroy(c.graph);
+  if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
 }
 
 double* node_field(Context& c, int field) {
@@ -97,7 +98,8 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
       return e;
     if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
   } else {
-    if ((e = otfem::launch_mixed_step(c, dt, warp, p)) != cudaSuccess) return e;
+    if ((e = otfem::launch_mixed_orient(c, dt, warp)) != cudaSuccess) return e;
+    if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return e;
   }
   return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
 }
@@ -169,6 +171,12 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
 #define OT_ALLOC(ptr, n) \
   if ((e = dalloc(&(ptr), (n))) != cudaSuccess) return bail(e, "cudaMalloc " #ptr);
   if ((e = cudaGetDevice(&c.device)) != cudaSuccess) return bail(e, "cudaGetDevice");
+  if (!c.stream) {
+    // A stream of our own: the legacy default stream cannot be captured into
+    // the step graph.  It synchronises with the legacy default stream.
+    if ((e = cudaStreamCreate(&c.stream)) != cudaSuccess) return bail(e, "cudaStreamCreate");
+    c.own_stream = true;
+  }
   if ((e = cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device)) != cudaSuccess)
     return bail(e, "cudaDeviceGetAttribute");
   OT_ALLOC(c.tets, T);
@@ -216,6 +224,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.p_d4, N);
   OT_ALLOC(c.v_d4, N);
   OT_ALLOC(c.sync, 1);
+  OT_ALLOC(c.trace, 4 * size_t(otfem::kTraceRows));
   OT_ALLOC(c.stats, 1);
   if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
@@ -395,12 +404,39 @@ int otfem_simulate_ex(otfem_handle h, double dt, int warp, const otfem_solver_pa
 
 int otfem_simulate(otfem_handle h, double dt, int warp) { return otfem_simulate_ex(h, dt, warp, nullptr, nullptr); }
 
+int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver_params* params, int phase) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (!(dt > 0.0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "time step must be positive");
+  otfem_solver_params p;
+  if (params) p = *params;
+  else otfem_default_params(&p);
+  int rc = check_params(p);
+  if (rc != OTFEM_OK) return rc;
+  if (p.solver == OTFEM_SOLVER_REFERENCE) return fail(OTFEM_ERR_UNSUPPORTED, "phases exist for the matrix-free solvers");
+  cudaError_t e;
+  if (phase == OTFEM_PHASE_ORIENT) {
+    if ((e = otfem::launch_mixed_orient(c, dt, warp != 0)) != cudaSuccess) return cuda_fail(e, "orient phase");
+    c.launches += 1 + (c.plastic_active ? 2 : 0);
+  } else if (phase == OTFEM_PHASE_SOLVE) {
+    if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return cuda_fail(e, "solve phase");
+    OT_CUDA(cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream));
+    c.launches += 1;
+    c.last_solver = p.solver;
+  } else {
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown phase");
+  }
+  return OTFEM_OK;
+}
+
 int otfem_last_stats(otfem_handle h, otfem_step_stats* s) {
   if (!h || !s) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   Context& c = h->c;
   OT_CUDA(cudaStreamSynchronize(c.stream));
   const otfem::DeviceStats& d = *c.stats_host;
   s->iterations = d.iterations;
+  s->applies = d.applies;
   s->status = d.status;
   s->bnorm = d.bb > 0 ? sqrt(d.bb) : 0.0;
   double ref = d.bb > 0 ? d.bb : 1.0;
@@ -497,6 +533,53 @@ static int get_tet_array(otfem_handle h, const double* src, size_t per, double* 
 int otfem_get_orientations(otfem_handle h, double* re) { return get_tet_array(h, h ? h->c.Re : nullptr, 9, re); }
 int otfem_get_plastic(otfem_handle h, double* pl) { return get_tet_array(h, h ? h->c.plastic : nullptr, 6, pl); }
 int otfem_get_volumes(otfem_handle h, double* vol) { return get_tet_array(h, h ? h->c.V : nullptr, 1, vol); }
+
+int otfem_apply_operator(otfem_handle h, int solver, double dt, double mass_damping, const double* x,
+                         double* y) {
+  if (!h || !x || !y) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (solver != OTFEM_SOLVER_MIXED && solver != OTFEM_SOLVER_FP64)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "solver must be OTFEM_SOLVER_MIXED or OTFEM_SOLVER_FP64");
+  size_t bytes = sizeof(double) * 3 * size_t(c.N);
+  double *dx = nullptr, *dy = nullptr;
+  OT_CUDA(dalloc(&dx, 3 * size_t(c.N)));
+  cudaError_t e = dalloc(&dy, 3 * size_t(c.N));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) e = otfem::launch_apply_operator(c, solver, dt, mass_damping, dx, dy);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  cudaFree(dx);
+  if (dy) cudaFree(dy);
+  if (e != cudaSuccess) return cuda_fail(e, "apply operator");
+  c.launches += 3;
+  return OTFEM_OK;
+}
+
+int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows) {
+  if (!h || !rows || (!out && max_rows > 0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  int n = c.stats_host->iterations;
+  if (n > otfem::kTraceRows) n = otfem::kTraceRows;
+  if (n > max_rows) n = max_rows;
+  if (n > 0) OT_CUDA(cudaMemcpy(out, c.trace, sizeof(double) * 4 * size_t(n), cudaMemcpyDeviceToHost));
+  *rows = n;
+  return OTFEM_OK;
+}
+
+int otfem_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *ptr = nullptr;
+  cudaError_t e = cudaMallocHost(ptr, bytes > 0 ? bytes : 1);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocHost");
+  return OTFEM_OK;
+}
+
+int otfem_host_free(void* ptr) {
+  if (ptr) OT_CUDA(cudaFreeHost(ptr));
+  return OTFEM_OK;
+}
 
 int otfem_launch_count(otfem_handle h, int64_t* n) {
   if (!h || !n) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");

@@ -484,6 +484,7 @@ __global__ void k_cg_direction(int N, const unsigned char* __restrict__ fixed, c
 
 __global__ void k_cg_stats(const RefCG* __restrict__ s, DeviceStats* st) {
   st->iterations = s->it;
+  st->applies = s->it + 1;
   st->status = 0;
   st->rr = 0.0;
   st->rr0 = 0.0;

@@ -13,6 +13,8 @@ namespace otfem {
 
 // Per-CTA partial sums written before a grid barrier (one slot per scalar).
 constexpr int kMaxPartials = 8;
+// Rows of the per-iteration CG trace (rho, p.q, alpha, beta) kept per step.
+constexpr int kTraceRows = 256;
 
 // Counters for the bounded grid barrier and the device status word.
 struct DeviceSync {
@@ -26,6 +28,8 @@ struct DeviceSync {
 struct DeviceStats {
   int iterations;
   int status;
+  int applies;     // element-apply sweeps (initial residual, iterations, refreshes)
+  int pad;
   double rr;       // squared residual norm at exit (free rows)
   double rr0;      // squared residual of the initial guess
   double bb;       // squared norm of b (free rows)
@@ -39,6 +43,7 @@ struct Context {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  bool own_stream = false;            // stream created by otfem_create
   int N = 0, T = 0;
   bool initialized = false;
   bool k_assembled = false;
@@ -82,6 +87,7 @@ struct Context {
   double4 *p_d4 = nullptr, *v_d4 = nullptr;               // N (FP64 apply operands)
   double* partials = nullptr;                              // kMaxPartials * max grid
   DeviceSync* sync = nullptr;
+  double* trace = nullptr;                                 // kTraceRows x 4 CG scalars
   DeviceStats* stats = nullptr;
   DeviceStats* stats_host = nullptr;  // pinned
   int mf_grid = 0, mf_block = 0;      // persistent CG launch shape
@@ -112,7 +118,11 @@ cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
 
 // ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
 cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
-cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solver_params& p);
+cudaError_t launch_mixed_orient(Context& c, double dt, bool warp);
+cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& p);
+// y = A x with the matrix-free apply of the given precision and the current
+// orientations (x, y: device, 3 doubles per node; rows of fixed nodes = 0).
+cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x, double* y);
 int mixed_grid_shape(Context& c, int* grid, int* block);
 
 }  // namespace otfem

@@ -67,6 +67,7 @@ struct MixedArgs {
   double* partials;
   DeviceSync* sync;
   DeviceStats* stats;
+  double* trace;  // kTraceRows x 4: rho, p.q, alpha, beta per iteration
   long long spin_limit;
 };
 
@@ -93,12 +94,15 @@ __device__ __forceinline__ void red_add(double4* q, double a, double b, double c
   atomicAdd(&q->z, c);
 }
 
-// Grid barrier with a bounded wait.  Thread 0 of each CTA arrives on a
-// counter; the last arrival resets it and advances the generation.  Returns
-// false on every thread of the CTA if the wait timed out or any CTA has set
-// an error status.
+// Grid barrier with a bounded wait.  Every thread first fences its own
+// writes and posted reductions at GPU scope (a fence only covers the issuing
+// thread's operations); then thread 0 of each CTA arrives on a counter, and
+// the last arrival resets it and advances the generation.  Returns false on
+// every thread of the CTA if the wait timed out or any CTA has set an error
+// status.
 __device__ bool grid_barrier(DeviceSync* s, long long spin_limit) {
   __shared__ int ok;
+  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     int good = 1;
@@ -130,9 +134,14 @@ __device__ bool grid_barrier(DeviceSync* s, long long spin_limit) {
 
 // Sums NV per-thread values over the whole grid in a fixed order (warp
 // shuffles, CTA tree, then CTA partials in index order), so every CTA obtains
-// bit-identical results.  Includes a grid barrier.
+// bit-identical results.  Includes a grid barrier.  Consecutive calls use
+// alternating halves of the partials array (`parity`, flipped on every call):
+// a CTA may start writing the next sum's partial while slower CTAs are still
+// reading this sum's, and the barrier inside the next call separates the
+// reads of call k from the writes of call k + 2.
 template <int NV>
-__device__ bool grid_sum(const MixedArgs& a, double (&val)[NV]) {
+__device__ bool grid_sum(const MixedArgs& a, double (&val)[NV], int& parity) {
+  static_assert(2 * NV <= kMaxPartials, "partials too small");
   __shared__ double s_warp[kBlock / 32][NV];
   __shared__ double s_out[NV];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -150,7 +159,7 @@ __device__ bool grid_sum(const MixedArgs& a, double (&val)[NV]) {
       double x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : 0.0;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) a.partials[k * gridDim.x + blockIdx.x] = x;
+      if (lane == 0) a.partials[(parity * (kMaxPartials / 2) + k) * gridDim.x + blockIdx.x] = x;
     }
   }
   if (!grid_barrier(a.sync, a.spin_limit)) return false;
@@ -158,7 +167,8 @@ __device__ bool grid_sum(const MixedArgs& a, double (&val)[NV]) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
       double x = 0.0;
-      for (int b = lane; b < (int)gridDim.x; b += 32) x += __ldcg(a.partials + k * gridDim.x + b);
+      for (int b = lane; b < (int)gridDim.x; b += 32)
+        x += __ldcg(a.partials + (parity * (kMaxPartials / 2) + k) * gridDim.x + b);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if (lane == 0) s_out[k] = x;
@@ -168,7 +178,17 @@ __device__ bool grid_sum(const MixedArgs& a, double (&val)[NV]) {
 #pragma unroll
   for (int k = 0; k < NV; ++k) val[k] = s_out[k];
   __syncthreads();
+  parity ^= 1;
   return true;
+}
+
+// Coherent (L2) load of node data written by other CTAs within the launch
+// (accumulators filled by their atomics, operands they rewrote).
+__device__ __forceinline__ float4 load_acc(const float4* p) { return __ldcg(p); }
+__device__ __forceinline__ double4 load_acc(const double4* p) {
+  double2 lo = __ldcg(reinterpret_cast<const double2*>(p));
+  double2 hi = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+  return make_double4(lo.x, lo.y, hi.x, hi.y);
 }
 
 template <typename R>
@@ -225,15 +245,19 @@ __device__ __forceinline__ void element_apply(const R* Re, const R* b, R c0, R c
 }
 
 // q += dt^2 K' u over the tets of this thread (grid-stride).  Contributions to
-// nodes whose operand w == 0 (fixed rows, never read) are skipped.
+// nodes whose operand w == 0 (fixed rows, never read) are skipped.  The
+// operand u4 is rewritten by other CTAs between sweeps of the same launch, so
+// it is read with L2 loads (no read-only or L1 path); the per-tet data is
+// constant during the launch and may use the read-only path.
 template <typename R>
-__device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* __restrict__ u4,
+__device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                            typename ApplyOps<R>::V4* q4, const R* __restrict__ re,
                            const R* __restrict__ bb, const R* __restrict__ cc, R scale) {
   const int T = a.T;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
     int4 n = a.tets[t];
-    typename ApplyOps<R>::V4 w[4] = {u4[n.x], u4[n.y], u4[n.z], u4[n.w]};
+    typename ApplyOps<R>::V4 w[4] = {load_acc(u4 + n.x), load_acc(u4 + n.y), load_acc(u4 + n.z),
+                                     load_acc(u4 + n.w)};
     R Re[9], b[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
@@ -282,6 +306,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
   const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
   const R scale = R(a.dt * a.dt);
   const V4 zero4 = make_v4<V4, double>(0.0, 0.0, 0.0, 0.0);
+  int parity = 0;  // alternates the halves of a.partials between grid sums
 
   // Phase 0: b = M v + dt (f_ext - g) with g gathered in ascending tet order;
   // diagonal M(1 + dt*alpha) as in fem_dynamics_assembly.h:84-85.
@@ -313,7 +338,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     vv[i] = make_v4<V4, double>(vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     qv[i] = zero4;
   }
-  if (!grid_sum<1>(a, bbsum)) return;
+  if (!grid_sum<1>(a, bbsum, parity)) return;
   const double bnorm2 = bbsum[0];
   const double thresh = a.rtol * a.rtol * bnorm2;
 
@@ -327,7 +352,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
       for (int c = 0; c < 3; ++c) a.p[3 * i + c] = 0.0, a.r[3 * i + c] = 0.0;
       continue;
     }
-    V4 q4 = qv[i];
+    V4 q4 = load_acc(qv + i);
     double qa[3] = {double(q4.x), double(q4.y), double(q4.z)};
     double d = a.diag[i];
     double ri[3];
@@ -337,22 +362,23 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     qv[i] = zero4;
     rr[0] += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
   }
-  if (!grid_sum<1>(a, rr)) return;
+  if (!grid_sum<1>(a, rr, parity)) return;
   double rho = rr[0];
   const double rho0 = rho;
-  int it = 0;
+  int it = 0, applies = 1;
   bool converged = rho <= thresh;
   bool v_fresh = false;
 
   while (!converged && it < a.max_it) {
     // q += dt^2 K' p
     apply_tets<R>(a, pv, qv, re, bb, cc, scale);
+    ++applies;
     if (!grid_barrier(a.sync, a.spin_limit)) return;
     // q = diag p + q; p.q, r.q, q.q
     double s3[3] = {0.0, 0.0, 0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
-      V4 q4 = qv[i];
+      V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
       double qi[3] = {d * a.p[3 * i] + double(q4.x), d * a.p[3 * i + 1] + double(q4.y),
                       d * a.p[3 * i + 2] + double(q4.z)};
@@ -362,7 +388,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         s3[2] += qi[c] * qi[c];
       }
     }
-    if (!grid_sum<3>(a, s3)) return;
+    if (!grid_sum<3>(a, s3, parity)) return;
     const double pq = s3[0];
     const double alpha = rho / pq;
     // ||r - alpha q||^2 from the three sums: the new beta is known before the
@@ -374,12 +400,18 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
       break;
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && it < kTraceRows) {
+      a.trace[4 * it + 0] = rho;
+      a.trace[4 * it + 1] = pq;
+      a.trace[4 * it + 2] = alpha;
+      a.trace[4 * it + 3] = beta;
+    }
     ++it;
     const bool want_refresh = (a.refresh > 0 && it % a.refresh == 0) || rho_est <= 4.0 * thresh;
     double rn[1] = {0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
-      V4 q4 = qv[i];
+      V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
       double pn[3], vn[3];
       for (int c = 0; c < 3; ++c) {
@@ -398,7 +430,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
       if (want_refresh) vv[i] = make_v4<V4, double>(vn[0], vn[1], vn[2], 1.0);
     }
     v_fresh = want_refresh;
-    if (!grid_sum<1>(a, rn)) return;
+    if (!grid_sum<1>(a, rn, parity)) return;
     rho = rn[0];
     bool refresh = (a.refresh > 0 && it % a.refresh == 0) || rho <= thresh;
     if (refresh) {
@@ -409,11 +441,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
       }
       // r = b - A v (residual replacement); q is zero here.
       apply_tets<R>(a, vv, qv, re, bb, cc, scale);
+      ++applies;
       if (!grid_barrier(a.sync, a.spin_limit)) return;
       double tr[1] = {0.0};
       for (long i = gtid; i < N; i += gstride) {
         if (a.fixed[i]) continue;
-        V4 q4 = qv[i];
+        V4 q4 = load_acc(qv + i);
         double d = a.diag[i];
         double qa[3] = {double(q4.x), double(q4.y), double(q4.z)};
         for (int c = 0; c < 3; ++c) {
@@ -423,7 +456,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         }
         qv[i] = zero4;
       }
-      if (!grid_sum<1>(a, tr)) return;
+      if (!grid_sum<1>(a, tr, parity)) return;
       rho = tr[0];
     }
     converged = rho <= thresh;
@@ -438,6 +471,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     int st = ld_status(&a.sync->status);
     if (st == 0 && !converged) st = OTFEM_WARN_NOT_CONVERGED;
     a.stats->iterations = it;
+    a.stats->applies = applies;
     a.stats->status = st;
     a.stats->rr = rho;
     a.stats->rr0 = rho0;
@@ -520,6 +554,43 @@ __global__ void k_prepare(int T, const double* __restrict__ Bv, const double* __
   }
 }
 
+// Standalone y = A x (diagnostics and the apply-only roofline measurement):
+// pack, one element-apply sweep, finalize.
+template <typename V4>
+__global__ void k_pack_operand(int N, const unsigned char* __restrict__ fixed, const double* __restrict__ x,
+                               V4* u, V4* q) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  u[i] = make_v4<V4, double>(x[3 * i], x[3 * i + 1], x[3 * i + 2], fixed[i] ? 0.0 : 1.0);
+  q[i] = make_v4<V4, double>(0.0, 0.0, 0.0, 0.0);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kBlock, 2) k_apply_sweep(MixedArgs a, const typename ApplyOps<R>::V4* u,
+                                                           typename ApplyOps<R>::V4* q) {
+  const R* re = sizeof(R) == 4 ? (const R*)a.re_f : (const R*)a.re_d;
+  const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
+  const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
+  apply_tets<R>(a, u, q, re, bb, cc, R(a.dt * a.dt));
+}
+
+template <typename V4>
+__global__ void k_finalize_operand(int N, const unsigned char* __restrict__ fixed, const double* __restrict__ mass,
+                                   double dt, double alpha, const double* __restrict__ x, const V4* q, double* y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  if (fixed[i]) {
+    y[3 * i] = y[3 * i + 1] = y[3 * i + 2] = 0.0;
+    return;
+  }
+  double m = mass[i];
+  double d = m + dt * (alpha * m);
+  V4 qq = q[i];
+  y[3 * i] = d * x[3 * i] + double(qq.x);
+  y[3 * i + 1] = d * x[3 * i + 1] + double(qq.y);
+  y[3 * i + 2] = d * x[3 * i + 2] + double(qq.z);
+}
+
 template <typename R>
 const void* cg_kernel() {
   return reinterpret_cast<const void*>(&k_cg_persistent<R>);
@@ -546,7 +617,7 @@ cudaError_t mixed_prepare(Context& c) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solver_params& prm) {
+cudaError_t launch_mixed_orient(Context& c, double dt, bool warp) {
   int nb = (c.T + 255) / 256;
   if (nb < 1) nb = 1;
   k_orient_rhs<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.E, c.V, c.Bv, c.D, c.Re,
@@ -554,9 +625,14 @@ cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solv
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   // add_plasticity_force (fem_simulate.h:102) runs between the assembly and
-  // the right-hand side, as in the reference; it is a no-op when creep and
-  // max are zero for every tet, which the host detects at init.
+  // the right-hand side, as in the reference; it only changes f_ext when
+  // creep and max are both positive, which the host records at init.
   if (c.plastic_active && (e = launch_plasticity(c, dt)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& prm) {
+  cudaError_t e;
   if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
   MixedArgs a;
   a.N = c.N;
@@ -594,6 +670,7 @@ cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solv
   a.partials = c.partials;
   a.sync = c.sync;
   a.stats = c.stats;
+  a.trace = c.trace;
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
   void* args[] = {&a};
   cudaLaunchConfig_t cfg = {};
@@ -608,6 +685,32 @@ cudaError_t launch_mixed_step(Context& c, double dt, bool warp, const otfem_solv
   cfg.numAttrs = 1;
   const void* fn = prm.solver == OTFEM_SOLVER_FP64 ? cg_kernel<double>() : cg_kernel<float>();
   return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x,
+                                  double* y) {
+  MixedArgs a = {};
+  a.N = c.N;
+  a.T = c.T;
+  a.tets = c.tets;
+  a.re_f = c.re_f;
+  a.b_f = c.b_f;
+  a.c_f = c.c_f;
+  a.re_d = c.re_d;
+  a.b_d = c.b_d;
+  a.c_d = c.c_d;
+  a.dt = dt;
+  int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
+  if (solver == OTFEM_SOLVER_FP64) {
+    k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, c.q_d);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_d4, c.q_d);
+    k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_d, y);
+  } else {
+    k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_f, c.q_f);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_f, c.q_f);
+    k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_f, y);
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace otfem
