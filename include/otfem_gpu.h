@@ -190,9 +190,17 @@ OTFEM_API int otfem_host_free(void* ptr);
  * x, y: host, 3 doubles per node; rows of fixed nodes are returned as 0. */
 OTFEM_API int otfem_apply_operator(otfem_handle h, int solver, double dt, double mass_damping, const double* x,
                                    double* y);
-/* Convergence history of the last matrix-free step: per CG iteration the
- * squared residual norm before the iteration, p.Ap, alpha and beta (4 doubles
- * per row, at most 256 rows). */
+/* Enqueues `sweeps` element-apply sweeps q += dt^2 K' p on the resident
+ * search direction of the last matrix-free step, asynchronously on the
+ * handle's stream: the stiffness apply alone, for timing.  Leaves the solver
+ * state unspecified until the next step. */
+OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t sweeps);
+/* Convergence history of the last matrix-free step, one row of 10 doubles per
+ * CG iteration (at most 256 rows): the squared residual norm before the
+ * iteration, p.Ap, alpha, beta, then six GPU-timer stamps in ns since the
+ * kernel started (taken by the first CTA): apply sweep done, its barrier
+ * passed, reduction phase done, reduction complete, update phase done,
+ * update reduction complete. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* Number of kernels this handle has enqueued so far (graph replays included). */
 OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);

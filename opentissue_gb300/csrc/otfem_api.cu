@@ -46,7 +46,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -220,11 +220,13 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.p_f, N);
   OT_ALLOC(c.v_f, N);
   OT_ALLOC(c.q_f, N);
+  OT_ALLOC(c.p_lo, N);
+  OT_ALLOC(c.v_lo, N);
   OT_ALLOC(c.q_d, N);
   OT_ALLOC(c.p_d4, N);
   OT_ALLOC(c.v_d4, N);
   OT_ALLOC(c.sync, 1);
-  OT_ALLOC(c.trace, 4 * size_t(otfem::kTraceRows));
+  OT_ALLOC(c.trace, size_t(otfem::kTraceCols) * otfem::kTraceRows);
   OT_ALLOC(c.stats, 1);
   if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
@@ -556,6 +558,18 @@ int otfem_apply_operator(otfem_handle h, int solver, double dt, double mass_damp
   return OTFEM_OK;
 }
 
+int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t sweeps) {
+  if (!h || sweeps < 0) return fail(OTFEM_ERR_INVALID_ARGUMENT, "bad argument");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (solver != OTFEM_SOLVER_MIXED && solver != OTFEM_SOLVER_FP64)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "solver must be OTFEM_SOLVER_MIXED or OTFEM_SOLVER_FP64");
+  cudaError_t e = otfem::launch_apply_sweeps(c, solver, dt, sweeps);
+  if (e != cudaSuccess) return cuda_fail(e, "apply sweeps");
+  c.launches += sweeps;
+  return OTFEM_OK;
+}
+
 int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows) {
   if (!h || !rows || (!out && max_rows > 0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   Context& c = h->c;
@@ -563,7 +577,8 @@ int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* r
   int n = c.stats_host->iterations;
   if (n > otfem::kTraceRows) n = otfem::kTraceRows;
   if (n > max_rows) n = max_rows;
-  if (n > 0) OT_CUDA(cudaMemcpy(out, c.trace, sizeof(double) * 4 * size_t(n), cudaMemcpyDeviceToHost));
+  if (n > 0)
+    OT_CUDA(cudaMemcpy(out, c.trace, sizeof(double) * otfem::kTraceCols * size_t(n), cudaMemcpyDeviceToHost));
   *rows = n;
   return OTFEM_OK;
 }

@@ -13,8 +13,13 @@ namespace otfem {
 
 // Per-CTA partial sums written before a grid barrier (one slot per scalar).
 constexpr int kMaxPartials = 8;
-// Rows of the per-iteration CG trace (rho, p.q, alpha, beta) kept per step.
+// Rows of the per-iteration CG trace kept per step.  Each row holds
+// kTraceCols doubles: rho, p.q, alpha, beta, then GPU-timer stamps (ns since
+// the kernel started, taken on CTA 0) after the apply sweep, after its
+// barrier, after the reduction phase, after its grid sum, after the update
+// phase and after its grid sum.
 constexpr int kTraceRows = 256;
+constexpr int kTraceCols = 10;
 
 // Counters for the bounded grid barrier and the device status word.
 struct DeviceSync {
@@ -82,12 +87,13 @@ struct Context {
   double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
   double* diag = nullptr;                                 // N: m(1+dt*alpha)
   double *r = nullptr, *p = nullptr, *bvec = nullptr;    // 3N
-  float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N
+  float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N (p_f/v_f: high part, w = free flag)
+  float4 *p_lo = nullptr, *v_lo = nullptr;                // N: low parts, x - double(float(x))
   double4* q_d = nullptr;                                  // N (FP64 apply accumulator)
   double4 *p_d4 = nullptr, *v_d4 = nullptr;               // N (FP64 apply operands)
   double* partials = nullptr;                              // kMaxPartials * max grid
   DeviceSync* sync = nullptr;
-  double* trace = nullptr;                                 // kTraceRows x 4 CG scalars
+  double* trace = nullptr;                                 // kTraceRows x kTraceCols
   DeviceStats* stats = nullptr;
   DeviceStats* stats_host = nullptr;  // pinned
   int mf_grid = 0, mf_block = 0;      // persistent CG launch shape
@@ -123,6 +129,9 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
 // y = A x with the matrix-free apply of the given precision and the current
 // orientations (x, y: device, 3 doubles per node; rows of fixed nodes = 0).
 cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x, double* y);
+// `sweeps` element-apply sweeps on the resident operand (no host transfer):
+// the apply kernel alone, for timing.
+cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps);
 int mixed_grid_shape(Context& c, int* grid, int* block);
 
 }  // namespace otfem

@@ -23,6 +23,15 @@
 // with b_k the B-vectors of fem_compute_b.h and (c0, c1, c2) = V (D0 - D1, D1, D2)
 // from fem_compute_isotropic_elasticity.h.  b_0 = -(b_1 + b_2 + b_3) is
 // implied, so a rigid translation gives exactly zero force.
+//
+// FP32 operands are stored as (hi, lo) float pairs, hi = float(x) and
+// lo = float(x - hi), and the element apply forms u_k - u_0 as
+// (hi_k - hi_0) + (lo_k - lo_0).  The stiffness sees only these tet-local
+// differences, which for a translating or swinging body are orders of
+// magnitude smaller than |u|: a single float(x) would keep ~1e-7 of |u| and
+// lose most digits of the differences, capping the attainable residual near
+// 1e-6.  The hi difference is exact for nearby values (Sterbenz), so the
+// differences keep full FP32 relative precision without FP64 arithmetic.
 #include <cfloat>
 
 #include "otfem_internal.h"
@@ -55,6 +64,8 @@ struct MixedArgs {
   float4* p_f;
   float4* v_f;
   float4* q_f;
+  float4* p_lo;
+  float4* v_lo;
   // FP64 apply
   const double* re_d;
   const double* b_d;
@@ -67,7 +78,7 @@ struct MixedArgs {
   double* partials;
   DeviceSync* sync;
   DeviceStats* stats;
-  double* trace;  // kTraceRows x 4: rho, p.q, alpha, beta per iteration
+  double* trace;  // kTraceRows x kTraceCols (see otfem_internal.h)
   long long spin_limit;
 };
 
@@ -75,6 +86,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
 __device__ __forceinline__ int ld_status(const int* p) {
@@ -205,12 +222,7 @@ struct ApplyOps<double> {
 // One element apply (see the file comment).  u: operands of the 4 nodes.
 template <typename R>
 __device__ __forceinline__ void element_apply(const R* Re, const R* b, R c0, R c1, R c2, R scale,
-                                              const R (&u)[4][3], R (&f)[4][3]) {
-  R du[3][3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-#pragma unroll
-    for (int a = 0; a < 3; ++a) du[k][a] = u[k + 1][a] - u[0][a];
+                                              const R (&du)[3][3], R (&f)[4][3]) {
   R G[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -244,6 +256,47 @@ __device__ __forceinline__ void element_apply(const R* Re, const R* b, R c0, R c
   for (int a = 0; a < 3; ++a) f[0][a] = -(f[1][a] + f[2][a] + f[3][a]);
 }
 
+// u_k - u_0 (k = 1..3) of one tet from the gathered operands.
+template <typename R>
+__device__ __forceinline__ void local_differences(const typename ApplyOps<R>::V4 (&w)[4],
+                                                  const typename ApplyOps<R>::V4* ulo, int4 n, R (&du)[3][3]);
+template <>
+__device__ __forceinline__ void local_differences<float>(const float4 (&w)[4], const float4* ulo, int4 n,
+                                                         float (&du)[3][3]) {
+  float4 l0 = load_acc(ulo + n.x), l1 = load_acc(ulo + n.y), l2 = load_acc(ulo + n.z), l3 = load_acc(ulo + n.w);
+  du[0][0] = (w[1].x - w[0].x) + (l1.x - l0.x);
+  du[0][1] = (w[1].y - w[0].y) + (l1.y - l0.y);
+  du[0][2] = (w[1].z - w[0].z) + (l1.z - l0.z);
+  du[1][0] = (w[2].x - w[0].x) + (l2.x - l0.x);
+  du[1][1] = (w[2].y - w[0].y) + (l2.y - l0.y);
+  du[1][2] = (w[2].z - w[0].z) + (l2.z - l0.z);
+  du[2][0] = (w[3].x - w[0].x) + (l3.x - l0.x);
+  du[2][1] = (w[3].y - w[0].y) + (l3.y - l0.y);
+  du[2][2] = (w[3].z - w[0].z) + (l3.z - l0.z);
+}
+template <>
+__device__ __forceinline__ void local_differences<double>(const double4 (&w)[4], const double4*, int4,
+                                                          double (&du)[3][3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    du[k][0] = w[k + 1].x - w[0].x;
+    du[k][1] = w[k + 1].y - w[0].y;
+    du[k][2] = w[k + 1].z - w[0].z;
+  }
+}
+
+// Stores operand x (and its free flag in w) for the apply: FP32 as (hi, lo).
+__device__ __forceinline__ void store_operand(float4* hi, float4* lo, long i, double x, double y, double z,
+                                              double w) {
+  float hx = float(x), hy = float(y), hz = float(z);
+  hi[i] = make_float4(hx, hy, hz, float(w));
+  lo[i] = make_float4(float(x - double(hx)), float(y - double(hy)), float(z - double(hz)), 0.0f);
+}
+__device__ __forceinline__ void store_operand(double4* hi, double4*, long i, double x, double y, double z,
+                                              double w) {
+  hi[i] = make_double4(x, y, z, w);
+}
+
 // q += dt^2 K' u over the tets of this thread (grid-stride).  Contributions to
 // nodes whose operand w == 0 (fixed rows, never read) are skipped.  The
 // operand u4 is rewritten by other CTAs between sweeps of the same launch, so
@@ -251,8 +304,9 @@ __device__ __forceinline__ void element_apply(const R* Re, const R* b, R c0, R c
 // constant during the launch and may use the read-only path.
 template <typename R>
 __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
-                           typename ApplyOps<R>::V4* q4, const R* __restrict__ re,
-                           const R* __restrict__ bb, const R* __restrict__ cc, R scale) {
+                           const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
+                           const R* __restrict__ re, const R* __restrict__ bb, const R* __restrict__ cc,
+                           R scale) {
   const int T = a.T;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
     int4 n = a.tets[t];
@@ -265,14 +319,9 @@ __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u
       b[k] = bb[(long)k * T + t];
     }
     R c0 = cc[t], c1 = cc[T + t], c2 = cc[2L * T + t];
-    R u[4][3], f[4][3];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      u[k][0] = w[k].x;
-      u[k][1] = w[k].y;
-      u[k][2] = w[k].z;
-    }
-    element_apply<R>(Re, b, c0, c1, c2, scale, u, f);
+    R du[3][3], f[4][3];
+    local_differences<R>(w, ulo, n, du);
+    element_apply<R>(Re, b, c0, c1, c2, scale, du, f);
     int nn[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -300,6 +349,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   V4* pv = sizeof(R) == 4 ? (V4*)a.p_f : (V4*)a.p_d;
   V4* vv = sizeof(R) == 4 ? (V4*)a.v_f : (V4*)a.v_d;
+  V4* plo = sizeof(R) == 4 ? (V4*)a.p_lo : nullptr;
+  V4* vlo = sizeof(R) == 4 ? (V4*)a.v_lo : nullptr;
   V4* qv = sizeof(R) == 4 ? (V4*)a.q_f : (V4*)a.q_d;
   const R* re = sizeof(R) == 4 ? (const R*)a.re_f : (const R*)a.re_d;
   const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
@@ -307,6 +358,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
   const R scale = R(a.dt * a.dt);
   const V4 zero4 = make_v4<V4, double>(0.0, 0.0, 0.0, 0.0);
   int parity = 0;  // alternates the halves of a.partials between grid sums
+  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const unsigned long long t_start = tracer ? global_ns() : 0ull;
+  double stamp[6] = {0, 0, 0, 0, 0, 0};
 
   // Phase 0: b = M v + dt (f_ext - g) with g gathered in ascending tet order;
   // diagonal M(1 + dt*alpha) as in fem_dynamics_assembly.h:84-85.
@@ -335,7 +389,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
     // never accumulated (w = 0).
-    vv[i] = make_v4<V4, double>(vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+    store_operand(vv, vlo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     qv[i] = zero4;
   }
   if (!grid_sum<1>(a, bbsum, parity)) return;
@@ -343,12 +397,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
   const double thresh = a.rtol * a.rtol * bnorm2;
 
   // Initial residual r = b - A v, p = r.
-  apply_tets<R>(a, vv, qv, re, bb, cc, scale);
+  apply_tets<R>(a, vv, vlo, qv, re, bb, cc, scale);
   if (!grid_barrier(a.sync, a.spin_limit)) return;
   double rr[1] = {0.0};
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) {
-      pv[i] = zero4;
+      store_operand(pv, plo, i, 0.0, 0.0, 0.0, 0.0);
       for (int c = 0; c < 3; ++c) a.p[3 * i + c] = 0.0, a.r[3 * i + c] = 0.0;
       continue;
     }
@@ -358,7 +412,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     double ri[3];
     for (int c = 0; c < 3; ++c) ri[c] = a.bvec[3 * i + c] - (d * a.v[3 * i + c] + qa[c]);
     for (int c = 0; c < 3; ++c) a.r[3 * i + c] = ri[c], a.p[3 * i + c] = ri[c];
-    pv[i] = make_v4<V4, double>(ri[0], ri[1], ri[2], 1.0);
+    store_operand(pv, plo, i, ri[0], ri[1], ri[2], 1.0);
     qv[i] = zero4;
     rr[0] += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
   }
@@ -371,9 +425,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
 
   while (!converged && it < a.max_it) {
     // q += dt^2 K' p
-    apply_tets<R>(a, pv, qv, re, bb, cc, scale);
+    apply_tets<R>(a, pv, plo, qv, re, bb, cc, scale);
     ++applies;
+    if (tracer) stamp[0] = double(global_ns() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit)) return;
+    if (tracer) stamp[1] = double(global_ns() - t_start);
     // q = diag p + q; p.q, r.q, q.q
     double s3[3] = {0.0, 0.0, 0.0};
     for (long i = gtid; i < N; i += gstride) {
@@ -388,7 +444,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         s3[2] += qi[c] * qi[c];
       }
     }
+    if (tracer) stamp[2] = double(global_ns() - t_start);
     if (!grid_sum<3>(a, s3, parity)) return;
+    if (tracer) stamp[3] = double(global_ns() - t_start);
     const double pq = s3[0];
     const double alpha = rho / pq;
     // ||r - alpha q||^2 from the three sums: the new beta is known before the
@@ -396,16 +454,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     double rho_est = rho - 2.0 * alpha * s3[1] + alpha * alpha * s3[2];
     if (rho_est < 0.0) rho_est = 0.0;
     const double beta = rho_est / rho;
-    if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) {
+    if (!isfinite(pq) || !isfinite(rho) || !isfinite(s3[1]) || !isfinite(s3[2])) {
+      // NaN/Inf in the system (e.g. a non-finite force): an error
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
       break;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && it < kTraceRows) {
-      a.trace[4 * it + 0] = rho;
-      a.trace[4 * it + 1] = pq;
-      a.trace[4 * it + 2] = alpha;
-      a.trace[4 * it + 3] = beta;
-    }
+    // finite breakdown (p.Ap <= 0 from rounding at the precision floor):
+    // stop; the step reports OTFEM_WARN_NOT_CONVERGED with its residual
+    if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) break;
+    const int row = it;
     ++it;
     const bool want_refresh = (a.refresh > 0 && it % a.refresh == 0) || rho_est <= 4.0 * thresh;
     double rn[1] = {0.0};
@@ -425,22 +482,32 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         pn[c] = ri + beta * pi;
         a.p[3 * i + c] = pn[c];
       }
-      pv[i] = make_v4<V4, double>(pn[0], pn[1], pn[2], 1.0);
+      store_operand(pv, plo, i, pn[0], pn[1], pn[2], 1.0);
       qv[i] = zero4;
-      if (want_refresh) vv[i] = make_v4<V4, double>(vn[0], vn[1], vn[2], 1.0);
+      if (want_refresh) store_operand(vv, vlo, i, vn[0], vn[1], vn[2], 1.0);
     }
     v_fresh = want_refresh;
+    if (tracer) stamp[4] = double(global_ns() - t_start);
     if (!grid_sum<1>(a, rn, parity)) return;
+    if (tracer && row < kTraceRows) {
+      double* tr = a.trace + kTraceCols * row;
+      tr[0] = rho;
+      tr[1] = pq;
+      tr[2] = alpha;
+      tr[3] = beta;
+      for (int k = 0; k < 5; ++k) tr[4 + k] = stamp[k];
+      tr[9] = double(global_ns() - t_start);
+    }
     rho = rn[0];
     bool refresh = (a.refresh > 0 && it % a.refresh == 0) || rho <= thresh;
     if (refresh) {
       if (!v_fresh) {
         for (long i = gtid; i < N; i += gstride)
-          if (!a.fixed[i]) vv[i] = make_v4<V4, double>(a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2], 1.0);
+          if (!a.fixed[i]) store_operand(vv, vlo, i, a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2], 1.0);
         if (!grid_barrier(a.sync, a.spin_limit)) return;
       }
       // r = b - A v (residual replacement); q is zero here.
-      apply_tets<R>(a, vv, qv, re, bb, cc, scale);
+      apply_tets<R>(a, vv, vlo, qv, re, bb, cc, scale);
       ++applies;
       if (!grid_barrier(a.sync, a.spin_limit)) return;
       double tr[1] = {0.0};
@@ -558,20 +625,21 @@ __global__ void k_prepare(int T, const double* __restrict__ Bv, const double* __
 // pack, one element-apply sweep, finalize.
 template <typename V4>
 __global__ void k_pack_operand(int N, const unsigned char* __restrict__ fixed, const double* __restrict__ x,
-                               V4* u, V4* q) {
+                               V4* u, V4* ulo, V4* q) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  u[i] = make_v4<V4, double>(x[3 * i], x[3 * i + 1], x[3 * i + 2], fixed[i] ? 0.0 : 1.0);
+  store_operand(u, ulo, i, x[3 * i], x[3 * i + 1], x[3 * i + 2], fixed[i] ? 0.0 : 1.0);
   q[i] = make_v4<V4, double>(0.0, 0.0, 0.0, 0.0);
 }
 
 template <typename R>
 __global__ void __launch_bounds__(kBlock, 2) k_apply_sweep(MixedArgs a, const typename ApplyOps<R>::V4* u,
+                                                           const typename ApplyOps<R>::V4* ulo,
                                                            typename ApplyOps<R>::V4* q) {
   const R* re = sizeof(R) == 4 ? (const R*)a.re_f : (const R*)a.re_d;
   const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
   const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
-  apply_tets<R>(a, u, q, re, bb, cc, R(a.dt * a.dt));
+  apply_tets<R>(a, u, ulo, q, re, bb, cc, R(a.dt * a.dt));
 }
 
 template <typename V4>
@@ -656,6 +724,8 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   a.p_f = c.p_f;
   a.v_f = c.v_f;
   a.q_f = c.q_f;
+  a.p_lo = c.p_lo;
+  a.v_lo = c.v_lo;
   a.re_d = c.re_d;
   a.b_d = c.b_d;
   a.c_d = c.c_d;
@@ -687,6 +757,27 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
+cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps) {
+  MixedArgs a = {};
+  a.N = c.N;
+  a.T = c.T;
+  a.tets = c.tets;
+  a.re_f = c.re_f;
+  a.b_f = c.b_f;
+  a.c_f = c.c_f;
+  a.re_d = c.re_d;
+  a.b_d = c.b_d;
+  a.c_d = c.c_d;
+  a.dt = dt;
+  for (int k = 0; k < sweeps; ++k) {
+    if (solver == OTFEM_SOLVER_FP64)
+      k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
+    else
+      k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.p_f, c.p_lo, c.q_f);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x,
                                   double* y) {
   MixedArgs a = {};
@@ -702,12 +793,12 @@ cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass
   a.dt = dt;
   int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   if (solver == OTFEM_SOLVER_FP64) {
-    k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, c.q_d);
-    k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_d4, c.q_d);
+    k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, nullptr, c.q_d);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_d4, nullptr, c.q_d);
     k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_d, y);
   } else {
-    k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_f, c.q_f);
-    k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_f, c.q_f);
+    k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_f, c.v_lo, c.q_f);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_f, c.v_lo, c.q_f);
     k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_f, y);
   }
   return cudaGetLastError();

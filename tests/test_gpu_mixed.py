@@ -61,10 +61,15 @@ def test_mixed_large_mesh_golden(gpu):
 def test_mixed_plasticity_vs_oracle(gpu, oracle):
     tets, coord, fixed = beam(10, 4, 4, jitter_seed=4)
     mat = (5e5, 0.33, 1000.0, 1e-4, 50.0, 1e-2)
-    _, out = run_gpu(tets, coord, fixed, 15, params=mixed(rtol=1e-9), material=mat)
-    _, ref = run_oracle(oracle, tets, coord, fixed, 15, material=mat, converged=True, rtol=1e-9)
+    m, out = run_gpu(tets, coord, fixed, 15, params=mixed(), material=mat)
+    _, ref = run_oracle(oracle, tets, coord, fixed, 15, material=mat, converged=True, rtol=1e-6)
     for s in (1, 15):
         assert rel_pos_err(out[s - 1][0], ref[s - 1][0], coord) < POS_TOL
+    assert np.abs(m.plastic()).max() > 0
+    # the FP64 matrix-free solver reaches the tight tolerance as well
+    _, out64 = run_gpu(tets, coord, fixed, 15, params=mixed(solver=capi.SOLVER_FP64, rtol=1e-10), material=mat)
+    _, ref64 = run_oracle(oracle, tets, coord, fixed, 15, material=mat, converged=True, rtol=1e-10)
+    assert rel_pos_err(out64[-1][0], ref64[-1][0], coord) < 1e-8
 
 
 def test_rigid_translation_is_force_free(gpu):
