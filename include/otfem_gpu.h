@@ -202,6 +202,13 @@ OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t 
  * passed, reduction phase done, reduction complete, update phase done,
  * update reduction complete. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
+/* The element-apply variant the autotuner chose for this mesh at otfem_init
+ * (0: patches with shared-memory atomics, 1: patches with a deterministic
+ * per-node gather, 2: one tet per thread with global reductions) and the
+ * measured time of one sweep of each (ms, 3 doubles; may be NULL). */
+OTFEM_API int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_variant);
+/* Forces an element-apply variant (0..2) for the following steps. */
+OTFEM_API int otfem_set_apply_variant(otfem_handle h, int32_t variant);
 /* Number of kernels this handle has enqueued so far (graph replays included). */
 OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);
 /* Launch shape of the persistent CG kernel (grid CTAs, threads per CTA). */

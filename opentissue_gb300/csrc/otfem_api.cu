@@ -44,10 +44,11 @@ cudaError_t dalloc(T** p, size_t count) {
 void free_all(Context& c) {
   void* ptrs[] = {c.tets, c.x, c.x0, c.v, c.fext, c.mass, c.f0, c.b, c.fixed, c.prev, c.update,
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
-                  c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.inc_ptr,
+                  c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.q_d,
-                  c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats};
+                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.q_d,
+                  c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
+                  c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c.stats_host) cudaFreeHost(c.stats_host);
@@ -98,7 +99,7 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
       return e;
     if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
   } else {
-    if ((e = otfem::launch_mixed_orient(c, dt, warp)) != cudaSuccess) return e;
+    if ((e = otfem::launch_mixed_orient(c, dt, warp, p.solver)) != cudaSuccess) return e;
     if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return e;
   }
   return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
@@ -207,6 +208,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.creep, T);
   OT_ALLOC(c.cmax, T);
   OT_ALLOC(c.tet_force, 12 * T);
+  OT_ALLOC(c.elastic_force, 12 * T);
   OT_ALLOC(c.re_f, 9 * T);
   OT_ALLOC(c.b_f, 9 * T);
   OT_ALLOC(c.c_f, 3 * T);
@@ -222,6 +224,8 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.q_f, N);
   OT_ALLOC(c.p_lo, N);
   OT_ALLOC(c.v_lo, N);
+  OT_ALLOC(c.r_f, N);
+  OT_ALLOC(c.g_f, 4 * T);
   OT_ALLOC(c.q_d, N);
   OT_ALLOC(c.p_d4, N);
   OT_ALLOC(c.v_d4, N);
@@ -231,6 +235,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
   memset(c.stats_host, 0, sizeof(otfem::DeviceStats));
+  if ((e = otfem::build_patches(c, d->tets)) != cudaSuccess) return bail(e, "build_patches");
   otfem::mixed_grid_shape(c, &c.mf_grid, &c.mf_block);
   OT_ALLOC(c.partials, size_t(otfem::kMaxPartials) * c.mf_grid);
 
@@ -307,6 +312,8 @@ int otfem_init(otfem_handle h, double young, double poisson, double density, dou
   // clear_stiffness_assembly (fem_init.h:60)
   OT_CUDA(cudaMemsetAsync(c.f0, 0, sizeof(double) * 3 * size_t(c.N), c.stream));
   if (c.k_assembled) OT_CUDA(cudaMemsetAsync(c.K, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream));
+  // choose the element-apply variant for this mesh
+  if ((e = otfem::autotune_apply(c)) != cudaSuccess) return cuda_fail(e, "autotune");
   std::vector<double> vol(size_t(c.T));
   if (c.T) OT_CUDA(cudaMemcpyAsync(vol.data(), c.V, sizeof(double) * c.T, cudaMemcpyDeviceToHost, c.stream));
   OT_CUDA(cudaStreamSynchronize(c.stream));
@@ -419,7 +426,7 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
   if (p.solver == OTFEM_SOLVER_REFERENCE) return fail(OTFEM_ERR_UNSUPPORTED, "phases exist for the matrix-free solvers");
   cudaError_t e;
   if (phase == OTFEM_PHASE_ORIENT) {
-    if ((e = otfem::launch_mixed_orient(c, dt, warp != 0)) != cudaSuccess) return cuda_fail(e, "orient phase");
+    if ((e = otfem::launch_mixed_orient(c, dt, warp != 0, p.solver)) != cudaSuccess) return cuda_fail(e, "orient phase");
     c.launches += 1 + (c.plastic_active ? 2 : 0);
   } else if (phase == OTFEM_PHASE_SOLVE) {
     if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return cuda_fail(e, "solve phase");
@@ -532,7 +539,13 @@ static int get_tet_array(otfem_handle h, const double* src, size_t per, double* 
   return OTFEM_OK;
 }
 
-int otfem_get_orientations(otfem_handle h, double* re) { return get_tet_array(h, h ? h->c.Re : nullptr, 9, re); }
+int otfem_get_orientations(otfem_handle h, double* re) {
+  if (h) {
+    cudaError_t e = otfem::sync_orientations(h->c);
+    if (e != cudaSuccess) return cuda_fail(e, "orientations");
+  }
+  return get_tet_array(h, h ? h->c.Re : nullptr, 9, re);
+}
 int otfem_get_plastic(otfem_handle h, double* pl) { return get_tet_array(h, h ? h->c.plastic : nullptr, 6, pl); }
 int otfem_get_volumes(otfem_handle h, double* vol) { return get_tet_array(h, h ? h->c.V : nullptr, 1, vol); }
 
@@ -580,6 +593,26 @@ int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* r
   if (n > 0)
     OT_CUDA(cudaMemcpy(out, c.trace, sizeof(double) * otfem::kTraceCols * size_t(n), cudaMemcpyDeviceToHost));
   *rows = n;
+  return OTFEM_OK;
+}
+
+int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_variant) {
+  if (!h || !variant) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  *variant = h->c.apply_variant;
+  if (ms_per_variant)
+    for (int v = 0; v < otfem::kNumApplyVariants; ++v) ms_per_variant[v] = h->c.apply_ms[v];
+  return OTFEM_OK;
+}
+
+int otfem_set_apply_variant(otfem_handle h, int32_t variant) {
+  if (!h || variant < 0 || variant >= otfem::kNumApplyVariants) return fail(OTFEM_ERR_INVALID_ARGUMENT, "bad variant");
+  Context& c = h->c;
+  c.apply_variant = variant;
+  if (c.graph) {
+    cudaGraphExecDestroy(c.graph);
+    c.graph = nullptr;
+    c.graph_key.clear();
+  }
   return OTFEM_OK;
 }
 

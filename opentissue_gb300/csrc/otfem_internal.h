@@ -14,19 +14,24 @@ namespace otfem {
 // Per-CTA partial sums written before a grid barrier (one slot per scalar).
 constexpr int kMaxPartials = 8;
 // Rows of the per-iteration CG trace kept per step.  Each row holds
-// kTraceCols doubles: rho, p.q, alpha, beta, then GPU-timer stamps (ns since
-// the kernel started, taken on CTA 0) after the apply sweep, after its
+// kTraceCols doubles: rho, p.q, alpha, beta, then SM-clock stamps (cycles
+// since the kernel started, taken on CTA 0) after the apply sweep, after its
 // barrier, after the reduction phase, after its grid sum, after the update
 // phase and after its grid sum.
 constexpr int kTraceRows = 256;
 constexpr int kTraceCols = 10;
 
-// Counters for the bounded grid barrier and the device status word.
+// Counters for the bounded grid barrier and the device status word.  Each
+// word sits on its own 128-byte line: arrivals (atomics on `count`) do not
+// contend with the CTAs polling `gen`.
 struct DeviceSync {
-  unsigned int count;    // CTAs arrived at the current barrier
-  unsigned int gen;      // barrier generation
-  int status;            // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
-  int pad;
+  unsigned int count;        // monotonic arrival counter
+  unsigned int pad0[31];
+  unsigned int gen;          // number of completed barriers (written by the last arrival)
+  unsigned int pad1[31];
+  int status;                // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
+  int pad2[31];
+  double result[2][4];       // grid-sum results, double-buffered by barrier parity
 };
 
 // Statistics written by the step kernels (device memory).
@@ -69,7 +74,8 @@ struct Context {
   double *Bv = nullptr, *D = nullptr, *plastic = nullptr;
   double *young = nullptr, *poisson = nullptr, *density = nullptr;
   double *yield = nullptr, *creep = nullptr, *cmax = nullptr;
-  double* tet_force = nullptr;  // 12*T scratch: per-tet node forces
+  double* tet_force = nullptr;      // 12*T scratch: per-tet plastic node forces
+  double* elastic_force = nullptr;  // 12*T: per-tet elastic node forces (matrix-free rhs)
 
   // node -> incident (tet, slot) lists, ascending tet index
   int* inc_ptr = nullptr;  // N+1
@@ -89,9 +95,24 @@ struct Context {
   double *r = nullptr, *p = nullptr, *bvec = nullptr;    // 3N
   float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N (p_f/v_f: high part, w = free flag)
   float4 *p_lo = nullptr, *v_lo = nullptr;                // N: low parts, x - double(float(x))
+  float4* r_f = nullptr;                                   // N: mixed-solver residual
+  float4* g_f = nullptr;                                   // 4T: mixed elastic node forces
+  bool re_f32_pending = false;  // the FP64 m_Re copy lags the FP32 orientations
   double4* q_d = nullptr;                                  // N (FP64 apply accumulator)
   double4 *p_d4 = nullptr, *v_d4 = nullptr;               // N (FP64 apply operands)
   double* partials = nullptr;                              // kMaxPartials * max grid
+  // patches: contiguous ranges of kPatchTets tets, each with its sorted set of
+  // nodes (bit 31 set when another patch touches the node too) and the tets'
+  // connectivity as patch-local 16-bit indices
+  int num_patches = 0, patch_max_nodes = 0;
+  int* patch_node_ptr = nullptr;  // num_patches + 1
+  int* patch_nodes = nullptr;
+  ushort4* lconn = nullptr;       // T
+  int* patch_inc_ptr = nullptr;   // per patch node (+1): offsets into patch_inc
+  unsigned short* patch_inc = nullptr;  // 4T entries (patch-local tet << 2) | slot
+  size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
+  int apply_variant = 0;          // element-apply variant chosen by the autotuner
+  double apply_ms[4] = {0, 0, 0, 0};  // measured time of one sweep per variant
   DeviceSync* sync = nullptr;
   double* trace = nullptr;                                 // kTraceRows x kTraceCols
   DeviceStats* stats = nullptr;
@@ -124,7 +145,15 @@ cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
 
 // ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
 cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
-cudaError_t launch_mixed_orient(Context& c, double dt, bool warp);
+// Builds the apply patches from the host connectivity (once per mesh).
+cudaError_t build_patches(Context& c, const int32_t* tets_host);
+cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver);
+// Times one element-apply sweep of every variant on this mesh and keeps the
+// fastest in c.apply_variant (synchronises the stream).
+cudaError_t autotune_apply(Context& c);
+constexpr int kNumApplyVariants = 3;
+// Writes m_Re (FP64) from the FP32 orientations of the last mixed step.
+cudaError_t sync_orientations(Context& c);
 cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& p);
 // y = A x with the matrix-free apply of the given precision and the current
 // orientations (x, y: device, 3 doubles per node; rows of fixed nodes = 0).

@@ -5,16 +5,14 @@
 //   b = M v + dt (f_ext - sum_e Re Ke (Re^T x - x0))   (fem_dynamics_assembly.h:79-91)
 // with Ke = V B^T D B in the B-form of fem_compute_ke.h:133-292.
 //
-// K1 k_orient_rhs   one thread per tet, FP64: Re by the reference's
-//                   Gram-Schmidt (fem_update_orientation.h), the elastic node
-//                   forces Re Ke (Re^T x - x0) of the tet, Re rounded to FP32.
-// K2 k_cg_persistent one cooperative launch per step: b, the initial residual,
-//                   all CG iterations with FP32 (or FP64) element apply,
-//                   FP64 vectors and reductions, residual replacement every
-//                   refresh_period iterations, and the position update
-//                   (fem_position_update.h).  CTAs meet at a bounded grid
-//                   barrier; a wait that exceeds its limit sets
-//                   OTFEM_ERR_TIMEOUT and the kernel returns.
+// Kernels of one step:
+//   K1 k_orient_rhs_f32 (mixed) / k_orient_rhs (FP64 solver), one thread per
+//      tet: Re by the reference's row Gram-Schmidt (fem_update_orientation.h,
+//      math_matrix3x3.h ortonormalize) and the elastic node forces
+//      Re Ke (Re^T x - x0) of the tet.
+//   K2 k_cg_mixed / k_cg_fp64: one cooperative persistent launch: b, the
+//      initial residual, all CG iterations, residual replacement every
+//      refresh_period iterations, the position update (fem_position_update.h).
 //
 // Element apply for a tet with nodes 0..3 and operand u (world frame):
 //   G = sum_{k=1..3} (u_k - u_0) (x) b_k,  H = Re^T G,
@@ -24,15 +22,27 @@
 // from fem_compute_isotropic_elasticity.h.  b_0 = -(b_1 + b_2 + b_3) is
 // implied, so a rigid translation gives exactly zero force.
 //
-// FP32 operands are stored as (hi, lo) float pairs, hi = float(x) and
-// lo = float(x - hi), and the element apply forms u_k - u_0 as
-// (hi_k - hi_0) + (lo_k - lo_0).  The stiffness sees only these tet-local
-// differences, which for a translating or swinging body are orders of
-// magnitude smaller than |u|: a single float(x) would keep ~1e-7 of |u| and
-// lose most digits of the differences, capping the attainable residual near
-// 1e-6.  The hi difference is exact for nearby values (Sterbenz), so the
-// differences keep full FP32 relative precision without FP64 arithmetic.
+// Precision of the mixed solver.  GB300 executes FP64 at ~1/64 of the FP32
+// rate, so FP64 is used only where cancellation needs it.
+//  * Element apply, search direction p, residual r: FP32.
+//  * Velocity v: a (hi, lo) float pair, updated with an exact two-sum, which
+//    is also the apply operand when the residual is recomputed.  The stiffness
+//    sees only tet-local differences u_k - u_0, which for a translating or
+//    swinging body are orders of magnitude smaller than |u|; they are formed
+//    as (hi_k - hi_0) + (lo_k - lo_0), exact for nearby values (Sterbenz), so
+//    they keep full FP32 relative precision.
+//  * Dot products: FP32 node terms accumulated as (hi, lo) float pairs
+//    (~48-bit mantissa, the accuracy of FP64 summation); alpha and beta in
+//    FP64, computed once per iteration by the last CTA of the grid sum.
+//  * b and the residual recompute b - A v: FP64 (once per step / every
+//    refresh_period iterations).
+//  * K1: FP32, except the FP64 edge differences of the FP64 coordinates.
+// The FP64 solver keeps every vector and reduction in FP64 (accuracy
+// reference).
+#include <algorithm>
 #include <cfloat>
+#include <type_traits>
+#include <vector>
 
 #include "otfem_internal.h"
 #include "otfem_refmath.cuh"
@@ -41,6 +51,16 @@ namespace otfem {
 namespace {
 
 constexpr int kBlock = 512;
+// Tets per apply patch: one tet per thread of a CTA.
+constexpr int kPatchTets = kBlock;
+// Element-apply variants, chosen per mesh by the autotuner at otfem_init.
+constexpr int kApplyAtomics = 0;  // patches, shared-memory atomic accumulation
+constexpr int kApplyGather = 1;   // patches, per-node gather over patch-local incidence (deterministic)
+constexpr int kApplyTets = 2;     // grid-stride over tets, global vector reductions
+constexpr int kApplyVariants = 3;
+// Largest persistent grid (CTAs): the last CTA of a grid sum loads one
+// partial per thread, so the grid may not exceed the CTA size.
+constexpr int kMaxGrid = kBlock;
 
 struct MixedArgs {
   int N, T;
@@ -48,7 +68,8 @@ struct MixedArgs {
   const unsigned char* fixed;
   const int* inc_ptr;
   const int* inc_ent;
-  const double* tet_force;  // 12 per tet: elastic node forces (K1)
+  const double* tet_force;  // FP64 solver: 12 per tet, elastic node forces (K1)
+  const float4* g_f;        // mixed: 4 per tet, elastic node forces (K1)
   const double* mass;
   const double* fext;
   double* x;
@@ -66,6 +87,7 @@ struct MixedArgs {
   float4* q_f;
   float4* p_lo;
   float4* v_lo;
+  float4* r_f;
   // FP64 apply
   const double* re_d;
   const double* b_d;
@@ -79,8 +101,18 @@ struct MixedArgs {
   DeviceSync* sync;
   DeviceStats* stats;
   double* trace;  // kTraceRows x kTraceCols (see otfem_internal.h)
+  int num_patches;
+  int patch_max_nodes_padded;
+  const int* patch_node_ptr;
+  const int* patch_nodes;
+  const ushort4* lconn;
+  const int* patch_inc_ptr;             // per patch node: offsets into patch_inc
+  const unsigned short* patch_inc;      // (patch-local tet << 2) | slot, ascending tet
+  int apply_variant;                    // kApplyAtomics / kApplyGather / kApplyTets
   long long spin_limit;
 };
+
+// ---- synchronisation ---------------------------------------------------
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -88,17 +120,15 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
 __device__ __forceinline__ int ld_status(const int* p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+
+// Stamps of the trace: SM clock cycles (the GPU timer's resolution is far
+// coarser than one CG phase).  All stamps come from the first CTA's SM.
+__device__ __forceinline__ long long cycles_now() { return clock64(); }
 
 __device__ __forceinline__ void red_add(float4* q, float a, float b, float c) {
   asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(q), "f"(a), "f"(b),
@@ -111,37 +141,53 @@ __device__ __forceinline__ void red_add(double4* q, double a, double b, double c
   atomicAdd(&q->z, c);
 }
 
-// Grid barrier with a bounded wait.  Every thread first fences its own
-// writes and posted reductions at GPU scope (a fence only covers the issuing
-// thread's operations); then thread 0 of each CTA arrives on a counter, and
-// the last arrival resets it and advances the generation.  Returns false on
-// every thread of the CTA if the wait timed out or any CTA has set an error
-// status.
-__device__ bool grid_barrier(DeviceSync* s, long long spin_limit) {
+// Grid barriers and grid reductions.  Every CTA passes the same sequence of
+// barriers, numbered 1, 2, ... (`round`).  Thread 0 of each CTA arrives on a
+// monotonic counter with an acq_rel atomic after a CTA barrier (by the PTX
+// memory model's causality order this publishes every write the CTA made
+// before the barrier); the CTA whose ticket completes round r (the last to
+// arrive) publishes r in `gen` with a release store, and the others wait for
+// it with acquire loads.  For a reduction the last CTA also adds up the
+// per-CTA partials in CTA order, derives the scalars the iteration needs and
+// publishes them before releasing, so every CTA reads identical values and
+// the scalar arithmetic runs once.  Waits are bounded: past `spin_limit`
+// cycles the waiter sets OTFEM_ERR_TIMEOUT, and every barrier returns false
+// on every thread of the CTA once any CTA has set an error status.
+__device__ __forceinline__ unsigned atom_add_acq_rel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 only: arrive; returns true if this CTA is the last of the round.
+__device__ __forceinline__ bool arrive(DeviceSync* s, unsigned round) {
+  unsigned ticket = atom_add_acq_rel(&s->count, 1u);
+  return ticket + 1u == round * gridDim.x;
+}
+
+// Thread 0 only: wait until round `round` is released; false on timeout.
+__device__ __forceinline__ bool wait_released(DeviceSync* s, unsigned round, long long spin_limit) {
+  long long start = clock64();
+  while (int(ld_acquire(&s->gen) - round) < 0) {
+    if (clock64() - start > spin_limit) {
+      atomicCAS(&s->status, 0, OTFEM_ERR_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ bool grid_barrier(DeviceSync* s, long long spin_limit, unsigned& round) {
   __shared__ int ok;
-  __threadfence();
+  ++round;
   __syncthreads();
   if (threadIdx.x == 0) {
     int good = 1;
-    unsigned gen = ld_acquire(&s->gen);
-    __threadfence();
-    unsigned arrived = atomicAdd(&s->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&s->count, 0u);
-      __threadfence();
-      atomicAdd(&s->gen, 1u);
-    } else {
-      long long start = clock64();
-      while (ld_acquire(&s->gen) == gen) {
-        if (clock64() - start > spin_limit) {
-          atomicCAS(&s->status, 0, OTFEM_ERR_TIMEOUT);
-          good = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
+    if (arrive(s, round)) st_release(&s->gen, round);
+    else good = wait_released(s, round, spin_limit) ? 1 : 0;
     if (ld_status(&s->status) != 0) good = 0;
     ok = good;
   }
@@ -149,58 +195,169 @@ __device__ bool grid_barrier(DeviceSync* s, long long spin_limit) {
   return ok != 0;
 }
 
-// Sums NV per-thread values over the whole grid in a fixed order (warp
-// shuffles, CTA tree, then CTA partials in index order), so every CTA obtains
-// bit-identical results.  Includes a grid barrier.  Consecutive calls use
-// alternating halves of the partials array (`parity`, flipped on every call):
-// a CTA may start writing the next sum's partial while slower CTAs are still
-// reading this sum's, and the barrier inside the next call separates the
-// reads of call k from the writes of call k + 2.
-template <int NV>
-__device__ bool grid_sum(const MixedArgs& a, double (&val)[NV], int& parity) {
-  static_assert(2 * NV <= kMaxPartials, "partials too small");
-  __shared__ double s_warp[kBlock / 32][NV];
-  __shared__ double s_out[NV];
+// (hi, lo) float pair: a value hi + lo with |lo| <= ulp(hi)/2.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  float h = s + e;
+  return DF{h, e - (h - s)};
+}
+// (hi, lo) += inc
+__device__ __forceinline__ void df_inc(float& hi, float& lo, float inc) {
+  float s, e;
+  two_sum(hi, inc, s, e);
+  e += lo;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
+// Accumulators of the reductions: FP64, or (hi, lo) float pairs.
+template <typename Acc>
+struct AccOps;
+template <>
+struct AccOps<double> {
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ double shfl_down(double a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+  static __device__ __forceinline__ double to_double(double a) { return a; }
+  static __device__ __forceinline__ double from_double(double a) { return a; }
+  static __device__ __forceinline__ double zero() { return 0.0; }
+};
+template <>
+struct AccOps<DF> {
+  static __device__ __forceinline__ DF add(DF a, DF b) { return df_add(a, b); }
+  static __device__ __forceinline__ DF shfl_down(DF a, int o) {
+    return DF{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
+  }
+  static __device__ __forceinline__ double to_double(DF a) { return double(a.hi) + double(a.lo); }
+  static __device__ __forceinline__ DF from_double(double a) {
+    float h = float(a);
+    return DF{h, float(a - double(h))};
+  }
+  static __device__ __forceinline__ DF zero() { return DF{0.f, 0.f}; }
+};
+
+// Sums NV per-thread values over the grid in a fixed order (warp shuffles,
+// warp totals in warp order, CTA partials in CTA order); the last CTA turns
+// the NV totals into NO outputs with fin(totals, outputs) and every thread of
+// every CTA receives the outputs.  Includes a grid barrier.  Partials
+// alternate between two halves of a.partials by round parity: the partials
+// of round r are read (by the last CTA of r) before that CTA arrives at
+// round r + 1, so the writes of round r + 2 cannot overtake them.
+template <typename Acc, int NV, int NO, typename Fin>
+__device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&out)[NO], unsigned& round,
+                            Fin fin) {
+  static_assert(2 * NV <= kMaxPartials && NO <= 4, "partials too small");
+  typedef AccOps<Acc> Ops;
+  __shared__ Acc s_warp[kBlock / 32][NV];
+  __shared__ double s_res[4];
+  __shared__ int s_flag;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ++round;
+  const int half = int(round & 1u);
+  double* part = a.partials + half * (kMaxPartials / 2) * gridDim.x;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    double x = val[k];
+    Acc x = val[k];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
     if (lane == 0) s_warp[warp][k] = x;
   }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : 0.0;
+      Acc x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : Ops::zero();
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) a.partials[(parity * (kMaxPartials / 2) + k) * gridDim.x + blockIdx.x] = x;
+      for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+      if (lane == 0) part[k * gridDim.x + blockIdx.x] = Ops::to_double(x);
     }
+    __syncwarp();
+    if (lane == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
   }
-  if (!grid_barrier(a.sync, a.spin_limit)) return false;
-  if (warp == 0) {
+  __syncthreads();
+  if (s_flag) {
+    // The last CTA: one partial per thread (gridDim.x <= blockDim.x), then a
+    // fixed-order tree.
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      double x = 0.0;
-      for (int b = lane; b < (int)gridDim.x; b += 32)
-        x += __ldcg(a.partials + (parity * (kMaxPartials / 2) + k) * gridDim.x + b);
+      Acc x = threadIdx.x < gridDim.x ? Ops::from_double(__ldcg(part + k * gridDim.x + threadIdx.x)) : Ops::zero();
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) s_out[k] = x;
+      for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+      if (lane == 0) s_warp[warp][k] = x;
     }
+    __syncthreads();
+    if (warp == 0) {
+      double tot[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        Acc x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : Ops::zero();
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+        tot[k] = Ops::to_double(x);
+      }
+      if (lane == 0) {
+        double res[NO];
+        fin(tot, res);
+        for (int k = 0; k < NO; ++k) {
+          s_res[k] = res[k];
+          a.sync->result[half][k] = res[k];
+        }
+        st_release(&a.sync->gen, round);
+        if (ld_status(&a.sync->status) != 0) s_flag = 0;
+      }
+    }
+  } else if (threadIdx.x == 0) {
+    int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
+    if (ld_status(&a.sync->status) != 0) ok = 0;
+    if (ok)
+      for (int k = 0; k < NO; ++k) s_res[k] = __ldcg(&a.sync->result[half][k]);
+    s_flag = ok;
   }
   __syncthreads();
+  const bool good = s_flag != 0;
 #pragma unroll
-  for (int k = 0; k < NV; ++k) val[k] = s_out[k];
+  for (int k = 0; k < NO; ++k) out[k] = s_res[k];
   __syncthreads();
-  parity ^= 1;
-  return true;
+  return good;
 }
 
-// Coherent (L2) load of node data written by other CTAs within the launch
-// (accumulators filled by their atomics, operands they rewrote).
+struct FinIdentity1 {
+  __device__ void operator()(const double* t, double* o) const { o[0] = t[0]; }
+};
+
+// The CG scalars from (p.q, r.q, q.q) and the current rho = r.r:
+// alpha = rho / p.q, ||r - alpha q||^2 = rho - 2 alpha r.q + alpha^2 q.q
+// (so beta is known before the vector update, which then updates v, r and p
+// in one pass), beta = that / rho.  outputs: alpha, beta, rho_est, flag
+// (0 ok, 1 non-finite system, 2 finite breakdown).
+struct FinAlphaBeta {
+  double rho;
+  __device__ void operator()(const double* t, double* o) const {
+    const double pq = t[0];
+    double alpha = rho / pq;
+    double est = rho - 2.0 * alpha * t[1] + alpha * alpha * t[2];
+    if (est < 0.0) est = 0.0;
+    double beta = est / rho;
+    double flag = 0.0;
+    if (!isfinite(pq) || !isfinite(rho) || !isfinite(t[1]) || !isfinite(t[2])) flag = 1.0;
+    else if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) flag = 2.0;
+    o[0] = alpha;
+    o[1] = beta;
+    o[2] = est;
+    o[3] = flag;
+  }
+};
+
+// Coherent (L2) load of node data written by other CTAs within the launch.
 __device__ __forceinline__ float4 load_acc(const float4* p) { return __ldcg(p); }
 __device__ __forceinline__ double4 load_acc(const double4* p) {
   double2 lo = __ldcg(reinterpret_cast<const double2*>(p));
@@ -256,35 +413,6 @@ __device__ __forceinline__ void element_apply(const R* Re, const R* b, R c0, R c
   for (int a = 0; a < 3; ++a) f[0][a] = -(f[1][a] + f[2][a] + f[3][a]);
 }
 
-// u_k - u_0 (k = 1..3) of one tet from the gathered operands.
-template <typename R>
-__device__ __forceinline__ void local_differences(const typename ApplyOps<R>::V4 (&w)[4],
-                                                  const typename ApplyOps<R>::V4* ulo, int4 n, R (&du)[3][3]);
-template <>
-__device__ __forceinline__ void local_differences<float>(const float4 (&w)[4], const float4* ulo, int4 n,
-                                                         float (&du)[3][3]) {
-  float4 l0 = load_acc(ulo + n.x), l1 = load_acc(ulo + n.y), l2 = load_acc(ulo + n.z), l3 = load_acc(ulo + n.w);
-  du[0][0] = (w[1].x - w[0].x) + (l1.x - l0.x);
-  du[0][1] = (w[1].y - w[0].y) + (l1.y - l0.y);
-  du[0][2] = (w[1].z - w[0].z) + (l1.z - l0.z);
-  du[1][0] = (w[2].x - w[0].x) + (l2.x - l0.x);
-  du[1][1] = (w[2].y - w[0].y) + (l2.y - l0.y);
-  du[1][2] = (w[2].z - w[0].z) + (l2.z - l0.z);
-  du[2][0] = (w[3].x - w[0].x) + (l3.x - l0.x);
-  du[2][1] = (w[3].y - w[0].y) + (l3.y - l0.y);
-  du[2][2] = (w[3].z - w[0].z) + (l3.z - l0.z);
-}
-template <>
-__device__ __forceinline__ void local_differences<double>(const double4 (&w)[4], const double4*, int4,
-                                                          double (&du)[3][3]) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    du[k][0] = w[k + 1].x - w[0].x;
-    du[k][1] = w[k + 1].y - w[0].y;
-    du[k][2] = w[k + 1].z - w[0].z;
-  }
-}
-
 // Stores operand x (and its free flag in w) for the apply: FP32 as (hi, lo).
 __device__ __forceinline__ void store_operand(float4* hi, float4* lo, long i, double x, double y, double z,
                                               double w) {
@@ -297,36 +425,274 @@ __device__ __forceinline__ void store_operand(double4* hi, double4*, long i, dou
   hi[i] = make_double4(x, y, z, w);
 }
 
-// q += dt^2 K' u over the tets of this thread (grid-stride).  Contributions to
-// nodes whose operand w == 0 (fixed rows, never read) are skipped.  The
-// operand u4 is rewritten by other CTAs between sweeps of the same launch, so
-// it is read with L2 loads (no read-only or L1 path); the per-tet data is
-// constant during the launch and may use the read-only path.
+template <typename R>
+struct SmemOperand;
+template <>
+struct SmemOperand<float> {  // per patch node: hi, lo, accumulator
+  static constexpr size_t bytes = sizeof(float4) * 2 + sizeof(float) * 3;
+};
+template <>
+struct SmemOperand<double> {
+  static constexpr size_t bytes = sizeof(double4) + sizeof(double) * 3;
+};
+
+// One element-apply sweep q += dt^2 K' u, by patches.  A CTA takes patches
+// blockIdx.x, blockIdx.x + gridDim.x, ...: it loads its tet's data, stages
+// the patch's nodes (the operand, as hi/lo pairs for FP32) in shared memory
+// once, computes one tet per thread, adds the four node forces into
+// shared-memory accumulators, and writes each node back once: a plain store
+// when no other patch touches the node, a global vector reduction otherwise.
+// Nodes whose operand w == 0 (fixed rows, never read) are not written.  ulo
+// may be null (operand exactly FP32).  The operand is rewritten by other
+// CTAs between sweeps of a launch, so it is loaded with plain (coherent)
+// loads, ordered after the writers by the grid barrier; the per-tet data is
+// constant during a launch.
+template <typename R>
+__device__ void apply_patches(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
+                              const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
+                              const R* __restrict__ re, const R* __restrict__ bb, const R* __restrict__ cc,
+                              R scale, unsigned char* smem) {
+  typedef typename ApplyOps<R>::V4 V4;
+  V4* s_hi = reinterpret_cast<V4*>(smem);
+  const int cap = a.patch_max_nodes_padded;
+  float4* s_lo = reinterpret_cast<float4*>(s_hi + cap);
+  R* s_acc = sizeof(R) == 4 ? reinterpret_cast<R*>(s_lo + cap) : reinterpret_cast<R*>(s_hi + cap);
+  const int T = a.T;
+  const bool has_lo = sizeof(R) == 4 && ulo != nullptr;
+  for (int patch = blockIdx.x; patch < a.num_patches; patch += gridDim.x) {
+    const int t = patch * kPatchTets + threadIdx.x;
+    const bool active = t < T;
+    // per-tet data first: independent of the staging, so the loads overlap it
+    ushort4 l = make_ushort4(0, 0, 0, 0);
+    R Re[9], b[9], c0 = R(0), c1 = R(0), c2 = R(0);
+    if (active) {
+      l = a.lconn[t];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        Re[k] = re[(long)k * T + t];
+        b[k] = bb[(long)k * T + t];
+      }
+      c0 = cc[t];
+      c1 = cc[T + t];
+      c2 = cc[2L * T + t];
+    }
+    const int nb = a.patch_node_ptr[patch];
+    const int nn = a.patch_node_ptr[patch + 1] - nb;
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      int id = a.patch_nodes[nb + j] & 0x7fffffff;
+      s_hi[j] = u4[id];
+      if (sizeof(R) == 4)
+        s_lo[j] = has_lo ? reinterpret_cast<const float4*>(ulo)[id] : make_float4(0.f, 0.f, 0.f, 0.f);
+      s_acc[3 * j] = R(0);
+      s_acc[3 * j + 1] = R(0);
+      s_acc[3 * j + 2] = R(0);
+    }
+    __syncthreads();
+    if (active) {
+      const int ln[4] = {l.x, l.y, l.z, l.w};
+      V4 w[4] = {s_hi[l.x], s_hi[l.y], s_hi[l.z], s_hi[l.w]};
+      R du[3][3];
+      if (sizeof(R) == 4) {
+        float4 lo[4] = {s_lo[l.x], s_lo[l.y], s_lo[l.z], s_lo[l.w]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          du[k][0] = R((float(w[k + 1].x) - float(w[0].x)) + (lo[k + 1].x - lo[0].x));
+          du[k][1] = R((float(w[k + 1].y) - float(w[0].y)) + (lo[k + 1].y - lo[0].y));
+          du[k][2] = R((float(w[k + 1].z) - float(w[0].z)) + (lo[k + 1].z - lo[0].z));
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          du[k][0] = R(w[k + 1].x - w[0].x);
+          du[k][1] = R(w[k + 1].y - w[0].y);
+          du[k][2] = R(w[k + 1].z - w[0].z);
+        }
+      }
+      R f[4][3];
+      element_apply<R>(Re, b, c0, c1, c2, scale, du, f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (w[k].w != 0) {
+          atomicAdd(s_acc + 3 * ln[k], f[k][0]);
+          atomicAdd(s_acc + 3 * ln[k] + 1, f[k][1]);
+          atomicAdd(s_acc + 3 * ln[k] + 2, f[k][2]);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      if (s_hi[j].w == 0) continue;
+      const int raw = a.patch_nodes[nb + j];
+      const int id = raw & 0x7fffffff;
+      R x = s_acc[3 * j], y = s_acc[3 * j + 1], z = s_acc[3 * j + 2];
+      if (raw < 0) {
+        red_add(q4 + id, x, y, z);
+      } else {
+        V4 v;
+        v.x = x;
+        v.y = y;
+        v.z = z;
+        v.w = R(0);
+        q4[id] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// u_k - u_0 of one tet from the four (hi, lo) operands (FP32) or FP64 operands.
+template <typename R, typename V4>
+__device__ __forceinline__ void tet_differences(const V4 (&w)[4], const float4 (&lo)[4], R (&du)[3][3]) {
+  if (sizeof(R) == 4) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      du[k][0] = R((float(w[k + 1].x) - float(w[0].x)) + (lo[k + 1].x - lo[0].x));
+      du[k][1] = R((float(w[k + 1].y) - float(w[0].y)) + (lo[k + 1].y - lo[0].y));
+      du[k][2] = R((float(w[k + 1].z) - float(w[0].z)) + (lo[k + 1].z - lo[0].z));
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      du[k][0] = R(w[k + 1].x - w[0].x);
+      du[k][1] = R(w[k + 1].y - w[0].y);
+      du[k][2] = R(w[k + 1].z - w[0].z);
+    }
+  }
+}
+
+// Variant kApplyGather: as apply_patches, but each thread writes its tet's
+// four node forces to shared memory and each node then sums its own entries
+// in ascending tet order (patch_inc): no atomics, deterministic.
+template <typename R>
+__device__ void apply_patches_gather(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
+                                     const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
+                                     const R* __restrict__ re, const R* __restrict__ bb, const R* __restrict__ cc,
+                                     R scale, unsigned char* smem) {
+  typedef typename ApplyOps<R>::V4 V4;
+  V4* s_hi = reinterpret_cast<V4*>(smem);
+  const int cap = a.patch_max_nodes_padded;
+  float4* s_lo = reinterpret_cast<float4*>(s_hi + cap);
+  R* s_f = sizeof(R) == 4 ? reinterpret_cast<R*>(s_lo + cap) : reinterpret_cast<R*>(s_hi + cap);
+  const int T = a.T;
+  const bool has_lo = sizeof(R) == 4 && ulo != nullptr;
+  for (int patch = blockIdx.x; patch < a.num_patches; patch += gridDim.x) {
+    const int t = patch * kPatchTets + threadIdx.x;
+    const bool active = t < T;
+    ushort4 l = make_ushort4(0, 0, 0, 0);
+    R Re[9], b[9], c0 = R(0), c1 = R(0), c2 = R(0);
+    if (active) {
+      l = a.lconn[t];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        Re[k] = re[(long)k * T + t];
+        b[k] = bb[(long)k * T + t];
+      }
+      c0 = cc[t];
+      c1 = cc[T + t];
+      c2 = cc[2L * T + t];
+    }
+    const int nb = a.patch_node_ptr[patch];
+    const int nn = a.patch_node_ptr[patch + 1] - nb;
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      int id = a.patch_nodes[nb + j] & 0x7fffffff;
+      s_hi[j] = u4[id];
+      if (sizeof(R) == 4)
+        s_lo[j] = has_lo ? reinterpret_cast<const float4*>(ulo)[id] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    if (active) {
+      V4 w[4] = {s_hi[l.x], s_hi[l.y], s_hi[l.z], s_hi[l.w]};
+      float4 lo[4];
+      if (sizeof(R) == 4) {
+        lo[0] = s_lo[l.x];
+        lo[1] = s_lo[l.y];
+        lo[2] = s_lo[l.z];
+        lo[3] = s_lo[l.w];
+      }
+      R du[3][3], f[4][3];
+      tet_differences<R>(w, lo, du);
+      element_apply<R>(Re, b, c0, c1, c2, scale, du, f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) s_f[(k * 3 + c) * kPatchTets + threadIdx.x] = f[k][c];
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nn; j += blockDim.x) {
+      if (s_hi[j].w == 0) continue;
+      R x = R(0), y = R(0), z = R(0);
+      for (int e = a.patch_inc_ptr[nb + j]; e < a.patch_inc_ptr[nb + j + 1]; ++e) {
+        const int ent = a.patch_inc[e], lt = ent >> 2, sl = ent & 3;
+        x += s_f[(sl * 3) * kPatchTets + lt];
+        y += s_f[(sl * 3 + 1) * kPatchTets + lt];
+        z += s_f[(sl * 3 + 2) * kPatchTets + lt];
+      }
+      const int raw = a.patch_nodes[nb + j];
+      const int id = raw & 0x7fffffff;
+      if (raw < 0) {
+        red_add(q4 + id, x, y, z);
+      } else {
+        V4 v;
+        v.x = x;
+        v.y = y;
+        v.z = z;
+        v.w = R(0);
+        q4[id] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Variant kApplyTets: one tet per thread over the whole mesh (grid-stride),
+// operands gathered from global memory, node forces added with global vector
+// reductions (the accumulator must be zero for every written node).
 template <typename R>
 __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                            const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
                            const R* __restrict__ re, const R* __restrict__ bb, const R* __restrict__ cc,
                            R scale) {
+  typedef typename ApplyOps<R>::V4 V4;
   const int T = a.T;
+  const bool has_lo = sizeof(R) == 4 && ulo != nullptr;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
-    int4 n = a.tets[t];
-    typename ApplyOps<R>::V4 w[4] = {load_acc(u4 + n.x), load_acc(u4 + n.y), load_acc(u4 + n.z),
-                                     load_acc(u4 + n.w)};
+    const int4 n = a.tets[t];
+    V4 w[4] = {u4[n.x], u4[n.y], u4[n.z], u4[n.w]};
+    float4 lo[4];
+    if (sizeof(R) == 4) {
+      if (has_lo) {
+        const float4* l4 = reinterpret_cast<const float4*>(ulo);
+        lo[0] = l4[n.x];
+        lo[1] = l4[n.y];
+        lo[2] = l4[n.z];
+        lo[3] = l4[n.w];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) lo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
     R Re[9], b[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       Re[k] = re[(long)k * T + t];
       b[k] = bb[(long)k * T + t];
     }
-    R c0 = cc[t], c1 = cc[T + t], c2 = cc[2L * T + t];
     R du[3][3], f[4][3];
-    local_differences<R>(w, ulo, n, du);
-    element_apply<R>(Re, b, c0, c1, c2, scale, du, f);
-    int nn[4] = {n.x, n.y, n.z, n.w};
+    tet_differences<R>(w, lo, du);
+    element_apply<R>(Re, b, cc[t], cc[T + t], cc[2L * T + t], scale, du, f);
+    const int nn[4] = {n.x, n.y, n.z, n.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-      if (w[k].w != R(0)) red_add(q4 + nn[k], f[k][0], f[k][1], f[k][2]);
+      if (w[k].w != 0) red_add(q4 + nn[k], f[k][0], f[k][1], f[k][2]);
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
+                                            const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
+                                            const R* re, const R* bb, const R* cc, R scale, unsigned char* smem) {
+  if (a.apply_variant == kApplyTets) apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale);
+  else if (a.apply_variant == kApplyGather) apply_patches_gather<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
+  else apply_patches<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
 }
 
 template <typename V4, typename R>
@@ -340,30 +706,222 @@ __device__ __forceinline__ double4 make_v4<double4, double>(double x, double y, 
   return make_double4(x, y, z, w);
 }
 
-// K2: the persistent CG of one step.  R = element-apply precision.
-template <typename R>
-__global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
-  typedef typename ApplyOps<R>::V4 V4;
+__device__ __forceinline__ void trace_row(const MixedArgs& a, int row, double rho, double pq, double alpha,
+                                          double beta, const double* stamp, long long t_start) {
+  if (row >= kTraceRows) return;
+  double* tr = a.trace + kTraceCols * row;
+  tr[0] = rho;
+  tr[1] = pq;
+  tr[2] = alpha;
+  tr[3] = beta;
+  for (int k = 0; k < 5; ++k) tr[4 + k] = stamp[k];
+  tr[9] = double(cycles_now() - t_start);
+}
+
+__device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int applies, bool converged, double rho,
+                                             double rho0, double bnorm2) {
+  int st = ld_status(&a.sync->status);
+  if (st == 0 && !converged) st = OTFEM_WARN_NOT_CONVERGED;
+  a.stats->iterations = it;
+  a.stats->applies = applies;
+  a.stats->status = st;
+  a.stats->rr = rho;
+  a.stats->rr0 = rho0;
+  a.stats->bb = bnorm2;
+}
+
+// K2, mixed precision (see the file comment).
+__global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const int N = a.N;
   const long gstride = (long)gridDim.x * blockDim.x;
   const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  V4* pv = sizeof(R) == 4 ? (V4*)a.p_f : (V4*)a.p_d;
-  V4* vv = sizeof(R) == 4 ? (V4*)a.v_f : (V4*)a.v_d;
-  V4* plo = sizeof(R) == 4 ? (V4*)a.p_lo : nullptr;
-  V4* vlo = sizeof(R) == 4 ? (V4*)a.v_lo : nullptr;
-  V4* qv = sizeof(R) == 4 ? (V4*)a.q_f : (V4*)a.q_d;
-  const R* re = sizeof(R) == 4 ? (const R*)a.re_f : (const R*)a.re_d;
-  const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
-  const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
-  const R scale = R(a.dt * a.dt);
-  const V4 zero4 = make_v4<V4, double>(0.0, 0.0, 0.0, 0.0);
-  int parity = 0;  // alternates the halves of a.partials between grid sums
+  const float scale = float(a.dt * a.dt);
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  unsigned round = 0;  // grid barriers and reductions passed so far
+  extern __shared__ __align__(16) unsigned char smem[];  // patch staging of the apply
   const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
-  const unsigned long long t_start = tracer ? global_ns() : 0ull;
-  double stamp[6] = {0, 0, 0, 0, 0, 0};
+  const long long t_start = tracer ? cycles_now() : 0ll;
+  __shared__ double stamp[6];  // trace stamps, written by the tracer thread only
 
-  // Phase 0: b = M v + dt (f_ext - g) with g gathered in ascending tet order;
-  // diagonal M(1 + dt*alpha) as in fem_dynamics_assembly.h:84-85.
+  // Phase 0: b = M v + dt (f_ext - g), g = the elastic forces gathered in
+  // ascending tet order and summed as (hi, lo) pairs; the diagonal
+  // M(1 + dt*alpha) of fem_dynamics_assembly.h:84-85; v split into (hi, lo).
+  DF bbsum[1] = {{0.f, 0.f}};
+  for (long i = gtid; i < N; i += gstride) {
+    DF g[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
+      int e = a.inc_ent[q];
+      float4 f = a.g_f[4L * (e >> 2) + (e & 3)];
+      df_inc(g[0].hi, g[0].lo, f.x);
+      df_inc(g[1].hi, g[1].lo, f.y);
+      df_inc(g[2].hi, g[2].lo, f.z);
+    }
+    bool fx = a.fixed[i] != 0;
+    double m = a.mass[i];
+    double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+    if (!fx) {
+      double b3[3];
+      for (int c = 0; c < 3; ++c)
+        b3[c] = m * vi[c] + a.dt * (a.fext[3 * i + c] - (double(g[c].hi) + double(g[c].lo)));
+      for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
+      float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
+      bbsum[0] = df_add(bbsum[0], DF{bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2], 0.f});
+      a.diag[i] = m + a.dt * (a.alpha * m);
+    } else {
+      a.diag[i] = 0.0;
+    }
+    // fixed columns keep their velocity in the initial residual (the reference
+    // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
+    // never accumulated (w = 0).
+    store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+    a.q_f[i] = zero4;
+  }
+  double tot[1];
+  if (!grid_reduce<DF, 1, 1>(a, bbsum, tot, round, FinIdentity1())) return;
+  const double bnorm2 = tot[0];
+  const double thresh = a.rtol * a.rtol * bnorm2;
+
+  // Initial residual r = b - A v (FP64), p = r.
+  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+  if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  DF rr[1] = {{0.f, 0.f}};
+  for (long i = gtid; i < N; i += gstride) {
+    if (a.fixed[i]) {
+      a.p_f[i] = zero4;
+      a.r_f[i] = zero4;
+      continue;
+    }
+    float4 q4 = load_acc(a.q_f + i);
+    float4 vh = a.v_f[i], vl = a.v_lo[i];
+    double d = a.diag[i];
+    float rf[3];
+    rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+    rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+    rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+    a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+    a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
+    a.q_f[i] = zero4;
+    rr[0] = df_add(rr[0], DF{rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2], 0.f});
+  }
+  if (!grid_reduce<DF, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
+  double rho = tot[0];
+  const double rho0 = rho;
+  int it = 0, applies = 1;
+  bool converged = rho <= thresh;
+
+  while (!converged && it < a.max_it) {
+    // q += dt^2 K' p
+    apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+    ++applies;
+    if (tracer) stamp[0] = double(cycles_now() - t_start);
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (tracer) stamp[1] = double(cycles_now() - t_start);
+    // q = diag p + q; p.q, r.q, q.q
+    DF s3[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (long i = gtid; i < N; i += gstride) {
+      if (a.fixed[i]) continue;
+      float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
+      float d = float(a.diag[i]);
+      float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+      s3[0] = df_add(s3[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
+      s3[1] = df_add(s3[1], DF{r4.x * qx + r4.y * qy + r4.z * qz, 0.f});
+      s3[2] = df_add(s3[2], DF{qx * qx + qy * qy + qz * qz, 0.f});
+    }
+    if (tracer) stamp[2] = double(cycles_now() - t_start);
+    double sc[4];
+    FinAlphaBeta fin;
+    fin.rho = rho;
+    if (!grid_reduce<DF, 3, 4>(a, s3, sc, round, fin)) return;
+    if (tracer) stamp[3] = double(cycles_now() - t_start);
+    if (sc[3] != 0.0) {
+      // 1: NaN/Inf in the system (e.g. a non-finite force), an error;
+      // 2: finite breakdown (p.Ap <= 0 from rounding at the precision
+      // floor): stop, the step reports OTFEM_WARN_NOT_CONVERGED
+      if (sc[3] == 1.0 && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
+      break;
+    }
+    const float alpha = float(sc[0]), beta = float(sc[1]);
+    const int row = it;
+    ++it;
+    for (long i = gtid; i < N; i += gstride) {
+      if (a.fixed[i]) continue;
+      float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
+      float4 vh = a.v_f[i], vl = a.v_lo[i];
+      float d = float(a.diag[i]);
+      float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+      df_inc(vh.x, vl.x, alpha * p4.x);
+      df_inc(vh.y, vl.y, alpha * p4.y);
+      df_inc(vh.z, vl.z, alpha * p4.z);
+      float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
+      a.v_f[i] = vh;
+      a.v_lo[i] = vl;
+      a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+      a.p_f[i] = make_float4(rx + beta * p4.x, ry + beta * p4.y, rz + beta * p4.z, 1.f);
+      a.q_f[i] = zero4;
+    }
+    if (tracer) stamp[4] = double(cycles_now() - t_start);
+    // The new rho is rho - 2 alpha r.q + alpha^2 q.q from the reduction above;
+    // the exact r.r comes with the residual recompute (every refresh_period
+    // iterations and before convergence is declared), so the update needs
+    // only a barrier (p must be complete before the next apply).
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (tracer) trace_row(a, row, rho, 0.0, sc[0], sc[1], stamp, t_start);
+    rho = sc[2];
+    if ((a.refresh > 0 && it % a.refresh == 0) || rho <= thresh) {
+      // r = b - A v (residual replacement, FP64); q is zero here and the
+      // (hi, lo) velocity is the apply operand.
+      apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+      ++applies;
+      if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+      DF tr[1] = {{0.f, 0.f}};
+      for (long i = gtid; i < N; i += gstride) {
+        if (a.fixed[i]) continue;
+        float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+        double d = a.diag[i];
+        float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+        float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+        float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+        a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+        a.q_f[i] = zero4;
+        tr[0] = df_add(tr[0], DF{rx * rx + ry * ry + rz * rz, 0.f});
+      }
+      if (!grid_reduce<DF, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
+      rho = tot[0];
+    }
+    converged = rho <= thresh;
+  }
+
+  // v back to FP64; position_update (fem_position_update.h:25-39)
+  for (long i = gtid; i < N; i += gstride) {
+    if (a.fixed[i]) continue;
+    float4 vh = a.v_f[i], vl = a.v_lo[i];
+    double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
+    for (int c = 0; c < 3; ++c) {
+      a.v[3 * i + c] = v3[c];
+      a.x[3 * i + c] += v3[c] * a.dt;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
+}
+
+// K2, FP64 solver: every vector and reduction in FP64.
+__global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
+  typedef double4 V4;
+  const int N = a.N;
+  const long gstride = (long)gridDim.x * blockDim.x;
+  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  V4* pv = a.p_d;
+  V4* vv = a.v_d;
+  V4* qv = a.q_d;
+  const double scale = a.dt * a.dt;
+  const V4 zero4 = make_double4(0.0, 0.0, 0.0, 0.0);
+  unsigned round = 0;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const long long t_start = tracer ? cycles_now() : 0ll;
+  __shared__ double stamp[6];
+
   double bbsum[1] = {0.0};
   for (long i = gtid; i < N; i += gstride) {
     double g[3] = {0.0, 0.0, 0.0};
@@ -386,94 +944,81 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
     } else {
       a.diag[i] = 0.0;
     }
-    // fixed columns keep their velocity in the initial residual (the reference
-    // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
-    // never accumulated (w = 0).
-    store_operand(vv, vlo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+    vv[i] = make_double4(vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     qv[i] = zero4;
   }
-  if (!grid_sum<1>(a, bbsum, parity)) return;
-  const double bnorm2 = bbsum[0];
+  double tot[1];
+  if (!grid_reduce<double, 1, 1>(a, bbsum, tot, round, FinIdentity1())) return;
+  const double bnorm2 = tot[0];
   const double thresh = a.rtol * a.rtol * bnorm2;
 
-  // Initial residual r = b - A v, p = r.
-  apply_tets<R>(a, vv, vlo, qv, re, bb, cc, scale);
-  if (!grid_barrier(a.sync, a.spin_limit)) return;
+  apply_sweep<double>(a, vv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
+  if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   double rr[1] = {0.0};
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) {
-      store_operand(pv, plo, i, 0.0, 0.0, 0.0, 0.0);
+      pv[i] = zero4;
       for (int c = 0; c < 3; ++c) a.p[3 * i + c] = 0.0, a.r[3 * i + c] = 0.0;
       continue;
     }
     V4 q4 = load_acc(qv + i);
-    double qa[3] = {double(q4.x), double(q4.y), double(q4.z)};
+    double qa[3] = {q4.x, q4.y, q4.z};
     double d = a.diag[i];
     double ri[3];
     for (int c = 0; c < 3; ++c) ri[c] = a.bvec[3 * i + c] - (d * a.v[3 * i + c] + qa[c]);
     for (int c = 0; c < 3; ++c) a.r[3 * i + c] = ri[c], a.p[3 * i + c] = ri[c];
-    store_operand(pv, plo, i, ri[0], ri[1], ri[2], 1.0);
+    pv[i] = make_double4(ri[0], ri[1], ri[2], 1.0);
     qv[i] = zero4;
     rr[0] += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
   }
-  if (!grid_sum<1>(a, rr, parity)) return;
-  double rho = rr[0];
+  if (!grid_reduce<double, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
+  double rho = tot[0];
   const double rho0 = rho;
   int it = 0, applies = 1;
   bool converged = rho <= thresh;
-  bool v_fresh = false;
 
   while (!converged && it < a.max_it) {
-    // q += dt^2 K' p
-    apply_tets<R>(a, pv, plo, qv, re, bb, cc, scale);
+    apply_sweep<double>(a, pv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
     ++applies;
-    if (tracer) stamp[0] = double(global_ns() - t_start);
-    if (!grid_barrier(a.sync, a.spin_limit)) return;
-    if (tracer) stamp[1] = double(global_ns() - t_start);
-    // q = diag p + q; p.q, r.q, q.q
+    if (tracer) stamp[0] = double(cycles_now() - t_start);
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (tracer) stamp[1] = double(cycles_now() - t_start);
     double s3[3] = {0.0, 0.0, 0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
-      double qi[3] = {d * a.p[3 * i] + double(q4.x), d * a.p[3 * i + 1] + double(q4.y),
-                      d * a.p[3 * i + 2] + double(q4.z)};
+      double qi[3] = {d * a.p[3 * i] + q4.x, d * a.p[3 * i + 1] + q4.y, d * a.p[3 * i + 2] + q4.z};
       for (int c = 0; c < 3; ++c) {
         s3[0] += a.p[3 * i + c] * qi[c];
         s3[1] += a.r[3 * i + c] * qi[c];
         s3[2] += qi[c] * qi[c];
       }
     }
-    if (tracer) stamp[2] = double(global_ns() - t_start);
-    if (!grid_sum<3>(a, s3, parity)) return;
-    if (tracer) stamp[3] = double(global_ns() - t_start);
-    const double pq = s3[0];
-    const double alpha = rho / pq;
-    // ||r - alpha q||^2 from the three sums: the new beta is known before the
-    // vector update, so v, r and p are updated in one pass.
-    double rho_est = rho - 2.0 * alpha * s3[1] + alpha * alpha * s3[2];
-    if (rho_est < 0.0) rho_est = 0.0;
-    const double beta = rho_est / rho;
-    if (!isfinite(pq) || !isfinite(rho) || !isfinite(s3[1]) || !isfinite(s3[2])) {
-      // NaN/Inf in the system (e.g. a non-finite force): an error
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
+    if (tracer) stamp[2] = double(cycles_now() - t_start);
+    double sc[4];
+    FinAlphaBeta fin;
+    fin.rho = rho;
+    if (!grid_reduce<double, 3, 4>(a, s3, sc, round, fin)) return;
+    if (tracer) stamp[3] = double(cycles_now() - t_start);
+    if (sc[3] != 0.0) {
+      if (sc[3] == 1.0 && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
       break;
     }
-    // finite breakdown (p.Ap <= 0 from rounding at the precision floor):
-    // stop; the step reports OTFEM_WARN_NOT_CONVERGED with its residual
-    if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) break;
+    const double alpha = sc[0], beta = sc[1];
     const int row = it;
     ++it;
-    const bool want_refresh = (a.refresh > 0 && it % a.refresh == 0) || rho_est <= 4.0 * thresh;
     double rn[1] = {0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
       double pn[3], vn[3];
+      const double qq[3] = {q4.x, q4.y, q4.z};
       for (int c = 0; c < 3; ++c) {
         double pi = a.p[3 * i + c];
-        double qi = d * pi + double(c == 0 ? q4.x : (c == 1 ? q4.y : q4.z));
+        double qi = d * pi + qq[c];
         vn[c] = a.v[3 * i + c] + alpha * pi;
         double ri = a.r[3 * i + c] - alpha * qi;
         a.v[3 * i + c] = vn[c];
@@ -482,40 +1027,24 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         pn[c] = ri + beta * pi;
         a.p[3 * i + c] = pn[c];
       }
-      store_operand(pv, plo, i, pn[0], pn[1], pn[2], 1.0);
+      pv[i] = make_double4(pn[0], pn[1], pn[2], 1.0);
+      vv[i] = make_double4(vn[0], vn[1], vn[2], 1.0);
       qv[i] = zero4;
-      if (want_refresh) store_operand(vv, vlo, i, vn[0], vn[1], vn[2], 1.0);
     }
-    v_fresh = want_refresh;
-    if (tracer) stamp[4] = double(global_ns() - t_start);
-    if (!grid_sum<1>(a, rn, parity)) return;
-    if (tracer && row < kTraceRows) {
-      double* tr = a.trace + kTraceCols * row;
-      tr[0] = rho;
-      tr[1] = pq;
-      tr[2] = alpha;
-      tr[3] = beta;
-      for (int k = 0; k < 5; ++k) tr[4 + k] = stamp[k];
-      tr[9] = double(global_ns() - t_start);
-    }
-    rho = rn[0];
-    bool refresh = (a.refresh > 0 && it % a.refresh == 0) || rho <= thresh;
-    if (refresh) {
-      if (!v_fresh) {
-        for (long i = gtid; i < N; i += gstride)
-          if (!a.fixed[i]) store_operand(vv, vlo, i, a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2], 1.0);
-        if (!grid_barrier(a.sync, a.spin_limit)) return;
-      }
-      // r = b - A v (residual replacement); q is zero here.
-      apply_tets<R>(a, vv, vlo, qv, re, bb, cc, scale);
+    if (tracer) stamp[4] = double(cycles_now() - t_start);
+    if (!grid_reduce<double, 1, 1>(a, rn, tot, round, FinIdentity1())) return;
+    if (tracer) trace_row(a, row, rho, 0.0, alpha, beta, stamp, t_start);
+    rho = tot[0];
+    if ((a.refresh > 0 && it % a.refresh == 0) || rho <= thresh) {
+      apply_sweep<double>(a, vv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
       ++applies;
-      if (!grid_barrier(a.sync, a.spin_limit)) return;
+      if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       double tr[1] = {0.0};
       for (long i = gtid; i < N; i += gstride) {
         if (a.fixed[i]) continue;
         V4 q4 = load_acc(qv + i);
         double d = a.diag[i];
-        double qa[3] = {double(q4.x), double(q4.y), double(q4.z)};
+        const double qa[3] = {q4.x, q4.y, q4.z};
         for (int c = 0; c < 3; ++c) {
           double ri = a.bvec[3 * i + c] - (d * a.v[3 * i + c] + qa[c]);
           a.r[3 * i + c] = ri;
@@ -523,27 +1052,118 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_persistent(MixedArgs a) {
         }
         qv[i] = zero4;
       }
-      if (!grid_sum<1>(a, tr, parity)) return;
-      rho = tr[0];
+      if (!grid_reduce<double, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
+      rho = tot[0];
     }
     converged = rho <= thresh;
   }
-
-  // position_update (fem_position_update.h:25-39)
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) continue;
     for (int c = 0; c < 3; ++c) a.x[3 * i + c] += a.v[3 * i + c] * a.dt;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    int st = ld_status(&a.sync->status);
-    if (st == 0 && !converged) st = OTFEM_WARN_NOT_CONVERGED;
-    a.stats->iterations = it;
-    a.stats->applies = applies;
-    a.stats->status = st;
-    a.stats->rr = rho;
-    a.stats->rr0 = rho0;
-    a.stats->bb = bnorm2;
+  if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
+}
+
+// K1, mixed: FP32 orientation and elastic forces.  Edge differences of the
+// FP64 current and model coordinates are taken in FP64, then rounded.  The
+// rows of E^-1 are -b_k (fem_compute_b.h), so F = -sum_k e'_k (x) b_k, which
+// Gram-Schmidt orthonormalises exactly as the reference's F (a positive
+// multiple of it) would be.
+__global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets, const double* __restrict__ x,
+                                 const double* __restrict__ x0, const float* __restrict__ b_f,
+                                 const float* __restrict__ c_f, float* re_f, float4* g_f) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  int4 n = tets[t];
+  const int nn[4] = {n.x, n.y, n.z, n.w};
+  float ep[3][3], e0[3][3];
+  {
+    double p0[3] = {x[3 * nn[0]], x[3 * nn[0] + 1], x[3 * nn[0] + 2]};
+    double m0[3] = {x0[3 * nn[0]], x0[3 * nn[0] + 1], x0[3 * nn[0] + 2]};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        ep[k][c] = float(x[3 * nn[k + 1] + c] - p0[c]);
+        e0[k][c] = float(x0[3 * nn[k + 1] + c] - m0[c]);
+      }
   }
+  float b[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) b[q] = b_f[(long)q * T + t];
+  float R[9];
+  if (warp) {
+    float F[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) F[3 * a + c] = -(ep[0][a] * b[c] + ep[1][a] * b[3 + c] + ep[2][a] * b[6 + c]);
+    // row Gram-Schmidt (math_matrix3x3.h:536-558)
+    float r0[3] = {F[0], F[1], F[2]}, r1[3] = {F[3], F[4], F[5]};
+    float l0 = sqrtf(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
+    if (l0 != 0.f) r0[0] /= l0, r0[1] /= l0, r0[2] /= l0;
+    float d = r0[0] * r1[0] + r0[1] * r1[1] + r0[2] * r1[2];
+    r1[0] -= r0[0] * d, r1[1] -= r0[1] * d, r1[2] -= r0[2] * d;
+    float l1 = sqrtf(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+    if (l1 != 0.f) r1[0] /= l1, r1[1] /= l1, r1[2] /= l1;
+    R[0] = r0[0], R[1] = r0[1], R[2] = r0[2];
+    R[3] = r1[0], R[4] = r1[1], R[5] = r1[2];
+    R[6] = r0[1] * r1[2] - r1[1] * r0[2];
+    R[7] = r1[0] * r0[2] - r0[0] * r1[2];
+    R[8] = r0[0] * r1[1] - r1[0] * r0[1];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) R[q] = (q == 0 || q == 4 || q == 8) ? 1.f : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) re_f[(long)q * T + t] = R[q];
+  // rest-frame displacements d_k = Re^T (x_k - x_0) - (x0_k - x0_0)
+  float dk[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dk[k][a] = (R[a] * ep[k][0] + R[3 + a] * ep[k][1] + R[6 + a] * ep[k][2]) - e0[k][a];
+  float H[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) H[a][c] = dk[0][a] * b[c] + dk[1][a] * b[3 + c] + dk[2][a] * b[6 + c];
+  const float c0 = c_f[t], c1 = c_f[T + t], c2 = c_f[2L * T + t];
+  float tr = c1 * (H[0][0] + H[1][1] + H[2][2]);
+  float s[3][3];
+  s[0][0] = c0 * H[0][0] + tr;
+  s[1][1] = c0 * H[1][1] + tr;
+  s[2][2] = c0 * H[2][2] + tr;
+  s[0][1] = s[1][0] = c2 * (H[0][1] + H[1][0]);
+  s[0][2] = s[2][0] = c2 * (H[0][2] + H[2][0]);
+  s[1][2] = s[2][1] = c2 * (H[1][2] + H[2][1]);
+  float S[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S[a][c] = R[3 * a] * s[0][c] + R[3 * a + 1] * s[1][c] + R[3 * a + 2] * s[2][c];
+  float f[4][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) f[k + 1][a] = S[a][0] * b[3 * k] + S[a][1] * b[3 * k + 1] + S[a][2] * b[3 * k + 2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) f[0][a] = -(f[1][a] + f[2][a] + f[3][a]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) g_f[4L * t + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+}
+
+__global__ void k_identity_f32(int T, float* re_f) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  for (int q = 0; q < 9; ++q) re_f[(long)q * T + t] = (q == 0 || q == 4 || q == 8) ? 1.f : 0.f;
+}
+
+// m_Re of every tet (FP64, row-major) from the FP32 structure-of-arrays copy.
+__global__ void k_re_from_f32(int T, const float* __restrict__ re_f, double* Re) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  for (int q = 0; q < 9; ++q) Re[9L * t + q] = double(re_f[(long)q * T + t]);
 }
 
 // K1: orientation (FP64, reference Gram-Schmidt) and the elastic forces
@@ -621,8 +1241,8 @@ __global__ void k_prepare(int T, const double* __restrict__ Bv, const double* __
   }
 }
 
-// Standalone y = A x (diagnostics and the apply-only roofline measurement):
-// pack, one element-apply sweep, finalize.
+// Standalone y = A x (diagnostics and the apply-only measurement): pack, one
+// element-apply sweep, finalize.
 template <typename V4>
 __global__ void k_pack_operand(int N, const unsigned char* __restrict__ fixed, const double* __restrict__ x,
                                V4* u, V4* ulo, V4* q) {
@@ -639,7 +1259,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_apply_sweep(MixedArgs a, const ty
   const R* re = sizeof(R) == 4 ? (const R*)a.re_f : (const R*)a.re_d;
   const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
   const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
-  apply_tets<R>(a, u, ulo, q, re, bb, cc, R(a.dt * a.dt));
+  extern __shared__ __align__(16) unsigned char smem[];
+  apply_sweep<R>(a, u, ulo, q, re, bb, cc, R(a.dt * a.dt), smem);
 }
 
 template <typename V4>
@@ -659,21 +1280,130 @@ __global__ void k_finalize_operand(int N, const unsigned char* __restrict__ fixe
   y[3 * i + 2] = d * x[3 * i + 2] + double(qq.z);
 }
 
+void set_patch_args(MixedArgs& a, const Context& c) {
+  a.num_patches = c.num_patches;
+  a.patch_max_nodes_padded = (c.patch_max_nodes + 3) / 4 * 4;
+  a.patch_node_ptr = c.patch_node_ptr;
+  a.patch_nodes = c.patch_nodes;
+  a.lconn = c.lconn;
+  a.patch_inc_ptr = c.patch_inc_ptr;
+  a.patch_inc = c.patch_inc;
+  a.apply_variant = c.apply_variant;
+}
+
 template <typename R>
 const void* cg_kernel() {
-  return reinterpret_cast<const void*>(&k_cg_persistent<R>);
+  return std::is_same<R, float>::value ? reinterpret_cast<const void*>(&k_cg_mixed)
+                                       : reinterpret_cast<const void*>(&k_cg_fp64);
 }
 
 }  // namespace
 
+// Patches of kPatchTets consecutive tets (in mesh order, which the block
+// generator and most mesh files lay out with spatial locality).  For each
+// patch: its nodes in ascending order (bit 31 set if another patch touches
+// the node), and every tet's nodes as indices into that list.
+cudaError_t build_patches(Context& c, const int32_t* tets) {
+  const int T = c.T, N = c.N;
+  const int P = (T + kPatchTets - 1) / kPatchTets;
+  std::vector<int> npatch(size_t(N), 0), stamp(size_t(N), -1), local(size_t(N), 0);
+  for (int p = 0; p < P; ++p)
+    for (int t = p * kPatchTets; t < std::min(T, (p + 1) * kPatchTets); ++t)
+      for (int k = 0; k < 4; ++k) {
+        int n = tets[4L * t + k];
+        if (stamp[n] != p) {
+          stamp[n] = p;
+          ++npatch[n];
+        }
+      }
+  std::vector<int> ptr(size_t(P) + 1, 0), nodes;
+  std::vector<ushort4> lconn(size_t(T > 0 ? T : 1));
+  std::fill(stamp.begin(), stamp.end(), -1);
+  int maxn = 0;
+  std::vector<int> list, inc_ptr;
+  std::vector<unsigned short> inc;
+  for (int p = 0; p < P; ++p) {
+    list.clear();
+    const int t0 = p * kPatchTets, t1 = std::min(T, (p + 1) * kPatchTets);
+    for (int t = t0; t < t1; ++t)
+      for (int k = 0; k < 4; ++k) {
+        int n = tets[4L * t + k];
+        if (stamp[n] != p) {
+          stamp[n] = p;
+          list.push_back(n);
+        }
+      }
+    std::sort(list.begin(), list.end());
+    for (size_t j = 0; j < list.size(); ++j) {
+      local[list[j]] = int(j);
+      nodes.push_back(list[j] | (npatch[list[j]] > 1 ? int(0x80000000u) : 0));
+    }
+    for (int t = t0; t < t1; ++t) {
+      const int32_t* n = tets + 4L * t;
+      lconn[t] = make_ushort4((unsigned short)local[n[0]], (unsigned short)local[n[1]],
+                              (unsigned short)local[n[2]], (unsigned short)local[n[3]]);
+    }
+    // per patch node, its (local tet, slot) entries in ascending tet order
+    std::vector<int> cnt(list.size() + 1, 0);
+    for (int t = t0; t < t1; ++t)
+      for (int k = 0; k < 4; ++k) ++cnt[local[tets[4L * t + k]] + 1];
+    for (size_t j = 0; j < list.size(); ++j) cnt[j + 1] += cnt[j];
+    const int base = int(inc.size());
+    inc.resize(inc.size() + size_t(4 * (t1 - t0)));
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int t = t0; t < t1; ++t)
+      for (int k = 0; k < 4; ++k)
+        inc[base + fill[local[tets[4L * t + k]]]++] = (unsigned short)(((t - t0) << 2) | k);
+    for (size_t j = 0; j < list.size(); ++j) inc_ptr.push_back(base + cnt[j]);
+    ptr[p + 1] = ptr[p] + int(list.size());
+    maxn = std::max(maxn, int(list.size()));
+  }
+  inc_ptr.push_back(int(inc.size()));
+  c.num_patches = P;
+  c.patch_max_nodes = maxn;
+  const int cap = (maxn + 3) / 4 * 4;
+  // the largest staging of all variants: atomics (operand + accumulators) or
+  // gather (operand + 12 forces per tet)
+  c.apply_smem = std::max(size_t(cap) * std::max(SmemOperand<float>::bytes, SmemOperand<double>::bytes),
+                          size_t(cap) * sizeof(double4) + size_t(kPatchTets) * 12 * sizeof(double));
+  cudaError_t e;
+  if ((e = cudaMalloc(&c.patch_node_ptr, sizeof(int) * ptr.size())) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c.patch_nodes, sizeof(int) * std::max<size_t>(nodes.size(), 1))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c.lconn, sizeof(ushort4) * lconn.size())) != cudaSuccess) return e;
+  if ((e = cudaMemcpy(c.patch_node_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  if (!nodes.empty() &&
+      (e = cudaMemcpy(c.patch_nodes, nodes.data(), sizeof(int) * nodes.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpy(c.lconn, lconn.data(), sizeof(ushort4) * lconn.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  if ((e = cudaMalloc(&c.patch_inc_ptr, sizeof(int) * inc_ptr.size())) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c.patch_inc, sizeof(unsigned short) * std::max<size_t>(inc.size(), 1))) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpy(c.patch_inc_ptr, inc_ptr.data(), sizeof(int) * inc_ptr.size(), cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return e;
+  if (!inc.empty() && (e = cudaMemcpy(c.patch_inc, inc.data(), sizeof(unsigned short) * inc.size(),
+                                      cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  // kernels that stage patches may need more than the default 48 KB
+  const void* fns[] = {cg_kernel<float>(), cg_kernel<double>(), reinterpret_cast<const void*>(&k_apply_sweep<float>),
+                       reinterpret_cast<const void*>(&k_apply_sweep<double>)};
+  for (const void* f : fns)
+    if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(c.apply_smem))) != cudaSuccess)
+      return e;
+  return cudaSuccess;
+}
+
 int mixed_grid_shape(Context& c, int* grid, int* block) {
   int occ32 = 0, occ64 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_cg_persistent<float>, kBlock, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_cg_persistent<double>, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_cg_mixed, kBlock, c.apply_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_cg_fp64, kBlock, c.apply_smem);
   int occ = occ32 < occ64 ? occ32 : occ64;
   if (occ < 1) occ = 1;
   if (occ > 2) occ = 2;
   *grid = c.num_sms * occ;
+  if (*grid > kMaxGrid) *grid = kMaxGrid;
   *block = kBlock;
   return occ;
 }
@@ -685,31 +1415,86 @@ cudaError_t mixed_prepare(Context& c) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_mixed_orient(Context& c, double dt, bool warp) {
+cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
   int nb = (c.T + 255) / 256;
   if (nb < 1) nb = 1;
-  k_orient_rhs<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.E, c.V, c.Bv, c.D, c.Re,
-                                         c.re_f, c.re_d, c.tet_force);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  cudaError_t e;
+  if (solver == OTFEM_SOLVER_FP64) {
+    k_orient_rhs<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.E, c.V, c.Bv, c.D, c.Re,
+                                           c.re_f, c.re_d, c.elastic_force);
+    c.re_f32_pending = false;
+  } else {
+    k_orient_rhs_f32<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.b_f, c.c_f, c.re_f,
+                                               c.g_f);
+    c.re_f32_pending = true;
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // add_plasticity_force (fem_simulate.h:102) runs between the assembly and
   // the right-hand side, as in the reference; it only changes f_ext when
-  // creep and max are both positive, which the host records at init.
-  if (c.plastic_active && (e = launch_plasticity(c, dt)) != cudaSuccess) return e;
+  // creep and max are both positive, which the host records at init.  It
+  // reads the FP64 orientations.
+  if (c.plastic_active) {
+    if (c.re_f32_pending && (e = sync_orientations(c)) != cudaSuccess) return e;
+    if ((e = launch_plasticity(c, dt)) != cudaSuccess) return e;
+  }
   return cudaSuccess;
 }
 
-cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& prm) {
-  cudaError_t e;
-  if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
-  MixedArgs a;
+cudaError_t autotune_apply(Context& c) {
+  if (c.T == 0) return cudaSuccess;
+  int nb = (c.T + 255) / 256, nbn = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
+  // representative operands: identity orientations, the node positions
+  k_identity_f32<<<nb, 256, 0, c.stream>>>(c.T, c.re_f);
+  k_pack_operand<float4><<<nbn, 256, 0, c.stream>>>(c.N, c.fixed, c.x, c.p_f, c.p_lo, c.q_f);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+  if ((e = cudaEventCreate(&e1)) != cudaSuccess) return e;
+  const int saved = c.apply_variant;
+  int best = 0;
+  for (int v = 0; v < kApplyVariants; ++v) {
+    c.apply_variant = v;
+    float best_ms = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1);
+      cudaEventRecord(e0, c.stream);
+      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 4);
+      cudaEventRecord(e1, c.stream);
+      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best_ms = std::min(best_ms, ms / 4.f);
+    }
+    c.apply_ms[v] = best_ms;
+    if (best_ms < c.apply_ms[best]) best = v;
+  }
+  (void)saved;
+  c.apply_variant = best;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+cudaError_t sync_orientations(Context& c) {
+  if (!c.re_f32_pending) return cudaSuccess;
+  int nb = (c.T + 255) / 256;
+  if (nb < 1) nb = 1;
+  k_re_from_f32<<<nb, 256, 0, c.stream>>>(c.T, c.re_f, c.Re);
+  c.re_f32_pending = false;
+  return cudaGetLastError();
+}
+
+static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_params& prm) {
+  a = MixedArgs();
   a.N = c.N;
   a.T = c.T;
   a.tets = c.tets;
   a.fixed = c.fixed;
   a.inc_ptr = c.inc_ptr;
   a.inc_ent = c.inc_ent;
-  a.tet_force = c.tet_force;
+  a.tet_force = c.elastic_force;
+  a.g_f = c.g_f;
   a.mass = c.mass;
   a.fext = c.fext;
   a.x = c.x;
@@ -726,6 +1511,7 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   a.q_f = c.q_f;
   a.p_lo = c.p_lo;
   a.v_lo = c.v_lo;
+  a.r_f = c.r_f;
   a.re_d = c.re_d;
   a.b_d = c.b_d;
   a.c_d = c.c_d;
@@ -741,12 +1527,20 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   a.sync = c.sync;
   a.stats = c.stats;
   a.trace = c.trace;
+  set_patch_args(a, c);
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
+}
+
+cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& prm) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
+  MixedArgs a;
+  fill_args(a, c, dt, prm);
   void* args[] = {&a};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(c.mf_grid);
   cfg.blockDim = dim3(c.mf_block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = c.apply_smem;
   cfg.stream = c.stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -758,47 +1552,33 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
 }
 
 cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps) {
-  MixedArgs a = {};
-  a.N = c.N;
-  a.T = c.T;
-  a.tets = c.tets;
-  a.re_f = c.re_f;
-  a.b_f = c.b_f;
-  a.c_f = c.c_f;
-  a.re_d = c.re_d;
-  a.b_d = c.b_d;
-  a.c_d = c.c_d;
-  a.dt = dt;
+  MixedArgs a;
+  otfem_solver_params prm;
+  otfem_default_params(&prm);
+  fill_args(a, c, dt, prm);
   for (int k = 0; k < sweeps; ++k) {
     if (solver == OTFEM_SOLVER_FP64)
-      k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
+      k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
     else
-      k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.p_f, c.p_lo, c.q_f);
+      k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_f, nullptr, c.q_f);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x,
                                   double* y) {
-  MixedArgs a = {};
-  a.N = c.N;
-  a.T = c.T;
-  a.tets = c.tets;
-  a.re_f = c.re_f;
-  a.b_f = c.b_f;
-  a.c_f = c.c_f;
-  a.re_d = c.re_d;
-  a.b_d = c.b_d;
-  a.c_d = c.c_d;
-  a.dt = dt;
+  MixedArgs a;
+  otfem_solver_params prm;
+  otfem_default_params(&prm);
+  fill_args(a, c, dt, prm);
   int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   if (solver == OTFEM_SOLVER_FP64) {
     k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, nullptr, c.q_d);
-    k_apply_sweep<double><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_d4, nullptr, c.q_d);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.v_d4, nullptr, c.q_d);
     k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_d, y);
   } else {
     k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_f, c.v_lo, c.q_f);
-    k_apply_sweep<float><<<c.mf_grid, kBlock, 0, c.stream>>>(a, c.v_f, c.v_lo, c.q_f);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.v_f, c.v_lo, c.q_f);
     k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_f, y);
   }
   return cudaGetLastError();

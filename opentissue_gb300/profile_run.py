@@ -1,0 +1,72 @@
+"""Profiling driver: a fixed sequence of library launches for `ncu`.
+
+Builds a jittered block beam (x = 0 face fixed, gravity), runs `--steps`
+matrix-free steps (OTFEM_SOLVER_MIXED, CG to rel. residual 1e-6) and then
+`--sweeps` standalone element-apply sweeps, and prints the step statistics
+and the autotuner's choice.  Run it plainly first, then under ncu, e.g.
+
+  python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
+  ncu --set full --clock-control none -k regex:k_apply_sweep -s 45 -c 2 -o prof \\
+      python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
+
+(the autotuner at otfem_init launches 45 apply sweeps before the step).
+"""
+import argparse
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from opentissue_gb300 import build, capi  # noqa: E402
+from opentissue_gb300.fem import generate_blocks  # noqa: E402
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dims", type=int, nargs=3, default=[128, 32, 32])
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--sweeps", type=int, default=4)
+    ap.add_argument("--variant", type=int, default=-1, help="force an element-apply variant (0..2)")
+    ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    args = ap.parse_args()
+    build.build()
+    lib = capi.lib()
+    I, J, K = args.dims
+    tets, coord = generate_blocks(I, J, K, 0.1, 0.1, 0.1)
+    coord = coord + np.random.default_rng(20261203).uniform(-0.01, 0.01, coord.shape)
+    fixed = (np.arange(coord.shape[0]) < (J + 1) * (K + 1)).astype(np.uint8)
+    N, T = coord.shape[0], tets.shape[0]
+    dp = ctypes.POINTER(ctypes.c_double)
+    desc = capi.MeshDesc(N, T, tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), coord.ctypes.data_as(dp),
+                         coord.ctypes.data_as(dp), fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    h = ctypes.c_void_p()
+    capi.check(lib.otfem_create(ctypes.byref(desc), None, ctypes.byref(h)))
+    capi.check(lib.otfem_init(h, 5e5, 0.33, 1000.0, 1e30, 0.0, 0.0))
+    if args.variant >= 0:
+        capi.check(lib.otfem_set_apply_variant(h, args.variant))
+    variant = ctypes.c_int32()
+    ms = np.zeros(3)
+    capi.check(lib.otfem_tuning(h, ctypes.byref(variant), ms.ctypes.data_as(dp)))
+    mass = np.zeros(N)
+    capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(dp), N))
+    f = np.zeros((N, 3))
+    f[fixed == 0, 1] = -9.81 * mass[fixed == 0]
+    capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
+    solver = capi.SOLVER_MIXED if args.solver == "mixed" else capi.SOLVER_FP64
+    p = capi.default_params(solver=solver, max_iterations=5000, rtol=1e-6, graph=0)
+    st = capi.StepStats()
+    for _ in range(args.steps):
+        capi.check(lib.otfem_simulate_ex(h, 0.01, 1, ctypes.byref(p), ctypes.byref(st)))
+        print(f"step: iterations {st.iterations}, applies {st.applies}, rel. residual {st.rel_residual:.3e}")
+    if args.sweeps:
+        capi.check(lib.otfem_apply_sweeps(h, solver, 0.01, args.sweeps))
+    capi.check(lib.otfem_synchronize(h))
+    print(f"tets {T}, nodes {N}, apply variant {variant.value}, sweep ms per variant {ms.tolist()}")
+    capi.check(lib.otfem_destroy(h))
+
+
+if __name__ == "__main__":
+    main()

@@ -114,16 +114,81 @@ def test_iteration_cap_is_a_warning(gpu):
     assert rc == capi.WARN_NOT_CONVERGED and st.iterations == 3
 
 
-def test_mixed_deterministic_setup_state(gpu):
-    # orientations of the matrix-free path follow the reference Gram-Schmidt
+def test_orientations_follow_reference_gram_schmidt(gpu):
+    # the FP64 matrix-free path reproduces the reference orientations to FP64
+    # rounding; the mixed path's FP32 Gram-Schmidt to FP32 rounding
     tets, coord, fixed = beam(5, 3, 3, jitter_seed=8)
-    a = GpuMesh(tets, coord, fixed)
-    a.init()
-    b = GpuMesh(tets, coord, fixed)
-    b.init()
-    f = gravity_force(a.get(capi.MASS), fixed)
-    for m in (a, b):
+    meshes = [GpuMesh(tets, coord, fixed) for _ in range(3)]
+    f = None
+    for m in meshes:
+        m.init()
+        f = gravity_force(m.get(capi.MASS), fixed) if f is None else f
         m.set(capi.F_EXTERNAL, f)
-    a.step(0.01, True, mixed())
-    b.step(0.01, True, capi.default_params(**{"sequential_dots": 0}))
-    assert np.abs(a.re() - b.re()).max() < 1e-14
+        m.set(capi.COORD, coord + np.random.default_rng(1).normal(0, 0.002, coord.shape))
+    meshes[0].step(0.01, True, capi.default_params(sequential_dots=1))
+    meshes[1].step(0.01, True, mixed(solver=capi.SOLVER_FP64))
+    meshes[2].step(0.01, True, mixed())
+    ref = meshes[0].re()
+    assert np.abs(meshes[1].re() - ref).max() < 1e-13
+    assert np.abs(meshes[2].re() - ref).max() < 2e-6
+
+
+@pytest.mark.parametrize("dims,seed", [((4, 2, 2), 3), ((12, 5, 4), 6)])
+def test_apply_operator_vs_assembled_reference(gpu, oracle, dims, seed):
+    """The matrix-free A x (FP32 and FP64 element apply) against the
+    reference's assembled A = K dt^2 + M (1 + dt alpha) (fem_dynamics_assembly.h)."""
+    import ctypes
+    tets, coord, fixed = beam(*dims, jitter_seed=seed)
+    n = coord.shape[0]
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*MATERIAL)
+    mass = o.get(oracle.MASS)
+    f = gravity_force(mass, fixed)
+    o.set(oracle.F_EXTERNAL, f)
+    o.simulate(0.01, True)  # assembles K from the orientations at the initial coordinates
+    rp, cols = o.k_pattern()
+    K = o.k_values()
+    dt = 0.01
+    x = np.random.default_rng(seed).normal(size=(n, 3))
+    ref = np.zeros_like(x)
+    for i in range(n):
+        if fixed[i]:
+            continue
+        for q in range(rp[i], rp[i + 1]):
+            ref[i] += K[q] @ x[cols[q]]
+        ref[i] = ref[i] * dt * dt + mass[i] * (1 + dt * 2.0) * x[i]
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    m.set(capi.F_EXTERNAL, f)
+    _dp = ctypes.POINTER(ctypes.c_double)
+    for solver, tol in ((capi.SOLVER_MIXED, 2e-6), (capi.SOLVER_FP64, 1e-13)):
+        # the orientations of the solver's own first phase
+        p = mixed(solver=solver)
+        capi.check(m.lib.otfem_simulate_phase(m.h, dt, 1, ctypes.byref(p), capi.PHASE_ORIENT))
+        y = np.zeros_like(x)
+        capi.check(m.lib.otfem_apply_operator(m.h, solver, dt, 2.0, x.ctypes.data_as(_dp), y.ctypes.data_as(_dp)))
+        assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), solver
+
+
+def test_every_apply_variant_solves_alike(gpu):
+    """The three element-apply variants the autotuner chooses from give the
+    same solution to FP32-apply accuracy."""
+    import ctypes
+    g = golden("converged")
+    results = []
+    for variant in range(3):
+        m = GpuMesh(g["tets"], g["coord"], g["fixed"])
+        m.init()
+        capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
+        mass = m.get(capi.MASS)
+        for _ in range(5):
+            m.set(capi.F_EXTERNAL, gravity_force(mass, g["fixed"]))
+            _, st = m.step(0.01, True, mixed())
+            assert st.rel_residual <= 1e-6
+        results.append(m.get(capi.COORD))
+        v = ctypes.c_int32()
+        ms = np.zeros(3)
+        capi.check(m.lib.otfem_tuning(m.h, ctypes.byref(v), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        assert v.value == variant and (ms > 0).all()
+    for x in results:
+        assert rel_pos_err(x, g["x_5"], g["coord"]) < POS_TOL
