@@ -334,11 +334,13 @@ struct FinIdentity1 {
   __device__ void operator()(const double* t, double* o) const { o[0] = t[0]; }
 };
 
-// The CG scalars from (p.q, r.q, q.q) and the current rho = r.r:
+// The CG scalars from (p.q, r.q, q.q) and rho = r.r of the current r:
 // alpha = rho / p.q, ||r - alpha q||^2 = rho - 2 alpha r.q + alpha^2 q.q
 // (so beta is known before the vector update, which then updates v, r and p
 // in one pass), beta = that / rho.  outputs: alpha, beta, rho_est, flag
-// (0 ok, 1 non-finite system, 2 finite breakdown).
+// (0 ok, 1 non-finite system, 2 finite breakdown).  With four totals the
+// fourth is the exact r.r (and `rho` is ignored); the estimate of the new
+// r.r then only sets beta, whose error is relative to rho.
 struct FinAlphaBeta {
   double rho;
   __device__ void operator()(const double* t, double* o) const {
@@ -354,6 +356,15 @@ struct FinAlphaBeta {
     o[1] = beta;
     o[2] = est;
     o[3] = flag;
+  }
+};
+
+struct FinAlphaBetaExact {
+  __device__ void operator()(const double* t, double* o) const {
+    FinAlphaBeta f;
+    f.rho = t[3];
+    f(t, o);
+    if (o[3] == 0.0 && !isfinite(t[3])) o[3] = 1.0;
   }
 };
 
@@ -816,22 +827,21 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
-    // q = diag p + q; p.q, r.q, q.q
-    DF s3[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    // q = diag p + q; p.q, r.q, q.q and the exact r.r of the current r
+    DF s4[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float d = float(a.diag[i]);
       float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
-      s3[0] = df_add(s3[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
-      s3[1] = df_add(s3[1], DF{r4.x * qx + r4.y * qy + r4.z * qz, 0.f});
-      s3[2] = df_add(s3[2], DF{qx * qx + qy * qy + qz * qz, 0.f});
+      s4[0] = df_add(s4[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
+      s4[1] = df_add(s4[1], DF{r4.x * qx + r4.y * qy + r4.z * qz, 0.f});
+      s4[2] = df_add(s4[2], DF{qx * qx + qy * qy + qz * qz, 0.f});
+      s4[3] = df_add(s4[3], DF{r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, 0.f});
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
     double sc[4];
-    FinAlphaBeta fin;
-    fin.rho = rho;
-    if (!grid_reduce<DF, 3, 4>(a, s3, sc, round, fin)) return;
+    if (!grid_reduce<DF, 4, 4>(a, s4, sc, round, FinAlphaBetaExact())) return;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
     if (sc[3] != 0.0) {
       // 1: NaN/Inf in the system (e.g. a non-finite force), an error;
@@ -861,14 +871,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       a.q_f[i] = zero4;
     }
     if (tracer) stamp[4] = double(cycles_now() - t_start);
-    // The new rho is rho - 2 alpha r.q + alpha^2 q.q from the reduction above;
-    // the exact r.r comes with the residual recompute (every refresh_period
-    // iterations and before convergence is declared), so the update needs
-    // only a barrier (p must be complete before the next apply).
+    // The exact r.r of the new r comes with the next reduction; here the
+    // update needs only a barrier (p must be complete before the next
+    // apply).  The estimate of the new r.r triggers the residual recompute,
+    // which alone declares convergence.
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) trace_row(a, row, rho, 0.0, sc[0], sc[1], stamp, t_start);
     rho = sc[2];
-    if ((a.refresh > 0 && it % a.refresh == 0) || rho <= thresh) {
+    if ((a.refresh > 0 && it % a.refresh == 0) || sc[2] <= thresh) {
       // r = b - A v (residual replacement, FP64); q is zero here and the
       // (hi, lo) velocity is the apply operand.
       apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
