@@ -190,6 +190,21 @@ OTFEM_API int otfem_host_free(void* ptr);
  * x, y: host, 3 doubles per node; rows of fixed nodes are returned as 0. */
 OTFEM_API int otfem_apply_operator(otfem_handle h, int solver, double dt, double mass_damping, const double* x,
                                    double* y);
+/* The same y = A x without allocating (no counterpart in the reference),
+ * for callers that may not allocate device memory at the call: fixed-rate
+ * loops, where cudaMalloc/cudaFree stall the device and take unbounded time,
+ * and hosts whose device memory is owned by another allocator with a cap or
+ * pool of its own.  x_device, y_device: device arrays of 3
+ * doubles per node, written on the handle's stream and not synchronized.
+ * The operand and accumulator live in one 16 MiB static device array that
+ * every GPU loading the library holds until exit, so meshes are limited to
+ * 262,144 nodes (larger ones return OTFEM_ERR_INVALID_ARGUMENT).  All calls
+ * share that array: calls that may overlap on the GPU (other handles, other
+ * streams) race; order them.  The first call on a device looks up the
+ * array's device address (with that device current, which must be the
+ * handle's device); make it before any stream capture. */
+OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt, double mass_damping,
+                                           const double* x_device, double* y_device);
 /* Enqueues `sweeps` element-apply sweeps q += dt^2 K' p on the resident
  * search direction of the last matrix-free step, asynchronously on the
  * handle's stream: the stiffness apply alone, for timing.  Leaves the solver

@@ -109,6 +109,8 @@ SIGNATURES = {
     "otfem_get_plastic": (ctypes.c_int, [_h, _dp]),
     "otfem_get_volumes": (ctypes.c_int, [_h, _dp]),
     "otfem_apply_operator": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp]),
+    "otfem_apply_operator_noalloc": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                    ctypes.c_void_p, ctypes.c_void_p]),
     "otfem_apply_sweeps": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_int32]),
     "otfem_solver_trace": (ctypes.c_int, [_h, _dp, ctypes.c_int32, _i32p]),
     "otfem_tuning": (ctypes.c_int, [_h, _i32p, _dp]),

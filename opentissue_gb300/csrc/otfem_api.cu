@@ -21,6 +21,18 @@ namespace {
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+namespace otfem {
+Context* context_of(otfem_handle h) { return h ? &h->c : nullptr; }
+int record_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+}  // namespace otfem
+
+namespace {
+
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
   return code;

@@ -49,6 +49,12 @@ struct DeviceStats {
 // doubles; per-tet matrices row-major.  Arrays named *_f are FP32 copies used
 // by the matrix-free apply, stored structure-of-arrays (component c of tet t
 // at [c*T + t]) so that a warp's loads are coalesced.
+struct Context;
+// Accessors for the allocation-free entry point (otfem_noalloc.cu): the
+// handle's context, and setting the message otfem_last_error returns.
+Context* context_of(otfem_handle h);
+int record_error(int code, const std::string& msg);
+
 struct Context {
   int device = 0;
   int num_sms = 0;
@@ -158,6 +164,10 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
 // y = A x with the matrix-free apply of the given precision and the current
 // orientations (x, y: device, 3 doubles per node; rows of fixed nodes = 0).
 cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x, double* y);
+// The same y = A x with the operand and accumulator in caller-provided
+// device scratch (48 B per node FP32, 64 B per node FP64); no allocation.
+cudaError_t launch_apply_operator_scratch(Context& c, int solver, double dt, double mass_damping, const double* x,
+                                          double* y, void* scratch);
 // `sweeps` element-apply sweeps on the resident operand (no host transfer):
 // the apply kernel alone, for timing.
 cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps);

@@ -1594,4 +1594,28 @@ cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass
   return cudaGetLastError();
 }
 
+cudaError_t launch_apply_operator_scratch(Context& c, int solver, double dt, double mass_damping,
+                                          const double* x, double* y, void* scratch) {
+  MixedArgs a;
+  otfem_solver_params prm;
+  otfem_default_params(&prm);
+  fill_args(a, c, dt, prm);
+  int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
+  if (solver == OTFEM_SOLVER_FP64) {
+    double4* u = static_cast<double4*>(scratch);
+    double4* q = u + c.N;
+    k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, u, nullptr, q);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, u, nullptr, q);
+    k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, q, y);
+  } else {
+    float4* u = static_cast<float4*>(scratch);
+    float4* ulo = u + c.N;
+    float4* q = ulo + c.N;
+    k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, u, ulo, q);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, u, ulo, q);
+    k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, q, y);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace otfem
