@@ -284,12 +284,29 @@ def run_ours(args, world, rank, local):
     peak = peaks.get("hbm_gbs")
     peak_note = "measured" if peak else "fallback"
     peak = peak or 6800.0
+    # DRAM bytes of one k_cg_mixed launch from an ncu capture of this workload,
+    # scaled to this run's element-apply sweeps per launch
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "cg_dram_traffic.json")))
-        traffic = prof["dram_bytes_per_apply_sweep"] * float(np.mean([b for b in applies]))
-    except (OSError, ValueError, KeyError):
+        traffic = prof["dram_bytes_per_launch"] / prof["applies_per_launch"] * float(np.mean(applies))
+    except (OSError, ValueError, KeyError, ZeroDivisionError):
         traffic = None
+
+    # ---- the element-apply sweep alone (the stiffness apply) ----------------
+    variant = ctypes.c_int32()
+    capi.check(lib.otfem_tuning(h, ctypes.byref(variant), None))
+    sweep_ms = []
+    for k in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush_l2()
+        e0.record(stream)
+        capi.check(lib.otfem_apply_sweeps(h, capi.SOLVER_MIXED, w["dt"], 1))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sweep_ms.append(e0.elapsed_time(e1))
+    sweep_bytes = BYTES_PER_TET_APPLY * T + BYTES_PER_NODE_APPLY * n_free
+    sweep_gbs = sweep_bytes / (float(np.median(sweep_ms)) * 1e-3) / 1e9
 
     # ---- end to end through the C ABI with host buffers ---------------------
     pin_x = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -329,9 +346,13 @@ def run_ours(args, world, rank, local):
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
                    "iterations_per_step": float(np.mean(its)), "max_rel_residual": float(np.max(res))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "k_cg_persistent<float>", "peak_source": peak_note,
+                     "traffic": traffic, "kernel": "k_cg_mixed", "peak_source": peak_note,
                      "algorithmic_bytes_per_launch": float(np.mean(cg_bytes)),
-                     "kernel_ms": float(np.mean(cg_ms))},
+                     "kernel_ms": float(np.mean(cg_ms)),
+                     "apply_sweep": {"kernel": "k_apply_sweep<float>", "variant": int(variant.value),
+                                     "ms": float(np.median(sweep_ms)), "algorithmic_bytes": sweep_bytes,
+                                     "achieved": sweep_gbs, "frac": sweep_gbs / peak,
+                                     "l2": "flushed before each sweep"}},
         "e2e": {"value": e2e_value, "unit": "tet-steps/s", "h2d_bytes_per_step": 3 * 24 * N,
                 "d2h_bytes_per_step": 2 * 24 * N},
         "gpu_launches": int(n1.value - n0.value),

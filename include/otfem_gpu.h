@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 1
+#define OTFEM_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -84,7 +84,9 @@ typedef struct otfem_solver_params {
   double rtol;              /* matrix-free: stop at ||r|| <= rtol*||b|| (free rows) */
   int refresh_period;       /* matrix-free: recompute r = b - A v every N iterations (16) */
   int sequential_dots;      /* reference solver: 1 = sum dot products in node order on one
-                               thread (bit-identical to the reference), 0 = parallel tree */
+                               thread (bit-identical to the reference), 0 = parallel tree.
+                               matrix-free: 1 = grid sums of the CTA totals in CTA order,
+                               0 = FP64 atomic accumulation of them (faster) */
   int warm_start;           /* OTFEM_WARM_START_* */
   int graph;                /* 1 = replay the step from a CUDA graph (default) */
 } otfem_solver_params;
@@ -219,10 +221,14 @@ OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t 
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* The element-apply variant the autotuner chose for this mesh at otfem_init
  * (0: patches with shared-memory atomics, 1: patches with a deterministic
- * per-node gather, 2: one tet per thread with global reductions) and the
- * measured time of one sweep of each (ms, 3 doubles; may be NULL). */
+ * per-node gather, 2: one tet per thread with global reductions, 3: as 2 with
+ * each tile of tets staged in shared memory by bulk copies) and the measured
+ * time of one sweep of each (ms, OTFEM_NUM_APPLY_VARIANTS doubles; may be
+ * NULL).  The FP64 solver runs variant 3 as 2. */
+#define OTFEM_NUM_APPLY_VARIANTS 4
 OTFEM_API int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_variant);
-/* Forces an element-apply variant (0..2) for the following steps. */
+/* Forces an element-apply variant (0..OTFEM_NUM_APPLY_VARIANTS-1) for the
+ * following steps. */
 OTFEM_API int otfem_set_apply_variant(otfem_handle h, int32_t variant);
 /* Number of kernels this handle has enqueued so far (graph replays included). */
 OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);

@@ -27,6 +27,7 @@ COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B = range(7)
 SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
 WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2
+NUM_APPLY_VARIANTS = 4
 
 
 class SolverParams(ctypes.Structure):

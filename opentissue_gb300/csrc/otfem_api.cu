@@ -57,7 +57,7 @@ void free_all(Context& c) {
   void* ptrs[] = {c.tets, c.x, c.x0, c.v, c.fext, c.mass, c.f0, c.b, c.fixed, c.prev, c.update,
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
-                  c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f,
+                  c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
                   c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
@@ -249,6 +249,8 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   memset(c.stats_host, 0, sizeof(otfem::DeviceStats));
   if ((e = otfem::build_patches(c, d->tets)) != cudaSuccess) return bail(e, "build_patches");
   otfem::mixed_grid_shape(c, &c.mf_grid, &c.mf_block);
+  otfem::staged_tiles(c);
+  OT_ALLOC(c.tile_f, size_t(c.num_tiles) * otfem::kTileWords * size_t(c.tile_tets));
   OT_ALLOC(c.partials, size_t(otfem::kMaxPartials) * c.mf_grid);
 
   // zero-initialised node members (math_vector3.h:63-66) and uploads

@@ -32,6 +32,11 @@ struct DeviceSync {
   int status;                // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
   int pad2[31];
   double result[2][4];       // grid-sum results, double-buffered by barrier parity
+  double pad3[8];
+  double acc[2][4];          // grid-sum accumulators (FP64 reductions), by barrier parity
+  double pad4[8];
+  unsigned tile_ticket;      // staged apply: monotonic tile tickets
+  unsigned pad5[31];
 };
 
 // Statistics written by the step kernels (device memory).
@@ -116,6 +121,11 @@ struct Context {
   ushort4* lconn = nullptr;       // T
   int* patch_inc_ptr = nullptr;   // per patch node (+1): offsets into patch_inc
   unsigned short* patch_inc = nullptr;  // 4T entries (patch-local tet << 2) | slot
+  // staged apply: tiles of tile_tets consecutive tets, each stored as 20
+  // word arrays of tile_tets entries (node ids, rotation quaternion, b_1..b_3,
+  // c0..c2), copied to shared memory whole by the bulk-copy engine
+  float* tile_f = nullptr;
+  int num_tiles = 0, tile_tets = 0;
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
   double apply_ms[4] = {0, 0, 0, 0};  // measured time of one sweep per variant
@@ -151,13 +161,20 @@ cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
 
 // ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
 cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
+// Tile size of the staged apply for the persistent grid (sets tile_tets and
+// num_tiles): tiles of at most kTileMaxTets tets, as even a share of the
+// tets per CTA as a multiple of 16 allows.
+void staged_tiles(Context& c);
 // Builds the apply patches from the host connectivity (once per mesh).
 cudaError_t build_patches(Context& c, const int32_t* tets_host);
 cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver);
 // Times one element-apply sweep of every variant on this mesh and keeps the
 // fastest in c.apply_variant (synchronises the stream).
 cudaError_t autotune_apply(Context& c);
-constexpr int kNumApplyVariants = 3;
+constexpr int kNumApplyVariants = OTFEM_NUM_APPLY_VARIANTS;
+// Staged-apply tiles: at most kTileMaxTets tets of kTileWords 32-bit words.
+constexpr int kTileMaxTets = 512;
+constexpr int kTileWords = 20;
 // Writes m_Re (FP64) from the FP32 orientations of the last mixed step.
 cudaError_t sync_orientations(Context& c);
 cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& p);

@@ -57,7 +57,11 @@ constexpr int kPatchTets = kBlock;
 constexpr int kApplyAtomics = 0;  // patches, shared-memory atomic accumulation
 constexpr int kApplyGather = 1;   // patches, per-node gather over patch-local incidence (deterministic)
 constexpr int kApplyTets = 2;     // grid-stride over tets, global vector reductions
-constexpr int kApplyVariants = 3;
+constexpr int kApplyStaged = 3;   // tiles of tets staged in shared memory by bulk copies, global reductions
+constexpr int kApplyVariants = kNumApplyVariants;
+// Staged apply: two tile buffers and their two mbarriers.
+constexpr size_t kStageBytes = size_t(kTileMaxTets) * kTileWords * sizeof(float);
+constexpr size_t kStagedSmem = 2 * kStageBytes + 2 * sizeof(unsigned long long);
 // Largest persistent grid (CTAs): the last CTA of a grid sum loads one
 // partial per thread, so the grid may not exceed the CTA size.
 constexpr int kMaxGrid = kBlock;
@@ -108,7 +112,10 @@ struct MixedArgs {
   const ushort4* lconn;
   const int* patch_inc_ptr;             // per patch node: offsets into patch_inc
   const unsigned short* patch_inc;      // (patch-local tet << 2) | slot, ascending tet
-  int apply_variant;                    // kApplyAtomics / kApplyGather / kApplyTets
+  int apply_variant;                    // kApplyAtomics / kApplyGather / kApplyTets / kApplyStaged
+  const float* tile_f;                  // staged apply tiles (see Context::tile_f)
+  int tile_tets, num_tiles;
+  int ordered_sums;                     // grid sums of the CTA totals in CTA order
   long long spin_limit;
 };
 
@@ -139,6 +146,82 @@ __device__ __forceinline__ void red_add(double4* q, double a, double b, double c
   atomicAdd(&q->x, a);
   atomicAdd(&q->y, b);
   atomicAdd(&q->z, c);
+}
+
+// ---- bulk copies into shared memory (staged apply) ----------------------
+// One thread arms an mbarrier with the byte count of a tile and issues the
+// bulk copy; the copy engine completes the transaction on the barrier, and
+// every thread waits for the barrier's phase with a bounded spin.
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arm(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for phase `parity` of the barrier to complete; false after
+// spin_limit cycles.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, long long spin_limit) {
+  long long start = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - start > spin_limit) return false;
+  return true;
+}
+
+// Rotation <-> unit quaternion (x, y, z, w).  The quaternion of a rotation
+// matrix by Shepperd's method (the largest of the four squared components
+// first, for accuracy); the matrix of a quaternion by the standard product
+// formula (Hamilton convention, v' = R v).
+__device__ __forceinline__ float4 rotation_to_quaternion(const float* R) {
+  const float tr = R[0] + R[4] + R[8];
+  float x, y, z, w;
+  if (tr > 0.f) {
+    const float s = 2.f * sqrtf(tr + 1.f);
+    w = 0.25f * s, x = (R[7] - R[5]) / s, y = (R[2] - R[6]) / s, z = (R[3] - R[1]) / s;
+  } else if (R[0] > R[4] && R[0] > R[8]) {
+    const float s = 2.f * sqrtf(1.f + R[0] - R[4] - R[8]);
+    w = (R[7] - R[5]) / s, x = 0.25f * s, y = (R[1] + R[3]) / s, z = (R[2] + R[6]) / s;
+  } else if (R[4] > R[8]) {
+    const float s = 2.f * sqrtf(1.f + R[4] - R[0] - R[8]);
+    w = (R[2] - R[6]) / s, x = (R[1] + R[3]) / s, y = 0.25f * s, z = (R[5] + R[7]) / s;
+  } else {
+    const float s = 2.f * sqrtf(1.f + R[8] - R[0] - R[4]);
+    w = (R[3] - R[1]) / s, x = (R[2] + R[6]) / s, y = (R[5] + R[7]) / s, z = 0.25f * s;
+  }
+  const float n = rsqrtf(x * x + y * y + z * z + w * w);
+  return make_float4(x * n, y * n, z * n, w * n);
+}
+__device__ __forceinline__ void quaternion_to_rotation(float4 q, float* R) {
+  const float xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
+  const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+  const float xw = q.x * q.w, yw = q.y * q.w, zw = q.z * q.w;
+  R[0] = 1.f - 2.f * (yy + zz), R[1] = 2.f * (xy - zw), R[2] = 2.f * (xz + yw);
+  R[3] = 2.f * (xy + zw), R[4] = 1.f - 2.f * (xx + zz), R[5] = 2.f * (yz - xw);
+  R[6] = 2.f * (xz - yw), R[7] = 2.f * (yz + xw), R[8] = 1.f - 2.f * (xx + yy);
+}
+
+// Word w of tet t in the staged-apply tiles.
+__device__ __forceinline__ long tile_word(int tile_tets, int t, int w) {
+  const int tile = t / tile_tets;
+  return (long(tile) * kTileWords + w) * tile_tets + (t - tile * tile_tets);
 }
 
 // Grid barriers and grid reductions.  Every CTA passes the same sequence of
@@ -245,19 +328,25 @@ struct AccOps<DF> {
   static __device__ __forceinline__ DF zero() { return DF{0.f, 0.f}; }
 };
 
-// Sums NV per-thread values over the grid in a fixed order (warp shuffles,
-// warp totals in warp order, CTA partials in CTA order); the last CTA turns
-// the NV totals into NO outputs with fin(totals, outputs) and every thread of
-// every CTA receives the outputs.  Includes a grid barrier.  Partials
-// alternate between two halves of a.partials by round parity: the partials
-// of round r are read (by the last CTA of r) before that CTA arrives at
-// round r + 1, so the writes of round r + 2 cannot overtake them.
+// Sums NV per-thread values over the grid: warp shuffles, then the warp
+// totals (NV warps in parallel, one value each), then the CTA totals.  With
+// a.ordered_sums the CTA totals go to per-CTA partials that the last CTA to
+// arrive adds up in CTA order (a fixed order); otherwise each CTA adds its
+// totals into FP64 accumulators with atomic reductions and the last CTA only
+// reads them (a shorter critical path; sums in arrival order).  The last CTA turns the NV totals into NO outputs with
+// fin(totals, outputs), and every thread of every CTA receives the outputs.
+// Includes a grid barrier.  Partials, accumulators and results alternate
+// between two halves by round parity: those of round r are consumed (and the
+// accumulators cleared) by the last CTA of r before it releases r, so the
+// writes of round r + 2 cannot overtake them.
 template <typename Acc, int NV, int NO, typename Fin>
 __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&out)[NO], unsigned& round,
                             Fin fin) {
-  static_assert(2 * NV <= kMaxPartials && NO <= 4, "partials too small");
+  static_assert(2 * NV <= kMaxPartials && NO <= 4 && NV <= 4, "partials too small");
   typedef AccOps<Acc> Ops;
-  __shared__ Acc s_warp[kBlock / 32][NV];
+  constexpr int kWarps = kBlock / 32;
+  __shared__ Acc s_warp[kWarps][NV];
+  __shared__ double s_tot[4];
   __shared__ double s_res[4];
   __shared__ int s_flag;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -272,48 +361,52 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
     if (lane == 0) s_warp[warp][k] = x;
   }
   __syncthreads();
-  if (warp == 0) {
+  if (warp < NV) {
+    // warp k: value k over the kWarps warp totals
+    Acc x = lane < kWarps ? s_warp[lane][warp] : Ops::zero();
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      Acc x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : Ops::zero();
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-      if (lane == 0) part[k * gridDim.x + blockIdx.x] = Ops::to_double(x);
+    for (int o = kWarps / 2; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+    if (lane == 0) {
+      if (a.ordered_sums) part[warp * gridDim.x + blockIdx.x] = Ops::to_double(x);
+      else atomicAdd(&a.sync->acc[half][warp], Ops::to_double(x));
     }
-    __syncwarp();
-    if (lane == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
   }
   __syncthreads();
+  if (threadIdx.x == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
+  __syncthreads();
   if (s_flag) {
-    // The last CTA: one partial per thread (gridDim.x <= blockDim.x), then a
-    // fixed-order tree.
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      Acc x = threadIdx.x < gridDim.x ? Ops::from_double(__ldcg(part + k * gridDim.x + threadIdx.x)) : Ops::zero();
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-      if (lane == 0) s_warp[warp][k] = x;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      double tot[NV];
+    if (a.ordered_sums) {
+      // one partial per thread (gridDim.x <= blockDim.x), then a fixed-order tree
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        Acc x = lane < (int)(blockDim.x >> 5) ? s_warp[lane][k] : Ops::zero();
+        Acc x = threadIdx.x < gridDim.x ? Ops::from_double(__ldcg(part + k * gridDim.x + threadIdx.x)) : Ops::zero();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-        tot[k] = Ops::to_double(x);
+        if (lane == 0) s_warp[warp][k] = x;
       }
-      if (lane == 0) {
-        double res[NO];
-        fin(tot, res);
-        for (int k = 0; k < NO; ++k) {
-          s_res[k] = res[k];
-          a.sync->result[half][k] = res[k];
-        }
-        st_release(&a.sync->gen, round);
-        if (ld_status(&a.sync->status) != 0) s_flag = 0;
+      __syncthreads();
+      if (warp < NV) {
+        Acc x = lane < kWarps ? s_warp[lane][warp] : Ops::zero();
+#pragma unroll
+        for (int o = kWarps / 2; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+        if (lane == 0) s_tot[warp] = Ops::to_double(x);
       }
+      __syncthreads();
+    } else if (threadIdx.x < NV) {
+      s_tot[threadIdx.x] = __ldcg(&a.sync->acc[half][threadIdx.x]);
+      a.sync->acc[half][threadIdx.x] = 0.0;  // for round r + 2
+    }
+    if (threadIdx.x == 0) {
+      double tot[NV], res[NO];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) tot[k] = s_tot[k];
+      fin(tot, res);
+      for (int k = 0; k < NO; ++k) {
+        s_res[k] = res[k];
+        a.sync->result[half][k] = res[k];
+      }
+      st_release(&a.sync->gen, round);
+      if (ld_status(&a.sync->status) != 0) s_flag = 0;
     }
   } else if (threadIdx.x == 0) {
     int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
@@ -345,10 +438,12 @@ struct FinAlphaBeta {
   double rho;
   __device__ void operator()(const double* t, double* o) const {
     const double pq = t[0];
-    double alpha = rho / pq;
+    // two independent reciprocals instead of two dependent divisions
+    const double inv_pq = 1.0 / pq, inv_rho = 1.0 / rho;
+    double alpha = rho * inv_pq;
     double est = rho - 2.0 * alpha * t[1] + alpha * alpha * t[2];
     if (est < 0.0) est = 0.0;
-    double beta = est / rho;
+    double beta = est * inv_rho;
     double flag = 0.0;
     if (!isfinite(pq) || !isfinite(rho) || !isfinite(t[1]) || !isfinite(t[2])) flag = 1.0;
     else if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) flag = 2.0;
@@ -697,11 +792,120 @@ __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u
   }
 }
 
+// Staged-apply tile claims.  Tickets come from one monotonic counter that is
+// zero at the start of a launch, and every CTA's claims in a sweep end with
+// exactly one ticket past the last tile, so a sweep consumes num_tiles +
+// gridDim.x tickets and ticket k is tile k mod (num_tiles + gridDim.x) of
+// its sweep (values >= num_tiles: no tile left).  Sweeps of a launch are
+// separated by grid barriers, so their tickets do not interleave.
+__device__ __forceinline__ int claim_tile(const MixedArgs& a) {
+  const unsigned span = unsigned(a.num_tiles) + gridDim.x;
+  const unsigned k = atomicAdd(&a.sync->tile_ticket, 1u) % span;
+  return k < unsigned(a.num_tiles) ? int(k) : -1;
+}
+
+// Variant kApplyStaged (FP32): as kApplyTets, but the per-tet data (node
+// ids, rotation quaternion, b_1..b_3, c0..c2: 80 bytes per tet) arrives in
+// shared memory by bulk copies, a tile of tile_tets tets at a time and one
+// tile ahead of the computation, so no thread waits on DRAM for it.  CTAs
+// claim tiles dynamically (claim_tile), so SMs that see more memory
+// bandwidth take more tiles.  On a copy that does not complete within
+// spin_limit cycles the CTA sets OTFEM_ERR_TIMEOUT, stops, and waits (again
+// bounded) for the copies it still has in flight before returning.
+__device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                             unsigned char* smem) {
+  const int TT = a.tile_tets;
+  const unsigned tile_bytes = unsigned(TT) * kTileWords * sizeof(float);
+  auto stage = [smem](int sb) { return reinterpret_cast<float*>(smem + sb * kStageBytes); };
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem + 2 * kStageBytes);
+  __shared__ int s_tile[2];  // tile in each buffer, -1: none
+  __shared__ int s_more;     // thread 0 has not yet drawn the sweep's last ticket
+  const int tid = threadIdx.x;
+  __syncthreads();  // the buffers' previous readers are done
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    int more = 1;
+    for (int sb = 0; sb < 2; ++sb) {
+      const int tile = more ? claim_tile(a) : -1;
+      if (tile < 0) more = 0;
+      s_tile[sb] = tile;
+      if (tile >= 0) {
+        mbar_arm(&bar[sb], tile_bytes);
+        bulk_copy_g2s(stage(sb), a.tile_f + size_t(tile) * kTileWords * TT, tile_bytes, &bar[sb]);
+      }
+    }
+    s_more = more;
+  }
+  __syncthreads();
+  int j = 0;
+  bool failed = false;
+  for (;; ++j) {
+    const int sb = j & 1;
+    const int tile = s_tile[sb];  // written before the previous CTA barrier
+    if (tile < 0) break;
+    const bool ok = mbar_wait(&bar[sb], (j >> 1) & 1, a.spin_limit);
+    const int t = tile * TT + tid;
+    if (ok && tid < TT && t < a.T) {
+      const float* w = stage(sb);
+      const int nn[4] = {__float_as_int(w[tid]), __float_as_int(w[TT + tid]), __float_as_int(w[2 * TT + tid]),
+                         __float_as_int(w[3 * TT + tid])};
+      float4 wv[4], lo[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) wv[k] = u4[nn[k]];
+      if (ulo) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) lo[k] = ulo[nn[k]];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) lo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      float Re[9], b[9];
+      quaternion_to_rotation(make_float4(w[4 * TT + tid], w[5 * TT + tid], w[6 * TT + tid], w[7 * TT + tid]), Re);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT + tid];
+      float du[3][3], f[4][3];
+      tet_differences<float>(wv, lo, du);
+      element_apply<float>(Re, b, w[17 * TT + tid], w[18 * TT + tid], w[19 * TT + tid], scale, du, f);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (wv[k].w != 0) red_add(q4 + nn[k], f[k][0], f[k][1], f[k][2]);
+    }
+    // every thread is done with buffer sb: refill it with the next claim
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    if (tid == 0) {
+      const int next = s_more ? claim_tile(a) : -1;
+      if (next < 0) s_more = 0;
+      s_tile[sb] = next;
+      if (next >= 0) {
+        mbar_arm(&bar[sb], tile_bytes);
+        bulk_copy_g2s(stage(sb), a.tile_f + size_t(next) * kTileWords * TT, tile_bytes, &bar[sb]);
+      }
+    }
+  }
+  if (failed && tid == 0) {
+    atomicCAS(&a.sync->status, 0, OTFEM_ERR_TIMEOUT);
+    // the copies of claims j and j + 1 may still be arriving
+    for (int k = j; k < j + 2; ++k)
+      if (s_tile[k & 1] >= 0) mbar_wait(&bar[k & 1], (k >> 1) & 1, a.spin_limit);
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                                             const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
                                             const R* re, const R* bb, const R* cc, R scale, unsigned char* smem) {
-  if (a.apply_variant == kApplyTets) apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale);
+  if constexpr (sizeof(R) == 4) {
+    if (a.apply_variant == kApplyStaged) {
+      apply_staged(a, u4, ulo, q4, scale, smem);
+      return;
+    }
+  }
+  if (a.apply_variant == kApplyTets || a.apply_variant == kApplyStaged) apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale);
   else if (a.apply_variant == kApplyGather) apply_patches_gather<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
   else apply_patches<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
 }
@@ -1081,7 +1285,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
 // multiple of it) would be.
 __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets, const double* __restrict__ x,
                                  const double* __restrict__ x0, const float* __restrict__ b_f,
-                                 const float* __restrict__ c_f, float* re_f, float4* g_f) {
+                                 const float* __restrict__ c_f, float* re_f, float4* g_f, float* tile_f,
+                                 int tile_tets) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int4 n = tets[t];
@@ -1125,6 +1330,14 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
 #pragma unroll
     for (int q = 0; q < 9; ++q) R[q] = (q == 0 || q == 4 || q == 8) ? 1.f : 0.f;
   }
+  // The rotation every FP32 apply variant uses is the one the staged apply
+  // rebuilds from its quaternion, so forces and operator agree.
+  const float4 quat = rotation_to_quaternion(R);
+  quaternion_to_rotation(quat, R);
+  tile_f[tile_word(tile_tets, t, 4)] = quat.x;
+  tile_f[tile_word(tile_tets, t, 5)] = quat.y;
+  tile_f[tile_word(tile_tets, t, 6)] = quat.z;
+  tile_f[tile_word(tile_tets, t, 7)] = quat.w;
 #pragma unroll
   for (int q = 0; q < 9; ++q) re_f[(long)q * T + t] = R[q];
   // rest-frame displacements d_k = Re^T (x_k - x_0) - (x0_k - x0_0)
@@ -1163,10 +1376,11 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
   for (int k = 0; k < 4; ++k) g_f[4L * t + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
 }
 
-__global__ void k_identity_f32(int T, float* re_f) {
+__global__ void k_identity_f32(int T, float* re_f, float* tile_f, int tile_tets) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   for (int q = 0; q < 9; ++q) re_f[(long)q * T + t] = (q == 0 || q == 4 || q == 8) ? 1.f : 0.f;
+  for (int q = 0; q < 4; ++q) tile_f[tile_word(tile_tets, t, 4 + q)] = q == 3 ? 1.f : 0.f;
 }
 
 // m_Re of every tet (FP64, row-major) from the FP32 structure-of-arrays copy.
@@ -1183,7 +1397,7 @@ __global__ void k_orient_rhs(int T, int warp, const int4* __restrict__ tets, con
                              const double* __restrict__ x0, const double* __restrict__ E,
                              const double* __restrict__ V, const double* __restrict__ Bv,
                              const double* __restrict__ D, double* Re, float* re_f, double* re_d,
-                             double* tet_force) {
+                             double* tet_force, float* tile_f, int tile_tets) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int4 n = tets[t];
@@ -1196,11 +1410,17 @@ __global__ void k_orient_rhs(int T, int warp, const int4* __restrict__ tets, con
     for (int q = 0; q < 9; ++q) R[q] = 0.0;
     R[0] = R[4] = R[8] = 1.0;
   }
+  float Rf[9];
   for (int q = 0; q < 9; ++q) {
     Re[9 * t + q] = R[q];
-    re_f[(long)q * T + t] = float(R[q]);
+    re_f[(long)q * T + t] = Rf[q] = float(R[q]);
     re_d[(long)q * T + t] = R[q];
   }
+  const float4 quat = rotation_to_quaternion(Rf);
+  tile_f[tile_word(tile_tets, t, 4)] = quat.x;
+  tile_f[tile_word(tile_tets, t, 5)] = quat.y;
+  tile_f[tile_word(tile_tets, t, 6)] = quat.z;
+  tile_f[tile_word(tile_tets, t, 7)] = quat.w;
   // rest-frame displacements relative to node 0
   double d[3][3];
   for (int k = 0; k < 3; ++k) {
@@ -1234,21 +1454,33 @@ __global__ void k_orient_rhs(int T, int warp, const int4* __restrict__ tets, con
 }
 
 // FP32/FP64 apply operands b_k (k = 1..3) and (c0, c1, c2) from the init data.
-__global__ void k_prepare(int T, const double* __restrict__ Bv, const double* __restrict__ D,
-                          const double* __restrict__ V, float* b_f, float* c_f, double* b_d, double* c_d) {
+__global__ void k_prepare(int T, const int4* __restrict__ tets, const double* __restrict__ Bv,
+                          const double* __restrict__ D, const double* __restrict__ V, float* b_f, float* c_f,
+                          double* b_d, double* c_d, float* tile_f, int tile_tets) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   for (int q = 0; q < 9; ++q) {
     double val = Bv[12 * t + 3 + q];
     b_f[(long)q * T + t] = float(val);
     b_d[(long)q * T + t] = val;
+    tile_f[tile_word(tile_tets, t, 8 + q)] = float(val);
   }
   double vol = V[t];
   double c[3] = {vol * (D[3 * t] - D[3 * t + 1]), vol * D[3 * t + 1], vol * D[3 * t + 2]};
   for (int q = 0; q < 3; ++q) {
     c_f[(long)q * T + t] = float(c[q]);
     c_d[(long)q * T + t] = c[q];
+    tile_f[tile_word(tile_tets, t, 17 + q)] = float(c[q]);
   }
+  const int4 n = tets[t];
+  tile_f[tile_word(tile_tets, t, 0)] = __int_as_float(n.x);
+  tile_f[tile_word(tile_tets, t, 1)] = __int_as_float(n.y);
+  tile_f[tile_word(tile_tets, t, 2)] = __int_as_float(n.z);
+  tile_f[tile_word(tile_tets, t, 3)] = __int_as_float(n.w);
+  tile_f[tile_word(tile_tets, t, 4)] = 0.f;  // identity until the first orientation
+  tile_f[tile_word(tile_tets, t, 5)] = 0.f;
+  tile_f[tile_word(tile_tets, t, 6)] = 0.f;
+  tile_f[tile_word(tile_tets, t, 7)] = 1.f;
 }
 
 // Standalone y = A x (diagnostics and the apply-only measurement): pack, one
@@ -1376,6 +1608,7 @@ cudaError_t build_patches(Context& c, const int32_t* tets) {
   // gather (operand + 12 forces per tet)
   c.apply_smem = std::max(size_t(cap) * std::max(SmemOperand<float>::bytes, SmemOperand<double>::bytes),
                           size_t(cap) * sizeof(double4) + size_t(kPatchTets) * 12 * sizeof(double));
+  c.apply_smem = std::max(c.apply_smem, kStagedSmem);
   cudaError_t e;
   if ((e = cudaMalloc(&c.patch_node_ptr, sizeof(int) * ptr.size())) != cudaSuccess) return e;
   if ((e = cudaMalloc(&c.patch_nodes, sizeof(int) * std::max<size_t>(nodes.size(), 1))) != cudaSuccess) return e;
@@ -1405,6 +1638,19 @@ cudaError_t build_patches(Context& c, const int32_t* tets) {
   return cudaSuccess;
 }
 
+void staged_tiles(Context& c) {
+  const long T = c.T;
+  const long G = c.mf_grid > 0 ? c.mf_grid : 1;
+  // rounds of tiles per CTA at the largest tile, then the smallest tile that
+  // still covers the tets in that many rounds, rounded up to a multiple of 16
+  // tets (each word array of a tile then starts on a 64-byte boundary)
+  const long rounds = std::max(1L, (T + G * kTileMaxTets - 1) / (G * kTileMaxTets));
+  long tt = (T + G * rounds - 1) / (G * rounds);
+  tt = std::min<long>(kTileMaxTets, std::max(16L, (tt + 15) / 16 * 16));
+  c.tile_tets = int(tt);
+  c.num_tiles = int((T + tt - 1) / tt);
+}
+
 int mixed_grid_shape(Context& c, int* grid, int* block) {
   int occ32 = 0, occ64 = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_cg_mixed, kBlock, c.apply_smem);
@@ -1421,7 +1667,12 @@ int mixed_grid_shape(Context& c, int* grid, int* block) {
 cudaError_t mixed_prepare(Context& c) {
   int nb = (c.T + 255) / 256;
   if (nb < 1) nb = 1;
-  k_prepare<<<nb, 256, 0, c.stream>>>(c.T, c.Bv, c.D, c.V, c.b_f, c.c_f, c.b_d, c.c_d);
+  // padding tets of the last tile: node 0, no stiffness (never computed)
+  cudaError_t e = cudaMemsetAsync(c.tile_f, 0, sizeof(float) * kTileWords * size_t(c.tile_tets) * c.num_tiles,
+                                  c.stream);
+  if (e != cudaSuccess) return e;
+  k_prepare<<<nb, 256, 0, c.stream>>>(c.T, c.tets, c.Bv, c.D, c.V, c.b_f, c.c_f, c.b_d, c.c_d, c.tile_f,
+                                      c.tile_tets);
   return cudaGetLastError();
 }
 
@@ -1431,11 +1682,11 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
   cudaError_t e;
   if (solver == OTFEM_SOLVER_FP64) {
     k_orient_rhs<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.E, c.V, c.Bv, c.D, c.Re,
-                                           c.re_f, c.re_d, c.elastic_force);
+                                           c.re_f, c.re_d, c.elastic_force, c.tile_f, c.tile_tets);
     c.re_f32_pending = false;
   } else {
     k_orient_rhs_f32<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.b_f, c.c_f, c.re_f,
-                                               c.g_f);
+                                               c.g_f, c.tile_f, c.tile_tets);
     c.re_f32_pending = true;
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1454,7 +1705,7 @@ cudaError_t autotune_apply(Context& c) {
   if (c.T == 0) return cudaSuccess;
   int nb = (c.T + 255) / 256, nbn = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   // representative operands: identity orientations, the node positions
-  k_identity_f32<<<nb, 256, 0, c.stream>>>(c.T, c.re_f);
+  k_identity_f32<<<nb, 256, 0, c.stream>>>(c.T, c.re_f, c.tile_f, c.tile_tets);
   k_pack_operand<float4><<<nbn, 256, 0, c.stream>>>(c.N, c.fixed, c.x, c.p_f, c.p_lo, c.q_f);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -1538,6 +1789,10 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.stats = c.stats;
   a.trace = c.trace;
   set_patch_args(a, c);
+  a.tile_f = c.tile_f;
+  a.tile_tets = c.tile_tets;
+  a.num_tiles = c.num_tiles;
+  a.ordered_sums = prm.sequential_dots ? 1 : 0;
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
 }
 
@@ -1561,11 +1816,18 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
+// Standalone element-apply launches start the staged apply's tile tickets
+// at zero, as a solver launch does.
+static cudaError_t reset_tile_tickets(Context& c) {
+  return cudaMemsetAsync(&c.sync->tile_ticket, 0, sizeof(unsigned), c.stream);
+}
+
 cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps) {
   MixedArgs a;
   otfem_solver_params prm;
   otfem_default_params(&prm);
   fill_args(a, c, dt, prm);
+  if (cudaError_t e = reset_tile_tickets(c)) return e;
   for (int k = 0; k < sweeps; ++k) {
     if (solver == OTFEM_SOLVER_FP64)
       k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
@@ -1581,6 +1843,7 @@ cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass
   otfem_solver_params prm;
   otfem_default_params(&prm);
   fill_args(a, c, dt, prm);
+  if (cudaError_t e = reset_tile_tickets(c)) return e;
   int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   if (solver == OTFEM_SOLVER_FP64) {
     k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, nullptr, c.q_d);
@@ -1600,6 +1863,7 @@ cudaError_t launch_apply_operator_scratch(Context& c, int solver, double dt, dou
   otfem_solver_params prm;
   otfem_default_params(&prm);
   fill_args(a, c, dt, prm);
+  if (cudaError_t e = reset_tile_tickets(c)) return e;
   int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   if (solver == OTFEM_SOLVER_FP64) {
     double4* u = static_cast<double4*>(scratch);

@@ -6,10 +6,10 @@ matrix-free steps (OTFEM_SOLVER_MIXED, CG to rel. residual 1e-6) and then
 and the autotuner's choice.  Run it plainly first, then under ncu, e.g.
 
   python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
-  ncu --set full --clock-control none -k regex:k_apply_sweep -s 45 -c 2 -o prof \\
+  ncu --set full --clock-control none -k regex:k_apply_sweep -s 60 -c 2 -o prof \\
       python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
 
-(the autotuner at otfem_init launches 45 apply sweeps before the step).
+(the autotuner at otfem_init launches 60 apply sweeps (15 per variant) before the step).
 """
 import argparse
 import ctypes
@@ -29,7 +29,7 @@ def main():
     ap.add_argument("--dims", type=int, nargs=3, default=[128, 32, 32])
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--sweeps", type=int, default=4)
-    ap.add_argument("--variant", type=int, default=-1, help="force an element-apply variant (0..2)")
+    ap.add_argument("--variant", type=int, default=-1, help="force an element-apply variant (0..3)")
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
     build.build()
@@ -48,7 +48,7 @@ def main():
     if args.variant >= 0:
         capi.check(lib.otfem_set_apply_variant(h, args.variant))
     variant = ctypes.c_int32()
-    ms = np.zeros(3)
+    ms = np.zeros(capi.NUM_APPLY_VARIANTS)
     capi.check(lib.otfem_tuning(h, ctypes.byref(variant), ms.ctypes.data_as(dp)))
     mass = np.zeros(N)
     capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(dp), N))

@@ -165,18 +165,21 @@ def test_apply_operator_vs_assembled_reference(gpu, oracle, dims, seed):
         # the orientations of the solver's own first phase
         p = mixed(solver=solver)
         capi.check(m.lib.otfem_simulate_phase(m.h, dt, 1, ctypes.byref(p), capi.PHASE_ORIENT))
-        y = np.zeros_like(x)
-        capi.check(m.lib.otfem_apply_operator(m.h, solver, dt, 2.0, x.ctypes.data_as(_dp), y.ctypes.data_as(_dp)))
-        assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), solver
+        for variant in range(capi.NUM_APPLY_VARIANTS):
+            capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
+            y = np.zeros_like(x)
+            capi.check(m.lib.otfem_apply_operator(m.h, solver, dt, 2.0, x.ctypes.data_as(_dp),
+                                                  y.ctypes.data_as(_dp)))
+            assert np.abs(y - ref).max() <= tol * np.abs(ref).max(), (solver, variant)
 
 
 def test_every_apply_variant_solves_alike(gpu):
-    """The three element-apply variants the autotuner chooses from give the
+    """Every element-apply variant the autotuner chooses from gives the
     same solution to FP32-apply accuracy."""
     import ctypes
     g = golden("converged")
     results = []
-    for variant in range(3):
+    for variant in range(capi.NUM_APPLY_VARIANTS):
         m = GpuMesh(g["tets"], g["coord"], g["fixed"])
         m.init()
         capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
@@ -187,7 +190,7 @@ def test_every_apply_variant_solves_alike(gpu):
             assert st.rel_residual <= 1e-6
         results.append(m.get(capi.COORD))
         v = ctypes.c_int32()
-        ms = np.zeros(3)
+        ms = np.zeros(capi.NUM_APPLY_VARIANTS)
         capi.check(m.lib.otfem_tuning(m.h, ctypes.byref(v), ms.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         assert v.value == variant and (ms > 0).all()
     for x in results:
