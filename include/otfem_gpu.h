@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 2
+#define OTFEM_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -179,6 +179,64 @@ OTFEM_API int otfem_k_values(otfem_handle h, double* host_values);
 OTFEM_API int otfem_get_orientations(otfem_handle h, double* host_re);
 OTFEM_API int otfem_get_plastic(otfem_handle h, double* host_plastic);
 OTFEM_API int otfem_get_volumes(otfem_handle h, double* host_volume);
+
+/* ---- learned warm start (no counterpart in the reference) ----------------
+ * fem_conjugate_gradients.h:44-46 starts CG from the previous velocity.  With
+ * OTFEM_WARM_START_LEARNED (OTFEM_SOLVER_MIXED only) CG starts instead from
+ * v + dv_prev + net(inputs), where dv_prev is the node's velocity change of
+ * the previous step and net is a node-wise MLP (inputs: v, dv_prev, f_ext
+ * and the mean of the 9 entries of Re over the node's tets; 3 hidden layers
+ * of 64 with GELU; BF16 tensor cores, FP32 accumulation) trained on the GPU
+ * on (inputs, dv - dv_prev) pairs of converged steps.  CG runs to the same
+ * relative residual either way.
+ *
+ * Network state (OTFEM_MLP_STATE_SIZE floats): W1[64][18], b1[64],
+ * W2[64][64], b2[64], W3[64][64], b3[64], W4[3][64], b4[3] (each W as
+ * weight[out][in]), then input mean[18], input std[18], target mean[3],
+ * target std[3].  Outputs and targets are normalised by the target mean/std. */
+#define OTFEM_MLP_STATE_SIZE 9773
+typedef struct otfem_mlp_s* otfem_mlp;
+/* A network with seeded random weights, identity normalisation and room for
+ * `capacity` training samples on the current device. */
+OTFEM_API int otfem_mlp_create(int64_t capacity, uint64_t seed, otfem_mlp* out);
+OTFEM_API int otfem_mlp_destroy(otfem_mlp m);
+/* Save / load the network state (weights and normalisation); loading resets
+ * the optimiser state. */
+OTFEM_API int otfem_mlp_get_state(otfem_mlp m, float* state, int64_t n);
+OTFEM_API int otfem_mlp_set_state(otfem_mlp m, const float* state, int64_t n);
+/* Training set: otfem_set_collect(h, 1) makes every matrix-free step of h
+ * keep the network inputs of its nodes; otfem_mlp_add_samples then appends
+ * the free nodes of h's last step (each kept with probability `fraction`,
+ * by a hash of the node index and `seed`) with targets dv - dv_prev. */
+OTFEM_API int otfem_set_collect(otfem_handle h, int32_t enable);
+/* The network inputs of every node in the last step (out[num_nodes][18]). */
+OTFEM_API int otfem_get_features(otfem_handle h, float* out, int64_t n);
+OTFEM_API int otfem_mlp_add_samples(otfem_mlp m, otfem_handle h, double fraction, uint64_t seed, int64_t* total);
+OTFEM_API int otfem_mlp_num_samples(otfem_mlp m, int64_t* count);
+OTFEM_API int otfem_mlp_clear_samples(otfem_mlp m);
+/* Sets the input and target normalisation to the training set's column means
+ * and standard deviations. */
+OTFEM_API int otfem_mlp_fit_normalization(otfem_mlp m);
+/* Adam (beta 0.9, 0.999, eps 1e-8) on the mean squared normalised error over
+ * shuffled minibatches of `batch` samples; returns the mean loss of the last
+ * epoch. */
+OTFEM_API int otfem_mlp_train(otfem_mlp m, int32_t epochs, int32_t batch, double learning_rate, uint64_t seed,
+                              double* last_epoch_loss);
+/* Mean squared normalised error over the training set. */
+OTFEM_API int otfem_mlp_evaluate(otfem_mlp m, double* loss);
+/* Diagnostics: loss and its gradient w.r.t. the OTFEM_MLP_STATE_SIZE - 42
+ * weights over n host samples (inputs x[n][18], targets y[n][3]); and the
+ * de-normalised predictions y[n][3] of n host inputs. */
+OTFEM_API int otfem_mlp_gradient(otfem_mlp m, const float* x, const float* y, int64_t n, double* loss, float* grad);
+OTFEM_API int otfem_mlp_predict(otfem_mlp m, const float* x, int64_t n, float* y);
+/* Attaches a network to a mesh for OTFEM_WARM_START_LEARNED (NULL detaches).
+ * The network must outlive its use and must not be trained while steps
+ * that use it are in flight. */
+OTFEM_API int otfem_set_mlp(otfem_handle h, otfem_mlp m);
+/* Passes (0..64) of 1-ring mean aggregation over the network's correction
+ * net(inputs) before it enters the initial guess: each pass replaces a
+ * node's correction by the mean over its tets of the tet's node mean. */
+OTFEM_API int otfem_set_warm_start_smoothing(otfem_handle h, int32_t passes);
 
 /* ---- host staging (no counterpart in the reference) ---------------------- */
 /* Page-locked host memory for fast transfers (used by the drop-in headers). */

@@ -28,6 +28,9 @@ SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
 WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2
 NUM_APPLY_VARIANTS = 4
+# learned warm start: network state = 9731 weights + 42 normalisation values
+MLP_STATE_SIZE = 9773
+MLP_NUM_WEIGHTS = 9731
 
 
 class SolverParams(ctypes.Structure):
@@ -77,6 +80,7 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
+_fp = ctypes.POINTER(ctypes.c_float)
 _h = ctypes.c_void_p
 
 # every exported symbol with (restype, argtypes); test_abi checks this list
@@ -120,6 +124,23 @@ SIGNATURES = {
     "otfem_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),
     "otfem_solver_shape": (ctypes.c_int, [_h, _i32p, _i32p]),
+    "otfem_mlp_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    "otfem_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "otfem_mlp_get_state": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_int64]),
+    "otfem_mlp_set_state": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_int64]),
+    "otfem_set_collect": (ctypes.c_int, [_h, ctypes.c_int32]),
+    "otfem_get_features": (ctypes.c_int, [_h, _fp, ctypes.c_int64]),
+    "otfem_mlp_add_samples": (ctypes.c_int, [ctypes.c_void_p, _h, ctypes.c_double, ctypes.c_uint64, _i64p]),
+    "otfem_mlp_num_samples": (ctypes.c_int, [ctypes.c_void_p, _i64p]),
+    "otfem_mlp_clear_samples": (ctypes.c_int, [ctypes.c_void_p]),
+    "otfem_mlp_fit_normalization": (ctypes.c_int, [ctypes.c_void_p]),
+    "otfem_mlp_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                       ctypes.c_uint64, _dp]),
+    "otfem_mlp_evaluate": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "otfem_mlp_gradient": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, ctypes.c_int64, _dp, _fp]),
+    "otfem_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_int64, _fp]),
+    "otfem_set_mlp": (ctypes.c_int, [_h, ctypes.c_void_p]),
+    "otfem_set_warm_start_smoothing": (ctypes.c_int, [_h, ctypes.c_int32]),
 }
 
 

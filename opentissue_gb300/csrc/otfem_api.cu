@@ -58,7 +58,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -83,7 +83,7 @@ double* node_field(Context& c, int field) {
 
 int64_t field_count(Context& c, int field) { return field == OTFEM_MASS ? int64_t(c.N) : 3 * int64_t(c.N); }
 
-int check_params(const otfem_solver_params& p) {
+int check_params(const Context& c, const otfem_solver_params& p) {
   if (p.solver < OTFEM_SOLVER_REFERENCE || p.solver > OTFEM_SOLVER_FP64)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown solver");
   if (p.max_iterations < 0 || p.min_iterations < 0)
@@ -92,9 +92,20 @@ int check_params(const otfem_solver_params& p) {
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
   if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
-  if (p.warm_start == OTFEM_WARM_START_LEARNED)
-    return fail(OTFEM_ERR_UNSUPPORTED, "learned warm start needs an attached warm-start network");
+  if (p.warm_start == OTFEM_WARM_START_LEARNED && p.solver != OTFEM_SOLVER_MIXED)
+    return fail(OTFEM_ERR_UNSUPPORTED, "the learned warm start runs with OTFEM_SOLVER_MIXED");
+  if (p.warm_start == OTFEM_WARM_START_LEARNED && !c.mlp)
+    return fail(OTFEM_ERR_NOT_INITIALIZED, "learned warm start without a network (otfem_set_mlp)");
   return OTFEM_OK;
+}
+
+// After the orientation phase of a matrix-free step: the network inputs of
+// the nodes (when collecting training samples) and the learned initial guess.
+cudaError_t launch_warm_start(Context& c, const otfem_solver_params& p) {
+  const bool predict = p.warm_start == OTFEM_WARM_START_LEARNED;
+  c.features_valid = c.collect != 0;
+  if (!predict && !c.collect) return cudaSuccess;
+  return otfem::launch_node_features(c, predict);
 }
 
 // Enqueues one step on c.stream (no host synchronisation).
@@ -112,21 +123,24 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
     if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
   } else {
     if ((e = otfem::launch_mixed_orient(c, dt, warp, p.solver)) != cudaSuccess) return e;
+    if ((e = launch_warm_start(c, p)) != cudaSuccess) return e;
     if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return e;
   }
   return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
 }
 
-std::string step_key(double dt, bool warp, const otfem_solver_params& p) {
-  char buf[256];
-  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d", p.solver, dt, int(warp), p.mass_damping,
-           p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots, p.warm_start);
+std::string step_key(const Context& c, double dt, bool warp, const otfem_solver_params& p) {
+  char buf[320];
+  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d|%p|%d|%d", p.solver, dt, int(warp), p.mass_damping,
+           p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots, p.warm_start,
+           static_cast<void*>(c.mlp), c.collect, c.warm_smoothing);
   return buf;
 }
 
 int kernels_per_step(const Context& c, const otfem_solver_params& p) {
   if (p.solver == OTFEM_SOLVER_REFERENCE) return 1 + 2 + 2 + 1 + (1 + 5 * p.max_iterations + 1) + 1;
-  return 2 + (c.plastic_active ? 2 : 0);
+  const bool features = p.warm_start == OTFEM_WARM_START_LEARNED || c.collect;
+  return 2 + (c.plastic_active ? 2 : 0) + (features ? 1 : 0);
 }
 
 }  // namespace
@@ -237,6 +251,8 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.p_lo, N);
   OT_ALLOC(c.v_lo, N);
   OT_ALLOC(c.r_f, N);
+  OT_ALLOC(c.dv_last, N);
+  OT_ALLOC(c.warm_dv, N);
   OT_ALLOC(c.g_f, 4 * T);
   OT_ALLOC(c.q_d, N);
   OT_ALLOC(c.p_d4, N);
@@ -326,6 +342,9 @@ int otfem_init(otfem_handle h, double young, double poisson, double density, dou
   // clear_stiffness_assembly (fem_init.h:60)
   OT_CUDA(cudaMemsetAsync(c.f0, 0, sizeof(double) * 3 * size_t(c.N), c.stream));
   if (c.k_assembled) OT_CUDA(cudaMemsetAsync(c.K, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream));
+  // no velocity history yet (learned warm start)
+  OT_CUDA(cudaMemsetAsync(c.dv_last, 0, sizeof(float4) * size_t(c.N), c.stream));
+  OT_CUDA(cudaMemsetAsync(c.warm_dv, 0, sizeof(float4) * size_t(c.N), c.stream));
   // choose the element-apply variant for this mesh
   if ((e = otfem::autotune_apply(c)) != cudaSuccess) return cuda_fail(e, "autotune");
   std::vector<double> vol(size_t(c.T));
@@ -392,12 +411,12 @@ int otfem_simulate_ex(otfem_handle h, double dt, int warp, const otfem_solver_pa
   otfem_solver_params p;
   if (params) p = *params;
   else otfem_default_params(&p);
-  int rc = check_params(p);
+  int rc = check_params(c, p);
   if (rc != OTFEM_OK) return rc;
   bool use_warp = warp != 0;
   cudaError_t e;
   if (p.graph) {
-    std::string key = step_key(dt, use_warp, p);
+    std::string key = step_key(c, dt, use_warp, p);
     if (!c.graph || key != c.graph_key) {
       if (c.graph) {
         cudaGraphExecDestroy(c.graph);
@@ -435,13 +454,15 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
   otfem_solver_params p;
   if (params) p = *params;
   else otfem_default_params(&p);
-  int rc = check_params(p);
+  int rc = check_params(c, p);
   if (rc != OTFEM_OK) return rc;
   if (p.solver == OTFEM_SOLVER_REFERENCE) return fail(OTFEM_ERR_UNSUPPORTED, "phases exist for the matrix-free solvers");
   cudaError_t e;
   if (phase == OTFEM_PHASE_ORIENT) {
     if ((e = otfem::launch_mixed_orient(c, dt, warp != 0, p.solver)) != cudaSuccess) return cuda_fail(e, "orient phase");
     c.launches += 1 + (c.plastic_active ? 2 : 0);
+    if ((e = launch_warm_start(c, p)) != cudaSuccess) return cuda_fail(e, "warm start");
+    if (p.warm_start == OTFEM_WARM_START_LEARNED || c.collect) c.launches += 1;
   } else if (phase == OTFEM_PHASE_SOLVE) {
     if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return cuda_fail(e, "solve phase");
     OT_CUDA(cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream));

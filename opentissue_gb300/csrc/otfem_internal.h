@@ -126,6 +126,18 @@ struct Context {
   // c0..c2), copied to shared memory whole by the bulk-copy engine
   float* tile_f = nullptr;
   int num_tiles = 0, tile_tets = 0;
+  // learned warm start: the velocity change of the last matrix-free step,
+  // the network's initial guess for the next, the per-node network inputs
+  // of the last step (kept when collecting training samples) and the
+  // attached network
+  float4* dv_last = nullptr;      // N (w unused)
+  float4* warm_dv = nullptr;      // N
+  float4* warm_tmp = nullptr;     // N, allocated with smoothing passes
+  int warm_smoothing = 0;         // 1-ring mean passes over the network's correction
+  float* features = nullptr;      // N x kFeatureStride, allocated when collecting
+  int collect = 0;
+  bool features_valid = false;    // c.features hold the inputs of the last step
+  struct otfem_mlp_s* mlp = nullptr;
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
   double apply_ms[4] = {0, 0, 0, 0};  // measured time of one sweep per variant
@@ -172,6 +184,14 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver);
 // fastest in c.apply_variant (synchronises the stream).
 cudaError_t autotune_apply(Context& c);
 constexpr int kNumApplyVariants = OTFEM_NUM_APPLY_VARIANTS;
+// Learned warm start: per-node inputs (v, previous dv, f_ext, 1-ring mean
+// of the 9 entries of Re) stored with this stride (floats).
+constexpr int kFeatures = 18;
+constexpr int kFeatureStride = 20;
+// Computes the network inputs of every node for the coming solve (into
+// c.features when collecting) and, with predict, the initial guess c.warm_dv
+// from the attached network.  After the orientation phase.
+cudaError_t launch_node_features(Context& c, bool predict);
 // Staged-apply tiles: at most kTileMaxTets tets of kTileWords 32-bit words.
 constexpr int kTileMaxTets = 512;
 constexpr int kTileWords = 20;

@@ -116,6 +116,8 @@ struct MixedArgs {
   const float* tile_f;                  // staged apply tiles (see Context::tile_f)
   int tile_tets, num_tiles;
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
+  const float4* warm_dv;                // learned initial guess v + warm_dv (null: v)
+  float4* dv_last;                      // out: v_new - v_old per free node
   long long spin_limit;
 };
 
@@ -454,12 +456,21 @@ struct FinAlphaBeta {
   }
 };
 
+// The same with the exact r.r as the fourth total.  The previous
+// iteration's estimate of this r.r (prev_est < 0: none) checks the
+// recurrence: when they disagree by more than a quarter, or on `restart`,
+// beta = 0 restarts the search direction from the residual (steepest
+// descent, which cannot grow the error), instead of letting an inaccurate
+// recurrence near the precision floor amplify itself.
 struct FinAlphaBetaExact {
+  double prev_est;
+  bool restart;
   __device__ void operator()(const double* t, double* o) const {
     FinAlphaBeta f;
     f.rho = t[3];
     f(t, o);
     if (o[3] == 0.0 && !isfinite(t[3])) o[3] = 1.0;
+    if (restart || (prev_est >= 0.0 && fabs(prev_est - t[3]) > 0.25 * t[3])) o[1] = 0.0;
   }
 };
 
@@ -987,7 +998,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     }
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
-    // never accumulated (w = 0).
+    // never accumulated (w = 0).  A learned warm start moves the initial
+    // guess of free nodes by the predicted velocity change.
+    if (a.warm_dv && !fx) {
+      const float4 w = a.warm_dv[i];
+      vi[0] += double(w.x), vi[1] += double(w.y), vi[2] += double(w.z);
+    }
     store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     a.q_f[i] = zero4;
   }
@@ -1023,6 +1039,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const double rho0 = rho;
   int it = 0, applies = 1;
   bool converged = rho <= thresh;
+  // recurrence check and restarts (FinAlphaBetaExact); stagnation of the
+  // true residual at the refreshes ends the solve unconverged
+  double prev_est = -1.0, best_true = rho0;
+  bool restart = false;
+  int stalls = 0;
 
   while (!converged && it < a.max_it) {
     // q += dt^2 K' p
@@ -1045,7 +1066,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
     double sc[4];
-    if (!grid_reduce<DF, 4, 4>(a, s4, sc, round, FinAlphaBetaExact())) return;
+    if (!grid_reduce<DF, 4, 4>(a, s4, sc, round, FinAlphaBetaExact{prev_est, restart})) return;
+    prev_est = sc[2];
+    restart = false;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
     if (sc[3] != 0.0) {
       // 1: NaN/Inf in the system (e.g. a non-finite force), an error;
@@ -1101,20 +1124,34 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
         tr[0] = df_add(tr[0], DF{rx * rx + ry * ry + rz * rz, 0.f});
       }
       if (!grid_reduce<DF, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
+      // the true residual well above the recursive one: the recurrence has
+      // decoupled from the system, restart the direction
+      restart = tot[0] > 4.0 * sc[2];
+      prev_est = -1.0;
       rho = tot[0];
+      if (rho < best_true) {
+        best_true = rho;
+        stalls = 0;
+      } else if (++stalls >= 3) {
+        break;  // at the precision floor: no progress over three refreshes
+      }
     }
     converged = rho <= thresh;
   }
 
-  // v back to FP64; position_update (fem_position_update.h:25-39)
+  // v back to FP64; position_update (fem_position_update.h:25-39); the
+  // velocity change is kept for the learned warm start
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) continue;
     float4 vh = a.v_f[i], vl = a.v_lo[i];
     double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
+    float dv[3];
     for (int c = 0; c < 3; ++c) {
+      dv[c] = float(v3[c] - a.v[3 * i + c]);
       a.v[3 * i + c] = v3[c];
       a.x[3 * i + c] += v3[c] * a.dt;
     }
+    a.dv_last[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
 }
@@ -1793,6 +1830,8 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.tile_tets = c.tile_tets;
   a.num_tiles = c.num_tiles;
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
+  a.warm_dv = prm.warm_start == OTFEM_WARM_START_LEARNED ? c.warm_dv : nullptr;
+  a.dv_last = c.dv_last;
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
 }
 

@@ -195,3 +195,23 @@ def test_every_apply_variant_solves_alike(gpu):
         assert v.value == variant and (ms > 0).all()
     for x in results:
         assert rel_pos_err(x, g["x_5"], g["coord"]) < POS_TOL
+
+
+def test_tolerance_below_the_precision_floor_ends_unconverged(gpu):
+    """A tolerance the FP32 apply cannot reach: the solve stops at the floor
+    with OTFEM_WARN_NOT_CONVERGED and a finite, small true residual (the
+    recurrence check restarts the direction instead of letting it grow)."""
+    tets, coord, fixed = beam(8, 3, 4, jitter_seed=8)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    mass = m.get(capi.MASS)
+    for variant in range(capi.NUM_APPLY_VARIANTS):
+        capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
+        m.set(capi.F_EXTERNAL, gravity_force(mass, fixed))
+        rc, st = m.step(0.01, True, mixed(rtol=1e-10, max_iterations=3000), check=False)
+        assert rc in (capi.OK, capi.WARN_NOT_CONVERGED), (variant, rc)
+        # the floor of the FP32 accumulation of node forces, far below the
+        # divergence (1e18) the unchecked recurrence reached
+        assert np.isfinite(st.rel_residual) and st.rel_residual < 1e-4, (variant, st.rel_residual)
+        assert st.iterations < 3000
+    m.close()

@@ -1,0 +1,256 @@
+"""Learned warm start: the network kernels (forward, backward, Adam, inputs)
+against the CPU oracle (oracle/mlp_oracle.py), and the warm start in the
+matrix-free solver against the plain previous-velocity start."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import GpuMesh, beam, gravity_force
+from oracle import mlp_oracle as mo
+from opentissue_gb300 import capi
+
+# ---- the oracle itself (CPU) ------------------------------------------------
+
+
+def random_state(rng, scale_out=1.0):
+    w = {}
+    for name, shape in mo.SHAPES:
+        fan_in = shape[1] if len(shape) == 2 else 64
+        w[name] = rng.uniform(-1, 1, shape) / np.sqrt(fan_in)
+    w["W4"] *= scale_out
+    norm = {"mu_x": rng.normal(size=18) * 0.1, "sd_x": rng.uniform(0.5, 2.0, 18),
+            "mu_y": rng.normal(size=3) * 0.1, "sd_y": rng.uniform(0.5, 2.0, 3)}
+    return mo.pack(w, norm)
+
+
+def test_bf16_rounds_to_nearest_even():
+    x = np.array([1.0, 1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, 1.0 + 2.0 ** -7, -2.5, 3.0e-3], np.float32)
+    r = mo.bf16(x)
+    assert r[0] == 1.0
+    assert r[1] == 1.0                      # tie -> even
+    assert r[2] == np.float32(1.0 + 2.0 ** -6)  # tie -> even (up)
+    assert r[3] == np.float32(1.0 + 2.0 ** -7)  # representable
+    assert r[4] == -2.5
+    assert abs(r[5] - 3.0e-3) <= 3.0e-3 * 2.0 ** -8
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(1)
+    state = random_state(rng).astype(np.float64)
+    x = rng.normal(size=(37, 18))
+    y = rng.normal(size=(37, 3))
+    loss, g = mo.loss_and_gradient(state, x, y, exact=True)
+    idx = rng.choice(mo.NUM_WEIGHTS, 60, replace=False)
+    h = 1e-6
+    for k in idx:
+        sp, sm = state.copy(), state.copy()
+        sp[k] += h
+        sm[k] -= h
+        fd = (mo.loss_and_gradient(sp, x, y, exact=True)[0] - mo.loss_and_gradient(sm, x, y, exact=True)[0]) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(fd)) + 1e-8, (k, fd, g[k])
+
+
+def test_oracle_bf16_gradient_close_to_exact():
+    rng = np.random.default_rng(2)
+    state = random_state(rng)
+    x = rng.normal(size=(500, 18)).astype(np.float32)
+    y = rng.normal(size=(500, 3)).astype(np.float32)
+    l32, g32 = mo.loss_and_gradient(state, x, y)
+    l64, g64 = mo.loss_and_gradient(state.astype(np.float64), x, y, exact=True)
+    assert abs(l32 - l64) <= 2e-2 * l64
+    assert np.linalg.norm(g32 - g64) <= 5e-2 * np.linalg.norm(g64)
+
+
+# ---- GPU kernels against the oracle -------------------------------------------
+
+
+@pytest.fixture()
+def net(gpu):
+    from opentissue_gb300.warmstart import WarmStartNet
+    n = WarmStartNet(capacity=1 << 16, seed=7)
+    yield n
+    n.close()
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_matches_oracle(net):
+    rng = np.random.default_rng(3)
+    state = random_state(rng)
+    net.set_state(state)
+    assert np.array_equal(net.state(), state)
+    for n in (1000, 64, 5):  # not a multiple of the 64-sample chunk, one chunk, a partial one
+        x = (rng.normal(size=(n, 18)) * 1.5).astype(np.float32)
+        y = rng.normal(size=(n, 3)).astype(np.float32)
+        loss, g = net.gradient(x, y)
+        lo, go = mo.loss_and_gradient(state, x, y)
+        assert abs(loss - lo) <= 1e-4 * lo, (n, loss, lo)
+        # same roundings; only FP32 summation order differs (and the odd
+        # BF16 rounding of a value near a tie)
+        assert np.linalg.norm(g - go) <= 2e-3 * np.linalg.norm(go), n
+        assert np.allclose(g, go, rtol=5e-2, atol=2e-3 * np.abs(go).max()), n
+        # and the mathematical gradient
+        _, ge = mo.loss_and_gradient(state.astype(np.float64), x, y, exact=True)
+        assert np.linalg.norm(g - ge) <= 5e-2 * np.linalg.norm(ge), n
+
+
+@pytest.mark.gpu
+def test_gpu_predict_matches_oracle(net):
+    rng = np.random.default_rng(4)
+    state = random_state(rng)
+    net.set_state(state)
+    x = rng.normal(size=(777, 18)).astype(np.float32)
+    y = net.predict(x)
+    yo = mo.predict(state, x)
+    err = np.abs(y - yo) / np.abs(yo).max()
+    # same roundings; an activation within FP32 noise of a BF16 tie can round
+    # the other way and move one output by ~1e-4 of the scale
+    assert np.quantile(err, 0.99) <= 1e-5
+    assert err.max() <= 1e-3
+
+
+@pytest.mark.gpu
+def test_gpu_train_step_is_adam_on_the_gradient(gpu):
+    """otfem_mlp_train (one epoch, one batch) applies exactly one Adam step
+    to the gradient of the collected samples."""
+    from opentissue_gb300.warmstart import WarmStartNet, node_features
+    tets, coord, fixed = beam(6, 3, 3, jitter_seed=8)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    mass = m.get(capi.MASS)
+    WarmStartNet.collect(m.h)
+    net = WarmStartNet(capacity=4096, seed=9)
+    p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6)
+    for s in range(3):
+        m.set(capi.F_EXTERNAL, gravity_force(mass, fixed))
+        m.step(0.01, True, p)
+        net.add_samples(m.h)
+    assert net.num_samples() == 3 * int((fixed == 0).sum())
+    net.fit_normalization()
+    state0 = net.state()
+    # a training set of known content: the free nodes of one more step
+    net.clear_samples()
+    m.set(capi.F_EXTERNAL, gravity_force(mass, fixed))
+    v_before = m.get(capi.VELOCITY)
+    m.step(0.01, True, p)
+    feats = node_features(m.h, m.N)
+    v_after = m.get(capi.VELOCITY)
+    net.add_samples(m.h)
+    free = fixed == 0
+    x = feats[free]
+    y = ((v_after - v_before)[free] - feats[free, 3:6]).astype(np.float32)
+    _, g = net.gradient(x, y)
+    net.train(1, batch=1 << 20, lr=1e-3, seed=1)
+    state1 = net.state()
+    p1, _, _ = mo.adam_step(state0, g, np.zeros(mo.NUM_WEIGHTS, np.float32), np.zeros(mo.NUM_WEIGHTS, np.float32), 1,
+                            1e-3)
+    clear = np.abs(g) > 1e-5 * np.abs(g).max()
+    assert np.allclose(state1[:mo.NUM_WEIGHTS][clear], p1[:mo.NUM_WEIGHTS][clear], rtol=0, atol=2e-5)
+    net.close()
+    m.close()
+
+
+@pytest.mark.gpu
+def test_gpu_node_features_match_oracle(gpu):
+    from opentissue_gb300.warmstart import WarmStartNet, node_features
+    tets, coord, fixed = beam(8, 3, 4, jitter_seed=10)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    mass = m.get(capi.MASS)
+    f = gravity_force(mass, fixed)
+    WarmStartNet.collect(m.h)
+    p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6)
+    m.set(capi.F_EXTERNAL, f)
+    m.step(0.01, True, p)
+    v1 = m.get(capi.VELOCITY)
+    f2 = f * 1.5
+    m.set(capi.F_EXTERNAL, f2)
+    m.step(0.01, True, p)
+    feats = node_features(m.h, m.N)
+    re = m.re().reshape(-1, 9)  # the orientations of step 2
+    ref = mo.node_features(tets, v1, v1 - 0.0, f2, re)
+    assert np.allclose(feats, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max(axis=0))
+    m.close()
+
+
+@pytest.mark.gpu
+def test_learned_start_needs_a_network(gpu):
+    tets, coord, fixed = beam(4, 2, 2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    p = capi.default_params(solver=capi.SOLVER_MIXED, warm_start=capi.WARM_START_LEARNED)
+    rc, _ = m.step(0.01, True, p, check=False)
+    assert rc == capi.ERR_NOT_INITIALIZED
+    p = capi.default_params(solver=capi.SOLVER_FP64, warm_start=capi.WARM_START_LEARNED)
+    rc, _ = m.step(0.01, True, p, check=False)
+    assert rc == capi.ERR_UNSUPPORTED
+    m.close()
+
+
+# ---- the warm start in the solver ---------------------------------------------
+
+
+def tip_load(coord, I, J, K, amp, freq, direction, t):
+    n = coord.shape[0]
+    tip = np.arange(n) >= I * (J + 1) * (K + 1)
+    f = np.zeros((n, 3))
+    f[tip] = amp * np.sin(2 * np.pi * freq * t) * np.asarray(direction) / tip.sum()
+    return f
+
+
+def run_loaded(m, dims, steps, params, amp, freq, direction, net=None, dt=0.01):
+    I, J, K = dims
+    mass = m.get(capi.MASS)
+    its, xs = [], []
+    for s in range(steps):
+        f = gravity_force(mass, m.fixed) + tip_load(m.coord, I, J, K, amp, freq, direction, s * dt)
+        m.set(capi.F_EXTERNAL, f)
+        _, st = m.step(dt, True, params)
+        assert st.rel_residual <= 1e-6
+        its.append(st.iterations)
+        xs.append(m.get(capi.COORD))
+        if net is not None:
+            net.add_samples(m.h)
+    return np.array(its), xs
+
+
+@pytest.mark.gpu
+def test_learned_warm_start_cuts_iterations_at_equal_accuracy(gpu):
+    from opentissue_gb300.warmstart import WarmStartNet
+    dims = (24, 6, 6)
+    tets, coord, fixed = beam(*dims, jitter_seed=11)
+    plain = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6)
+    learned = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6,
+                                  warm_start=capi.WARM_START_LEARNED)
+    net = WarmStartNet(capacity=1 << 18, seed=12)
+    # training data: plain solver trajectories under two loads
+    for amp, freq, d in ((60.0, 1.5, (0.0, -1.0, 0.3)), (90.0, 3.0, (0.2, 0.6, -1.0))):
+        m = GpuMesh(tets, coord, fixed)
+        m.init()
+        WarmStartNet.collect(m.h)
+        run_loaded(m, dims, 60, plain, amp, freq, d, net=net)
+        m.close()
+    assert net.num_samples() > 100000
+    net.fit_normalization()
+    before = net.evaluate()
+    net.train(40, batch=8192, lr=1e-3, seed=3)
+    after = net.evaluate()
+    assert after < 0.5 * before, (before, after)
+    # a load not in the training set
+    amp, freq, d = 75.0, 2.2, (0.0, -0.8, -0.6)
+    m0 = GpuMesh(tets, coord, fixed)
+    m0.init()
+    its0, x0 = run_loaded(m0, dims, 50, plain, amp, freq, d)
+    m1 = GpuMesh(tets, coord, fixed)
+    m1.init()
+    net.attach(m1.h)
+    its1, x1 = run_loaded(m1, dims, 50, learned, amp, freq, d)
+    # same answer: both solves stop at rel. residual 1e-6
+    for a, b in zip(x1, x0):
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b - coord).max()
+    # fewer iterations after the first steps
+    assert its1[5:].mean() < 0.9 * its0[5:].mean(), (its0.mean(), its1.mean())
+    net.detach(m1.h)
+    m0.close()
+    m1.close()
+    net.close()
