@@ -7,11 +7,18 @@ x = 0 face fixed, E = 5e5 Pa, nu = 0.33, rho = 1000 kg/m^3, mass damping 2.0,
 dt = 0.01 s, gravity -9.81 in y, stiffness warping on, CG to relative
 residual 1e-6.  A "step" is one fem::simulate time step of the whole mesh.
 
-Metric: tet-steps/s = tets x steps / seconds.  `value` is measured with the
-mesh resident in HBM (device-side CUDA events around each step, L2 flushed
-between steps); `e2e` goes through the C ABI with host buffers: each step
-uploads coord, velocity and f_external and downloads coord and velocity, as
-the drop-in fem::simulate does.
+Metric: tet-steps/s = tets x steps / seconds with the learned warm start,
+next to the plain CG (previous-velocity start) on the same trajectory.  The
+run first builds the network's training set with the plain solver on beams
+of the workload's family (other jitter seeds; gravity, every other beam
+with a sinusoidal tip load; 2M node samples) and trains it on the GPU
+(Adam, lr 1e-3, batch 65,536, 60 epochs); both are timed outside the
+measured steps and reported in config.training.
+
+`value` is measured with the mesh resident in HBM (device-side CUDA events
+around each step, L2 flushed between steps); `e2e` goes through the C ABI
+with host buffers: each step uploads coord, velocity and f_external and
+downloads coord and velocity, as the drop-in fem::simulate does.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 With N > 1 (torchrun), every rank runs an independent replica of the
@@ -53,11 +60,11 @@ BYTES_PER_NODE_ITER = 120
 L2_FLUSH_BYTES = 512 << 20
 
 
-def build_mesh():
+def build_mesh(seed=None):
     from opentissue_gb300.fem import generate_blocks
     w = WORKLOAD
     tets, coord = generate_blocks(w["I"], w["J"], w["K"], w["edge"], w["edge"], w["edge"])
-    rng = np.random.default_rng(w["seed"])
+    rng = np.random.default_rng(w["seed"] if seed is None else seed)
     coord = coord + rng.uniform(-w["jitter"] * w["edge"] / 0.1, w["jitter"] * w["edge"] / 0.1, coord.shape)
     fixed = (np.arange(coord.shape[0]) < (w["J"] + 1) * (w["K"] + 1)).astype(np.uint8)
     return tets, coord, fixed
@@ -193,6 +200,79 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def train_warm_start(lib, capi, stream, args, rng):
+    """Training set and training of the learned warm start (the network of
+    the metric): (inputs, dv - dv_prev) pairs of the plain solver on beams of
+    the workload's family (other jitter seeds; gravity, half of them with a
+    sinusoidal tip load), Adam lr 1e-3, batch 65,536.  Returns the network
+    and a summary."""
+    from opentissue_gb300.warmstart import WarmStartNet
+    w = WORKLOAD
+    n_target = args.train_samples
+    net = WarmStartNet(capacity=n_target, seed=args.seed)
+    params = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                 max_iterations=5000, refresh_period=16)
+    t0 = time.perf_counter()
+    beams = 0
+    while net.num_samples() < n_target and beams < 64:
+        tets, coord, fixed = build_mesh(seed=int(rng.integers(1 << 30)))
+        h = make_handle(lib, capi, tets, coord, fixed, stream)
+        WarmStartNet.collect(h)
+        mass = get_mass(lib, capi, h, coord.shape[0])
+        amp = 0.0 if beams % 2 == 0 else float(rng.uniform(0, 100))
+        freq, d = float(rng.uniform(0.5, 5)), rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        free = int((fixed == 0).sum())
+        steps = args.train_steps
+        frac = min(1.0, n_target / (2 * steps * free))
+        for s in range(steps):
+            f = gravity(mass, fixed) + tip_load(coord, amp, freq, d, s * w["dt"])
+            capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(_dp), f.size))
+            capi.check(lib.otfem_simulate_ex(h, w["dt"], 1, ctypes.byref(params), None))
+            net.add_samples(h, fraction=frac, seed=int(rng.integers(1 << 62)))
+        capi.check(lib.otfem_destroy(h))
+        beams += 1
+    gen_s = time.perf_counter() - t0
+    net.fit_normalization()
+    loss0 = net.evaluate()
+    t0 = time.perf_counter()
+    loss = net.train(args.train_epochs, batch=65536, lr=1e-3, seed=args.seed)
+    train_s = time.perf_counter() - t0
+    return net, {"samples": net.num_samples(), "beams": beams, "epochs": args.train_epochs, "batch": 65536,
+                 "lr": 1e-3, "loss_initial": loss0, "loss_final": loss, "generate_s": round(gen_s, 2),
+                 "train_s": round(train_s, 2)}
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def make_handle(lib, capi, tets, coord, fixed, stream):
+    w = WORKLOAD
+    desc = capi.MeshDesc(coord.shape[0], tets.shape[0], tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                         coord.ctypes.data_as(_dp), coord.ctypes.data_as(_dp),
+                         fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    h = ctypes.c_void_p()
+    capi.check(lib.otfem_create(ctypes.byref(desc), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
+    capi.check(lib.otfem_init(h, w["young"], w["poisson"], w["density"], 1e30, 0.0, 0.0))
+    return h
+
+
+def get_mass(lib, capi, h, N):
+    mass = np.zeros(N)
+    capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(_dp), N))
+    return mass
+
+
+def tip_load(coord, amp, freq, d, t):
+    w = WORKLOAD
+    f = np.zeros_like(coord)
+    if amp == 0.0:
+        return f
+    tip = np.arange(coord.shape[0]) >= w["I"] * (w["J"] + 1) * (w["K"] + 1)
+    f[tip] = amp * np.sin(2 * np.pi * freq * t) * d / tip.sum()
+    return f
+
+
 def run_ours(args, world, rank, local):
     import torch
     from opentissue_gb300 import build as ext_build
@@ -202,76 +282,85 @@ def run_ours(args, world, rank, local):
     lib = capi.lib()
     torch.cuda.set_device(local)
     stream = torch.cuda.Stream()
+    rng = np.random.default_rng(args.seed + rank)
+    w = WORKLOAD
+    net, train_info = train_warm_start(lib, capi, stream, args, rng)
+
     tets, coord, fixed = build_mesh()
     T, N = tets.shape[0], coord.shape[0]
     n_free = int((fixed == 0).sum())
-    w = WORKLOAD
-    _dp = ctypes.POINTER(ctypes.c_double)
-    desc = capi.MeshDesc(N, T, tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), coord.ctypes.data_as(_dp),
-                         coord.ctypes.data_as(_dp), fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
-    h = ctypes.c_void_p()
-    capi.check(lib.otfem_create(ctypes.byref(desc), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
-    capi.check(lib.otfem_init(h, w["young"], w["poisson"], w["density"], 1e30, 0.0, 0.0))
-    mass = np.zeros(N)
-    capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(_dp), N))
-    fext = gravity(mass, fixed)
-    capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, fext.ctypes.data_as(_dp), fext.size))
-    params = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                 max_iterations=5000, refresh_period=16)
+    plain = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                max_iterations=5000, refresh_period=16)
+    learned = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                  max_iterations=5000, refresh_period=16, warm_start=capi.WARM_START_LEARNED)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    stats = capi.StepStats()
 
     def flush_l2():
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
 
-    def step():
-        capi.check(lib.otfem_simulate_ex(h, w["dt"], 1, ctypes.byref(params), None))
+    def timed_run(h, params):
+        """W warm-up steps, then K steps timed on the device (L2 flushed
+        before each); the workload's gravity load."""
+        mass = get_mass(lib, capi, h, N)
+        fext = gravity(mass, fixed)
+        capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, fext.ctypes.data_as(_dp), fext.size))
+        stats = capi.StepStats()
+        for _ in range(args.warmup):
+            capi.check(lib.otfem_simulate_ex(h, w["dt"], 1, ctypes.byref(params), None))
+        torch.cuda.synchronize()
+        n0 = ctypes.c_int64()
+        capi.check(lib.otfem_launch_count(h, ctypes.byref(n0)))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        its, res, applies = [], [], []
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush_l2()
+            ev[k][0].record(stream)
+            capi.check(lib.otfem_simulate_ex(h, w["dt"], 1, ctypes.byref(params), None))
+            ev[k][1].record(stream)
+            capi.check(lib.otfem_last_stats(h, ctypes.byref(stats)))
+            its.append(stats.iterations)
+            res.append(stats.rel_residual)
+            applies.append(stats.applies)
+        torch.cuda.synchronize()
+        dist_barrier(world)
+        n1 = ctypes.c_int64()
+        capi.check(lib.otfem_launch_count(h, ctypes.byref(n1)))
+        dev_s = dist_max(world, sum(a.elapsed_time(b) for a, b in ev) / 1e3)
+        x = np.zeros((N, 3))
+        capi.check(lib.otfem_get_nodes(h, capi.COORD, x.ctypes.data_as(_dp), x.size))
+        return {"dev_s": dev_s, "its": its, "res": res, "applies": applies, "launches": int(n1.value - n0.value),
+                "x": x, "fext": fext}
 
-    for _ in range(args.warmup):
-        step()
-    capi.check(lib.otfem_last_stats(h, ctypes.byref(stats)))
-    torch.cuda.synchronize()
-
-    # ---- device-resident timed region --------------------------------------
-    n0 = ctypes.c_int64()
-    capi.check(lib.otfem_launch_count(h, ctypes.byref(n0)))
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    its, res, applies = [], [], []
+    # ---- plain CG (previous velocity) and learned warm start, same trajectory
+    h_plain = make_handle(lib, capi, tets, coord, fixed, stream)
+    h_learn = make_handle(lib, capi, tets, coord, fixed, stream)
+    net.attach(h_learn)
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    dist_barrier(world)
-    torch.cuda.synchronize()
-    for k in range(args.steps):
-        flush_l2()
-        ev[k][0].record(stream)
-        step()
-        ev[k][1].record(stream)
-        capi.check(lib.otfem_last_stats(h, ctypes.byref(stats)))
-        its.append(stats.iterations)
-        res.append(stats.rel_residual)
-        applies.append(stats.applies)
-    torch.cuda.synchronize()
-    dist_barrier(world)
+    r_plain = timed_run(h_plain, plain)
+    r_learn = timed_run(h_learn, learned)
     clocks = sampler.stop()
-    n1 = ctypes.c_int64()
-    capi.check(lib.otfem_launch_count(h, ctypes.byref(n1)))
-    dev_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
-    dev_s = dist_max(world, dev_s)
+    disp = np.abs(r_plain["x"] - coord).max()
+    pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))
 
     # ---- roofline: the persistent CG kernel timed on its own ---------------
-    cg_ms, cg_bytes = [], []
+    cg_ms, cg_bytes, cg_applies = [], [], []
+    stats = capi.StepStats()
     for k in range(max(3, min(args.steps, 10))):
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         flush_l2()
         e0.record(stream)
-        capi.check(lib.otfem_simulate_phase(h, w["dt"], 1, ctypes.byref(params), capi.PHASE_ORIENT))
+        capi.check(lib.otfem_simulate_phase(h_plain, w["dt"], 1, ctypes.byref(plain), capi.PHASE_ORIENT))
         e1.record(stream)
-        capi.check(lib.otfem_simulate_phase(h, w["dt"], 1, ctypes.byref(params), capi.PHASE_SOLVE))
+        capi.check(lib.otfem_simulate_phase(h_plain, w["dt"], 1, ctypes.byref(plain), capi.PHASE_SOLVE))
         e2.record(stream)
-        capi.check(lib.otfem_last_stats(h, ctypes.byref(stats)))
+        capi.check(lib.otfem_last_stats(h_plain, ctypes.byref(stats)))
         cg_ms.append(e1.elapsed_time(e2))
+        cg_applies.append(stats.applies)
         cg_bytes.append(stats.applies * (BYTES_PER_TET_APPLY * T + BYTES_PER_NODE_APPLY * n_free)
                         + stats.iterations * BYTES_PER_NODE_ITER * n_free)
     cg_s = np.array(cg_ms) / 1e3
@@ -285,66 +374,77 @@ def run_ours(args, world, rank, local):
     peak_note = "measured" if peak else "fallback"
     peak = peak or 6800.0
     # DRAM bytes of one k_cg_mixed launch from an ncu capture of this workload,
-    # scaled to this run's element-apply sweeps per launch
+    # scaled to the element-apply sweeps of the launches timed here
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "cg_dram_traffic.json")))
-        traffic = prof["dram_bytes_per_launch"] / prof["applies_per_launch"] * float(np.mean(applies))
+        traffic = prof["dram_bytes_per_launch"] / prof["applies_per_launch"] * float(np.mean(cg_applies))
     except (OSError, ValueError, KeyError, ZeroDivisionError):
         traffic = None
 
     # ---- the element-apply sweep alone (the stiffness apply) ----------------
     variant = ctypes.c_int32()
-    capi.check(lib.otfem_tuning(h, ctypes.byref(variant), None))
+    capi.check(lib.otfem_tuning(h_plain, ctypes.byref(variant), None))
     sweep_ms = []
     for k in range(10):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         flush_l2()
         e0.record(stream)
-        capi.check(lib.otfem_apply_sweeps(h, capi.SOLVER_MIXED, w["dt"], 1))
+        capi.check(lib.otfem_apply_sweeps(h_plain, capi.SOLVER_MIXED, w["dt"], 1))
         e1.record(stream)
         torch.cuda.synchronize()
         sweep_ms.append(e0.elapsed_time(e1))
     sweep_bytes = BYTES_PER_TET_APPLY * T + BYTES_PER_NODE_APPLY * n_free
     sweep_gbs = sweep_bytes / (float(np.median(sweep_ms)) * 1e-3) / 1e9
 
-    # ---- end to end through the C ABI with host buffers ---------------------
+    # ---- end to end through the C ABI with host buffers (learned) ----------
     pin_x = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     pin_v = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     pin_f = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
-    capi.check(lib.otfem_get_nodes(h, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-    capi.check(lib.otfem_get_nodes(h, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
-    pin_f[:] = fext
+    capi.check(lib.otfem_get_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+    capi.check(lib.otfem_get_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+    pin_f[:] = r_learn["fext"]
     e2e_ms = []
     dist_barrier(world)
     for k in range(args.steps):
         flush_l2()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        capi.check(lib.otfem_set_nodes(h, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-        capi.check(lib.otfem_set_nodes(h, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
-        capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
-        step()
-        capi.check(lib.otfem_get_nodes(h, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-        capi.check(lib.otfem_get_nodes(h, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        capi.check(lib.otfem_set_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+        capi.check(lib.otfem_set_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        capi.check(lib.otfem_set_nodes(h_learn, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
+        capi.check(lib.otfem_simulate_ex(h_learn, w["dt"], 1, ctypes.byref(learned), None))
+        capi.check(lib.otfem_get_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+        capi.check(lib.otfem_get_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = dist_max(world, sum(e2e_ms) / 1e3)
     dist_barrier(world)
 
     total_tet_steps = T * args.steps * world
-    value = total_tet_steps / dev_s
+    value = total_tet_steps / r_learn["dev_s"]
+    plain_value = total_tet_steps / r_plain["dev_s"]
     e2e_value = total_tet_steps / e2e_s
     if rank != 0:
         return
     line = {
         "metric": METRIC, "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 element apply, f64 CG vectors and reductions",
+        "warmup": args.warmup, "ms_per_step": 1e3 * r_learn["dev_s"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 element apply, f64 CG vectors and reductions, bf16/f32 warm-start network",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD["name"], "warm_start": "previous velocity (plain CG)",
+        "config": {"workload": WORKLOAD["name"],
+                   "warm_start": "learned (node MLP + 1-ring smoothing), trained in this run",
                    "solver": "matrix-free persistent CG (OTFEM_SOLVER_MIXED), CUDA graph per step",
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
-                   "iterations_per_step": float(np.mean(its)), "max_rel_residual": float(np.max(res))},
+                   "iterations_per_step": float(np.mean(r_learn["its"])),
+                   "max_rel_residual": float(np.max(r_learn["res"])),
+                   "plain": {"value": plain_value, "unit": "tet-steps/s",
+                             "ms_per_step": 1e3 * r_plain["dev_s"] / args.steps,
+                             "iterations_per_step": float(np.mean(r_plain["its"])),
+                             "max_rel_residual": float(np.max(r_plain["res"]))},
+                   "learned_over_plain": value / plain_value,
+                   "position_difference_learned_vs_plain": pos_diff,
+                   "training": train_info},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_cg_mixed", "peak_source": peak_note,
                      "algorithmic_bytes_per_launch": float(np.mean(cg_bytes)),
@@ -355,7 +455,7 @@ def run_ours(args, world, rank, local):
                                      "l2": "flushed before each sweep"}},
         "e2e": {"value": e2e_value, "unit": "tet-steps/s", "h2d_bytes_per_step": 3 * 24 * N,
                 "d2h_bytes_per_step": 2 * 24 * N},
-        "gpu_launches": int(n1.value - n0.value),
+        "gpu_launches": r_learn["launches"],
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -365,7 +465,10 @@ def run_ours(args, world, rank, local):
                                 "sample": f"{args.cpu_steps} steps of the full workload from rest, converged CG "
                                           f"({float(np.mean(cits)):.0f} iterations/step), one host core"}
     print(json.dumps(line), flush=True)
-    capi.check(lib.otfem_destroy(h))
+    net.detach(h_learn)
+    capi.check(lib.otfem_destroy(h_plain))
+    capi.check(lib.otfem_destroy(h_learn))
+    net.close()
 
 
 def main():
@@ -377,6 +480,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="beam128", choices=sorted(WORKLOADS))
+    ap.add_argument("--train-samples", type=int, default=2_000_000)
+    ap.add_argument("--train-steps", type=int, default=40)
+    ap.add_argument("--train-epochs", type=int, default=60)
+    ap.add_argument("--seed", type=int, default=20261203)
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = WORKLOADS[args.workload]

@@ -233,9 +233,11 @@ OTFEM_API int otfem_mlp_predict(otfem_mlp m, const float* x, int64_t n, float* y
  * The network must outlive its use and must not be trained while steps
  * that use it are in flight. */
 OTFEM_API int otfem_set_mlp(otfem_handle h, otfem_mlp m);
-/* Passes (0..64) of 1-ring mean aggregation over the network's correction
- * net(inputs) before it enters the initial guess: each pass replaces a
- * node's correction by the mean over its tets of the tet's node mean. */
+/* Passes (0..64, default 4) of 1-ring mean aggregation over the network's
+ * correction net(inputs) before it enters the initial guess: each pass
+ * replaces a node's correction by the mean over its tets of the tet's node
+ * mean.  (The network's per-node errors are rough; the smoothed correction
+ * leaves a smaller initial residual.) */
 OTFEM_API int otfem_set_warm_start_smoothing(otfem_handle h, int32_t passes);
 
 /* ---- host staging (no counterpart in the reference) ---------------------- */

@@ -133,7 +133,7 @@ struct Context {
   float4* dv_last = nullptr;      // N (w unused)
   float4* warm_dv = nullptr;      // N
   float4* warm_tmp = nullptr;     // N, allocated with smoothing passes
-  int warm_smoothing = 0;         // 1-ring mean passes over the network's correction
+  int warm_smoothing = 4;         // 1-ring mean passes over the network's correction
   float* features = nullptr;      // N x kFeatureStride, allocated when collecting
   int collect = 0;
   bool features_valid = false;    // c.features hold the inputs of the last step

@@ -1122,6 +1122,10 @@ int otfem_set_mlp(otfem_handle h, otfem_mlp m) {
   // kernel attributes outside any stream capture of the step
   if (cudaError_t e = set_attributes()) return mlp_cuda(e, "cudaFuncSetAttribute");
   if (m && m->device != c->device) return mlp_fail(OTFEM_ERR_INVALID_ARGUMENT, "network and mesh on different devices");
+  if (m && !c->warm_tmp) {
+    cudaError_t e = cudaMalloc(&c->warm_tmp, sizeof(float4) * size_t(std::max(c->N, 1)));
+    if (e != cudaSuccess) return mlp_cuda(e, "cudaMalloc");
+  }
   c->mlp = m;
   return OTFEM_OK;
 }
