@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 3
+#define OTFEM_ABI_VERSION 4
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -179,6 +179,23 @@ OTFEM_API int otfem_k_values(otfem_handle h, double* host_values);
 OTFEM_API int otfem_get_orientations(otfem_handle h, double* host_re);
 OTFEM_API int otfem_get_plastic(otfem_handle h, double* host_plastic);
 OTFEM_API int otfem_get_volumes(otfem_handle h, double* host_volume);
+
+/* ---- batches of meshes (no counterpart in the reference) -----------------
+ * One handle over `count` independent meshes (uneven sizes allowed), stepped
+ * together by one persistent launch per step in which every mesh runs its
+ * own CG (own alpha, beta, residuals and convergence; OTFEM_SOLVER_MIXED).
+ * Node fields of the handle are the meshes' fields one after another
+ * (otfem_batch_layout gives the offsets); otfem_last_stats reports the
+ * largest iteration count and relative residual and the worst status. */
+OTFEM_API int otfem_batch_create(const otfem_mesh_desc* meshes, int32_t count, void* stream, otfem_handle* out);
+/* fem::init with one material per mesh (arrays of `count`). */
+OTFEM_API int otfem_batch_init(otfem_handle h, const double* young, const double* poisson, const double* density,
+                               double c_yield, double c_creep, double c_max);
+/* Number of meshes and the first node / tet of each (count + 1 entries). */
+OTFEM_API int otfem_batch_layout(otfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets);
+/* Per-mesh results of the last step (arrays of `count`, each may be NULL). */
+OTFEM_API int otfem_batch_stats(otfem_handle h, int32_t* iterations, int32_t* status, double* rel_residual,
+                                double* initial_rel_residual);
 
 /* ---- learned warm start (no counterpart in the reference) ----------------
  * fem_conjugate_gradients.h:44-46 starts CG from the previous velocity.  With

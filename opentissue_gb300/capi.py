@@ -124,6 +124,11 @@ SIGNATURES = {
     "otfem_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),
     "otfem_solver_shape": (ctypes.c_int, [_h, _i32p, _i32p]),
+    "otfem_batch_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.POINTER(_h)]),
+    "otfem_batch_init": (ctypes.c_int, [_h, _dp, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
+    "otfem_batch_layout": (ctypes.c_int, [_h, _i32p, _i32p, _i32p]),
+    "otfem_batch_stats": (ctypes.c_int, [_h, _i32p, _i32p, _dp, _dp]),
     "otfem_mlp_create": (ctypes.c_int, [ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
     "otfem_mlp_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_mlp_get_state": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.c_int64]),

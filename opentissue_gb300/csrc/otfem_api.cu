@@ -1,6 +1,7 @@
 // otfem_api.cu -- the C ABI of libotfem_gpu.so (include/otfem_gpu.h): context
 // lifetime, host<->device transfers, and the step orchestration, replayed
 // from a CUDA graph per (solver, dt, warp, parameters) key.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -64,6 +65,10 @@ void free_all(Context& c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c.stats_host) cudaFreeHost(c.stats_host);
+  if (c.bmesh_host) cudaFreeHost(c.bmesh_host);
+  void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.bmesh, c.bacc, c.bmask};
+  for (void* p : batch)
+    if (p) cudaFree(p);
   if (c.graph) cudaGraphExecDestroy(c.graph);
   if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
 }
@@ -92,6 +97,8 @@ int check_params(const Context& c, const otfem_solver_params& p) {
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
   if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
+  if (c.num_meshes > 1 && p.solver != OTFEM_SOLVER_MIXED)
+    return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes steps with OTFEM_SOLVER_MIXED (one CG per mesh)");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && p.solver != OTFEM_SOLVER_MIXED)
     return fail(OTFEM_ERR_UNSUPPORTED, "the learned warm start runs with OTFEM_SOLVER_MIXED");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && !c.mlp)
@@ -124,7 +131,9 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
   } else {
     if ((e = otfem::launch_mixed_orient(c, dt, warp, p.solver)) != cudaSuccess) return e;
     if ((e = launch_warm_start(c, p)) != cudaSuccess) return e;
-    if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return e;
+    if (c.num_meshes > 1) e = otfem::launch_batch_solve(c, dt, p);
+    else e = otfem::launch_mixed_solve(c, dt, p);
+    if (e != cudaSuccess) return e;
   }
   return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
 }
@@ -326,17 +335,20 @@ int otfem_num_tets(otfem_handle h, int32_t* t) {
   return OTFEM_OK;
 }
 
-int otfem_init(otfem_handle h, double young, double poisson, double density, double c_yield,
-               double c_creep, double c_max) {
-  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
-  Context& c = h->c;
-  // fem_uniform_young.h:32, fem_uniform_poisson.h:33-34, fem_uniform_density.h:27,
-  // fem_initialize_plastic.h:42-44 (debug asserts in the reference)
-  if (!(young >= 0.0) || !(poisson >= 0.0 && poisson <= 0.5) || !(density > 0.0) || !(c_yield >= 0.0) ||
-      !(c_creep >= 0.0) || !(c_max >= 0.0))
+// fem_uniform_young.h:32, fem_uniform_poisson.h:33-34, fem_uniform_density.h:27,
+// fem_initialize_plastic.h:42-44 (debug asserts in the reference)
+static bool material_ok(double young, double poisson, double density) {
+  return young >= 0.0 && poisson >= 0.0 && poisson <= 0.5 && density > 0.0;
+}
+
+// fem::init with uniform materials, or per tet (device arrays) when given.
+static int init_impl(Context& c, double young, double poisson, double density, double c_yield, double c_creep,
+                     double c_max, const double* young_t, const double* poisson_t, const double* density_t) {
+  if (!(c_yield >= 0.0) || !(c_creep >= 0.0) || !(c_max >= 0.0))
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "material parameter out of range");
   cudaError_t e;
-  if ((e = otfem::launch_init_elements(c, young, poisson, density, c_yield, c_creep, c_max)) != cudaSuccess)
+  if ((e = otfem::launch_init_elements(c, young, poisson, density, c_yield, c_creep, c_max, young_t, poisson_t,
+                                       density_t)) != cudaSuccess)
     return cuda_fail(e, "init elements");
   if ((e = otfem::mixed_prepare(c)) != cudaSuccess) return cuda_fail(e, "prepare");
   // clear_stiffness_assembly (fem_init.h:60)
@@ -361,6 +373,130 @@ int otfem_init(otfem_handle h, double young, double poisson, double density, dou
   for (int t = 0; t < c.T; ++t)
     if (!(vol[t] > 0.0))
       return fail(OTFEM_ERR_BAD_MESH, "tet " + std::to_string(t) + " has non-positive volume");
+  return OTFEM_OK;
+}
+
+int otfem_init(otfem_handle h, double young, double poisson, double density, double c_yield,
+               double c_creep, double c_max) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  if (!material_ok(young, poisson, density)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "material parameter out of range");
+  return init_impl(h->c, young, poisson, density, c_yield, c_creep, c_max, nullptr, nullptr, nullptr);
+}
+
+int otfem_batch_create(const otfem_mesh_desc* meshes, int32_t count, void* stream, otfem_handle* out) {
+  if (!meshes || count < 1 || !out) return fail(OTFEM_ERR_INVALID_ARGUMENT, "bad argument");
+  *out = nullptr;
+  int64_t N = 0, T = 0;
+  for (int m = 0; m < count; ++m) {
+    const otfem_mesh_desc& d = meshes[m];
+    if (d.num_nodes < 0 || d.num_tets < 0 || (d.num_tets > 0 && !d.tets) || (d.num_nodes > 0 && !d.coord))
+      return fail(OTFEM_ERR_INVALID_ARGUMENT, "mesh " + std::to_string(m) + ": bad descriptor");
+    N += d.num_nodes;
+    T += d.num_tets;
+  }
+  if (N > INT32_MAX || T > INT32_MAX) return fail(OTFEM_ERR_INVALID_ARGUMENT, "batch too large");
+  std::vector<int32_t> tets(size_t(4) * T);
+  std::vector<double> coord(size_t(3) * N), model(size_t(3) * N);
+  std::vector<uint8_t> fixed(size_t(N), 0);
+  std::vector<int> noff(size_t(count) + 1, 0), toff(size_t(count) + 1, 0);
+  for (int m = 0; m < count; ++m) {
+    const otfem_mesh_desc& d = meshes[m];
+    const int n0 = noff[m], t0 = toff[m];
+    for (int64_t k = 0; k < 4LL * d.num_tets; ++k) {
+      if (d.tets[k] < 0 || d.tets[k] >= d.num_nodes)
+        return fail(OTFEM_ERR_BAD_MESH, "mesh " + std::to_string(m) + ": node index out of range");
+      tets[size_t(4) * t0 + k] = d.tets[k] + n0;
+    }
+    const double* mc = d.model_coord ? d.model_coord : d.coord;
+    std::copy(d.coord, d.coord + 3 * d.num_nodes, coord.begin() + 3 * size_t(n0));
+    std::copy(mc, mc + 3 * d.num_nodes, model.begin() + 3 * size_t(n0));
+    if (d.fixed) std::copy(d.fixed, d.fixed + d.num_nodes, fixed.begin() + n0);
+    noff[m + 1] = n0 + d.num_nodes;
+    toff[m + 1] = t0 + d.num_tets;
+  }
+  otfem_mesh_desc all = {int32_t(N), int32_t(T), tets.data(), coord.data(), model.data(), fixed.data()};
+  int rc = otfem_create(&all, stream, out);
+  if (rc != OTFEM_OK) return rc;
+  Context& c = (*out)->c;
+  c.num_meshes = count;
+  c.mesh_node_off = noff;
+  c.mesh_tet_off = toff;
+  std::vector<int> mon(size_t(std::max<int64_t>(N, 1))), mot(size_t(std::max<int64_t>(T, 1)));
+  for (int m = 0; m < count; ++m) {
+    for (int i = noff[m]; i < noff[m + 1]; ++i) mon[size_t(i)] = m;
+    for (int t = toff[m]; t < toff[m + 1]; ++t) mot[size_t(t)] = m;
+  }
+  cudaError_t e = cudaMalloc(&c.mesh_of_node, sizeof(int) * mon.size());
+  if (e == cudaSuccess) e = cudaMalloc(&c.mesh_of_tet, sizeof(int) * mot.size());
+  if (e == cudaSuccess) e = cudaMalloc(&c.bmesh, sizeof(otfem::BatchMesh) * size_t(count));
+  if (e == cudaSuccess) e = cudaMallocHost(&c.bmesh_host, sizeof(otfem::BatchMesh) * size_t(count));
+  if (e == cudaSuccess) e = cudaMalloc(&c.bacc, sizeof(double) * 8 * size_t(count));
+  if (e == cudaSuccess) e = cudaMalloc(&c.bmask, 3 * size_t(count));
+  if (e == cudaSuccess) e = cudaMemcpy(c.mesh_of_node, mon.data(), sizeof(int) * mon.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(c.mesh_of_tet, mot.data(), sizeof(int) * mot.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(c.bmesh, 0, sizeof(otfem::BatchMesh) * size_t(count));
+  if (e != cudaSuccess) {
+    otfem_destroy(*out);
+    *out = nullptr;
+    return cuda_fail(e, "batch arrays");
+  }
+  return OTFEM_OK;
+}
+
+int otfem_batch_init(otfem_handle h, const double* young, const double* poisson, const double* density,
+                     double c_yield, double c_creep, double c_max) {
+  if (!h || !young || !poisson || !density) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  const int M = c.num_meshes;
+  for (int m = 0; m < M; ++m)
+    if (!material_ok(young[m], poisson[m], density[m]))
+      return fail(OTFEM_ERR_INVALID_ARGUMENT, "mesh " + std::to_string(m) + ": material parameter out of range");
+  std::vector<double> e_t(size_t(std::max(c.T, 1))), nu_t(e_t.size()), rho_t(e_t.size());
+  for (int m = 0; m < M; ++m) {
+    const int t0 = M > 1 ? c.mesh_tet_off[m] : 0, t1 = M > 1 ? c.mesh_tet_off[m + 1] : c.T;
+    for (int t = t0; t < t1; ++t) e_t[size_t(t)] = young[m], nu_t[size_t(t)] = poisson[m], rho_t[size_t(t)] = density[m];
+  }
+  double* d = nullptr;
+  const size_t n = e_t.size();
+  OT_CUDA(cudaMalloc(&d, sizeof(double) * 3 * n));
+  cudaError_t e = cudaMemcpy(d, e_t.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, nu_t.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + 2 * n, rho_t.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? init_impl(c, 0.0, 0.0, 1.0, c_yield, c_creep, c_max, d, d + n, d + 2 * n)
+                            : cuda_fail(e, "batch materials");
+  cudaStreamSynchronize(c.stream);
+  cudaFree(d);
+  return rc;
+}
+
+int otfem_batch_layout(otfem_handle h, int32_t* count, int32_t* node_offsets, int32_t* tet_offsets) {
+  if (!h || !count) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  const Context& c = h->c;
+  *count = c.num_meshes;
+  for (int m = 0; m <= c.num_meshes; ++m) {
+    const bool single = c.num_meshes == 1;
+    if (node_offsets) node_offsets[m] = single ? (m ? c.N : 0) : c.mesh_node_off[m];
+    if (tet_offsets) tet_offsets[m] = single ? (m ? c.T : 0) : c.mesh_tet_off[m];
+  }
+  return OTFEM_OK;
+}
+
+int otfem_batch_stats(otfem_handle h, int32_t* iterations, int32_t* status, double* rel_residual,
+                      double* initial_rel_residual) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (c.num_meshes < 2 || !c.bmesh) return fail(OTFEM_ERR_INVALID_ARGUMENT, "not a batch of meshes");
+  const int M = c.num_meshes;
+  OT_CUDA(cudaMemcpyAsync(c.bmesh_host, c.bmesh, sizeof(otfem::BatchMesh) * M, cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  for (int m = 0; m < M; ++m) {
+    const otfem::BatchMesh& b = c.bmesh_host[m];
+    const double bb = b.bnorm2 > 0.0 ? b.bnorm2 : 1.0;
+    if (iterations) iterations[m] = b.iterations;
+    if (status) status[m] = b.status;
+    if (rel_residual) rel_residual[m] = std::sqrt(b.rho / bb);
+    if (initial_rel_residual) initial_rel_residual[m] = std::sqrt(b.rho0 / bb);
+  }
   return OTFEM_OK;
 }
 
@@ -464,7 +600,8 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
     if ((e = launch_warm_start(c, p)) != cudaSuccess) return cuda_fail(e, "warm start");
     if (p.warm_start == OTFEM_WARM_START_LEARNED || c.collect) c.launches += 1;
   } else if (phase == OTFEM_PHASE_SOLVE) {
-    if ((e = otfem::launch_mixed_solve(c, dt, p)) != cudaSuccess) return cuda_fail(e, "solve phase");
+    e = c.num_meshes > 1 ? otfem::launch_batch_solve(c, dt, p) : otfem::launch_mixed_solve(c, dt, p);
+    if (e != cudaSuccess) return cuda_fail(e, "solve phase");
     OT_CUDA(cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream));
     c.launches += 1;
     c.last_solver = p.solver;
@@ -642,6 +779,8 @@ int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_variant) {
 int otfem_set_apply_variant(otfem_handle h, int32_t variant) {
   if (!h || variant < 0 || variant >= otfem::kNumApplyVariants) return fail(OTFEM_ERR_INVALID_ARGUMENT, "bad variant");
   Context& c = h->c;
+  if (c.num_meshes > 1 && variant < 2)
+    return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes uses apply variant 2 or 3");
   c.apply_variant = variant;
   if (c.graph) {
     cudaGraphExecDestroy(c.graph);

@@ -20,12 +20,18 @@ inline int blocks_for(long n) { return int((n + kThreads - 1) / kThreads) > 0 ? 
 // compute_B (fem_compute_b.h:28-400), compute_isotropic_elasticity_vector
 // (fem_compute_isotropic_elasticity.h:25-51); one thread per tet.
 __global__ void k_init_elements(int T, const int4* __restrict__ tets, const double* __restrict__ x0,
-                                double young, double poisson, double density, double c_yield,
+                                double young_u, double poisson_u, double density_u, double c_yield,
                                 double c_creep, double c_max, double* Ke, double* Re, double* V,
                                 double* E, double* Bv, double* D, double* plastic, double* yng,
-                                double* poi, double* den, double* yld, double* crp, double* cmx) {
+                                double* poi, double* den, double* yld, double* crp, double* cmx,
+                                const double* __restrict__ young_t, const double* __restrict__ poisson_t,
+                                const double* __restrict__ density_t) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
+  // uniform materials (fem_uniform_young.h etc.), or per tet when given
+  const double young = young_t ? young_t[t] : young_u;
+  const double poisson = poisson_t ? poisson_t[t] : poisson_u;
+  const double density = density_t ? density_t[t] : density_u;
   int4 n = tets[t];
   const double* p0 = x0 + 3 * n.x;
   const double* p1 = x0 + 3 * n.y;
@@ -541,10 +547,12 @@ __global__ void k_export_fill(int N, int assembled, const unsigned char* __restr
 // ---- host launch wrappers ---------------------------------------------------
 
 cudaError_t launch_init_elements(Context& c, double young, double poisson, double density,
-                                 double c_yield, double c_creep, double c_max) {
+                                 double c_yield, double c_creep, double c_max, const double* young_t,
+                                 const double* poisson_t, const double* density_t) {
   k_init_elements<<<blocks_for(c.T), kThreads, 0, c.stream>>>(
       c.T, c.tets, c.x0, young, poisson, density, c_yield, c_creep, c_max, c.Ke, c.Re, c.V, c.E,
-      c.Bv, c.D, c.plastic, c.young, c.poisson, c.density, c.yield, c.creep, c.cmax);
+      c.Bv, c.D, c.plastic, c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, young_t, poisson_t,
+      density_t);
   k_mass<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.inc_ptr, c.inc_ent, c.fixed, c.density,
                                                      c.V, c.mass);
   return cudaGetLastError();

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/otfem_gpu.h"
 
@@ -37,6 +38,12 @@ struct DeviceSync {
   double pad4[8];
   unsigned tile_ticket;      // staged apply: monotonic tile tickets
   unsigned pad5[31];
+};
+
+// Per-mesh state of a batched solve (device memory, one per mesh).
+struct BatchMesh {
+  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta;
+  int active, restart, stalls, iterations, applies, status, converged, pad;
 };
 
 // Statistics written by the step kernels (device memory).
@@ -138,6 +145,16 @@ struct Context {
   int collect = 0;
   bool features_valid = false;    // c.features hold the inputs of the last step
   struct otfem_mlp_s* mlp = nullptr;
+  // batch of independent meshes (otfem_batch_create): mesh m owns nodes
+  // [mesh_node_off[m], mesh_node_off[m+1]) and tets [mesh_tet_off[m], ...)
+  int num_meshes = 1;
+  std::vector<int> mesh_node_off, mesh_tet_off;  // host, num_meshes + 1
+  int* mesh_of_node = nullptr;                    // N
+  int* mesh_of_tet = nullptr;                     // T
+  BatchMesh* bmesh = nullptr;                     // num_meshes
+  BatchMesh* bmesh_host = nullptr;                // num_meshes, pinned
+  double* bacc = nullptr;                         // 2 x num_meshes x 4 accumulators
+  unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
   double apply_ms[4] = {0, 0, 0, 0};  // measured time of one sweep per variant
@@ -160,8 +177,9 @@ cudaError_t build_incidence(Context& c);
 cudaError_t build_pattern(Context& c);
 
 // ---- reference-order FP64 kernels (otfem_exact.cu) ------------------------
-cudaError_t launch_init_elements(Context& c, double young, double poisson, double density,
-                                 double c_yield, double c_creep, double c_max);
+cudaError_t launch_init_elements(Context& c, double young, double poisson, double density, double c_yield,
+                                 double c_creep, double c_max, const double* young_t = nullptr,
+                                 const double* poisson_t = nullptr, const double* density_t = nullptr);
 cudaError_t launch_orientation(Context& c, bool warp);
 cudaError_t launch_assembly(Context& c);
 cudaError_t launch_plasticity(Context& c, double dt);
@@ -198,6 +216,9 @@ constexpr int kTileWords = 20;
 // Writes m_Re (FP64) from the FP32 orientations of the last mixed step.
 cudaError_t sync_orientations(Context& c);
 cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& p);
+// Batched matrix-free solve: every mesh of the batch runs its own CG (own
+// scalars, convergence and iteration count) in one persistent launch.
+cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params& prm);
 // y = A x with the matrix-free apply of the given precision and the current
 // orientations (x, y: device, 3 doubles per node; rows of fixed nodes = 0).
 cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass_damping, const double* x, double* y);

@@ -118,6 +118,13 @@ struct MixedArgs {
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
   const float4* warm_dv;                // learned initial guess v + warm_dv (null: v)
   float4* dv_last;                      // out: v_new - v_old per free node
+  // batched solve (see Context)
+  int num_meshes;
+  const int* mesh_of_node;
+  const int* mesh_of_tet;
+  BatchMesh* bm;
+  double* bacc;
+  unsigned char* bmask;
   long long spin_limit;
 };
 
@@ -767,11 +774,12 @@ template <typename R>
 __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                            const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
                            const R* __restrict__ re, const R* __restrict__ bb, const R* __restrict__ cc,
-                           R scale) {
+                           R scale, const unsigned char* mask) {
   typedef typename ApplyOps<R>::V4 V4;
   const int T = a.T;
   const bool has_lo = sizeof(R) == 4 && ulo != nullptr;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+    if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
     const int4 n = a.tets[t];
     V4 w[4] = {u4[n.x], u4[n.y], u4[n.z], u4[n.w]};
     float4 lo[4];
@@ -824,7 +832,7 @@ __device__ __forceinline__ int claim_tile(const MixedArgs& a) {
 // spin_limit cycles the CTA sets OTFEM_ERR_TIMEOUT, stops, and waits (again
 // bounded) for the copies it still has in flight before returning.
 __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
-                             unsigned char* smem) {
+                             unsigned char* smem, const unsigned char* mask) {
   const int TT = a.tile_tets;
   const unsigned tile_bytes = unsigned(TT) * kTileWords * sizeof(float);
   auto stage = [smem](int sb) { return reinterpret_cast<float*>(smem + sb * kStageBytes); };
@@ -858,7 +866,7 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
     if (tile < 0) break;
     const bool ok = mbar_wait(&bar[sb], (j >> 1) & 1, a.spin_limit);
     const int t = tile * TT + tid;
-    if (ok && tid < TT && t < a.T) {
+    if (ok && tid < TT && t < a.T && (!mask || mask[a.mesh_of_tet[t]])) {
       const float* w = stage(sb);
       const int nn[4] = {__float_as_int(w[tid]), __float_as_int(w[TT + tid]), __float_as_int(w[2 * TT + tid]),
                          __float_as_int(w[3 * TT + tid])};
@@ -906,17 +914,22 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
   }
 }
 
+// One element-apply sweep with the mesh's variant.  `mask` (batched solves
+// only, variants kApplyTets and kApplyStaged) selects the meshes whose tets
+// take part.
 template <typename R>
 __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                                             const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
-                                            const R* re, const R* bb, const R* cc, R scale, unsigned char* smem) {
+                                            const R* re, const R* bb, const R* cc, R scale, unsigned char* smem,
+                                            const unsigned char* mask = nullptr) {
   if constexpr (sizeof(R) == 4) {
     if (a.apply_variant == kApplyStaged) {
-      apply_staged(a, u4, ulo, q4, scale, smem);
+      apply_staged(a, u4, ulo, q4, scale, smem, mask);
       return;
     }
   }
-  if (a.apply_variant == kApplyTets || a.apply_variant == kApplyStaged) apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale);
+  if (a.apply_variant == kApplyTets || a.apply_variant == kApplyStaged || mask)
+    apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale, mask);
   else if (a.apply_variant == kApplyGather) apply_patches_gather<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
   else apply_patches<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
 }
@@ -1315,6 +1328,433 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
 }
 
+// ---- batched solve -------------------------------------------------------
+// Every mesh of a batch runs its own CG (own alpha, beta, residuals,
+// recurrence checks and convergence) in lock-step with the others inside one
+// persistent launch: the apply and node phases skip the meshes that are not
+// in the current sweep (masks), the grid sums are per mesh, and the last CTA
+// to arrive at a reduction updates the scalars of all meshes at once (one
+// thread per mesh).  Node phases walk one contiguous node range per warp, so
+// a warp meets each mesh boundary at most once and adds its per-mesh sums
+// with one FP64 atomic per value and mesh.
+
+constexpr int kMaskApply = 0, kMaskUpdate = 1, kMaskRefresh = 2;
+
+struct NodeRange {
+  long beg, end;
+};
+__device__ __forceinline__ NodeRange warp_node_range(int N) {
+  const long nw = (long)gridDim.x * (blockDim.x >> 5);
+  const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long chunk = ((N + nw - 1) / nw + 31) / 32 * 32;
+  NodeRange r;
+  r.beg = w * chunk < N ? w * chunk : N;
+  r.end = r.beg + chunk < N ? r.beg + chunk : N;
+  return r;
+}
+
+// Running per-mesh sums of a warp (mesh ids are non-decreasing along nodes).
+template <int NV>
+struct SegSum {
+  int cur;  // uniform across the warp; -1: none yet
+  DF acc[NV];
+  __device__ __forceinline__ void start(int mesh) {
+    cur = mesh;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = DF{0.f, 0.f};
+  }
+  __device__ __forceinline__ void flush(double* acc_half) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      DF x = acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = AccOps<DF>::add(x, AccOps<DF>::shfl_down(x, o));
+      if ((threadIdx.x & 31) == 0 && cur >= 0) atomicAdd(&acc_half[4 * cur + k], AccOps<DF>::to_double(x));
+      acc[k] = DF{0.f, 0.f};
+    }
+  }
+  // adds each valid lane's values to the sums of its mesh m (m >= cur)
+  __device__ __forceinline__ void add(bool valid, int m, const float (&v)[NV], double* acc_half) {
+    if (valid && m == cur) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) acc[k] = df_add(acc[k], DF{v[k], 0.f});
+    }
+    unsigned rest = __ballot_sync(0xffffffffu, valid && m != cur);
+    while (rest) {
+      flush(acc_half);
+      cur = __shfl_sync(0xffffffffu, m, __ffs(rest) - 1);
+      if (valid && m == cur) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] = df_add(acc[k], DF{v[k], 0.f});
+      }
+      rest = __ballot_sync(0xffffffffu, valid && m > cur);
+    }
+  }
+};
+
+// Grid barrier whose last CTA runs fin(a, mesh, totals[4], counts) for every
+// mesh (totals: this round's accumulators, which it clears) and publishes
+// the 4 integer counts the finisher accumulates (e.g. meshes still active).
+template <typename Fin>
+__device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (&counts)[4]) {
+  __shared__ int s_flag;
+  __shared__ int s_cnt[4];
+  ++round;
+  const int half = int(round & 1u);
+  __syncthreads();
+  if (threadIdx.x == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
+  if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  if (s_flag) {
+    double* acc = a.bacc + size_t(half) * a.num_meshes * 4;
+    for (int m = threadIdx.x; m < a.num_meshes; m += blockDim.x) {
+      double t[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        t[k] = __ldcg(acc + 4 * m + k);
+        acc[4 * m + k] = 0.0;  // for round r + 2
+      }
+      fin(a, m, t, s_cnt);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < 4; ++k) a.sync->result[half][k] = double(s_cnt[k]);
+      st_release(&a.sync->gen, round);
+      if (ld_status(&a.sync->status) != 0) s_flag = 0;
+    }
+  } else if (threadIdx.x == 0) {
+    int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
+    if (ld_status(&a.sync->status) != 0) ok = 0;
+    if (ok)
+      for (int k = 0; k < 4; ++k) s_cnt[k] = int(__ldcg(&a.sync->result[half][k]));
+    s_flag = ok;
+  }
+  __syncthreads();
+  const bool good = s_flag != 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) counts[k] = s_cnt[k];
+  __syncthreads();
+  return good;
+}
+
+// totals: |b|^2 of the free rows
+struct FinBatchInit {
+  __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
+    BatchMesh& b = a.bm[m];
+    b.bnorm2 = t[0];
+    b.thresh = a.rtol * a.rtol * t[0];
+  }
+};
+
+// totals: |r0|^2 of the initial guess
+struct FinBatchStart {
+  __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
+    BatchMesh& b = a.bm[m];
+    b.rho = b.rho0 = b.best_true = b.est = t[0];
+    b.prev_est = -1.0;
+    b.restart = b.stalls = b.iterations = 0;
+    b.applies = 1;
+    b.status = isfinite(t[0]) && isfinite(b.bnorm2) ? 0 : OTFEM_ERR_NONFINITE;
+    b.converged = b.status == 0 && t[0] <= b.thresh;
+    b.active = b.status == 0 && !b.converged && a.max_it > 0;
+    unsigned char* mk = a.bmask;
+    mk[kMaskApply * a.num_meshes + m] = b.active;
+    mk[kMaskUpdate * a.num_meshes + m] = 0;
+    mk[kMaskRefresh * a.num_meshes + m] = 0;
+    if (b.active) atomicAdd(&cnt[0], 1);
+  }
+};
+
+// totals: p.q, r.q, q.q and the exact r.r of the meshes in the sweep
+struct FinBatchIter {
+  __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
+    BatchMesh& b = a.bm[m];
+    unsigned char* mk = a.bmask;
+    const int M = a.num_meshes;
+    mk[kMaskUpdate * M + m] = 0;
+    mk[kMaskRefresh * M + m] = 0;
+    if (!mk[kMaskApply * M + m]) return;
+    double o[4];
+    FinAlphaBetaExact fin;
+    fin.prev_est = b.prev_est;
+    fin.restart = b.restart != 0;
+    fin(t, o);
+    if (o[3] != 0.0) {
+      // 1: NaN/Inf in this mesh's system (an error); 2: finite breakdown
+      if (o[3] == 1.0) b.status = OTFEM_ERR_NONFINITE;
+      b.active = 0;
+      mk[kMaskApply * M + m] = 0;
+      return;
+    }
+    b.alpha = o[0];
+    b.beta = o[1];
+    b.est = b.rho = b.prev_est = o[2];
+    b.restart = 0;
+    ++b.iterations;
+    ++b.applies;
+    mk[kMaskUpdate * M + m] = 1;
+    const bool refresh = (a.refresh > 0 && b.iterations % a.refresh == 0) || o[2] <= b.thresh;
+    if (refresh) {
+      mk[kMaskRefresh * M + m] = 1;
+      ++b.applies;
+      atomicAdd(&cnt[1], 1);
+    } else if (b.iterations >= a.max_it) {
+      b.active = 0;  // the update of this iteration is its last
+      mk[kMaskApply * M + m] = 0;
+    }
+    if (b.active) atomicAdd(&cnt[0], 1);
+  }
+};
+
+// totals: the true |b - A v|^2 of the refreshed meshes
+struct FinBatchRefresh {
+  __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
+    BatchMesh& b = a.bm[m];
+    unsigned char* mk = a.bmask;
+    const int M = a.num_meshes;
+    if (mk[kMaskRefresh * M + m]) {
+      b.restart = t[0] > 4.0 * b.est;
+      b.prev_est = -1.0;
+      b.rho = t[0];
+      if (t[0] < b.best_true) {
+        b.best_true = t[0];
+        b.stalls = 0;
+      } else if (++b.stalls >= 3) {
+        b.active = 0;  // at the precision floor
+      }
+      if (t[0] <= b.thresh) {
+        b.converged = 1;
+        b.active = 0;
+      }
+      if (b.iterations >= a.max_it) b.active = 0;
+      mk[kMaskApply * M + m] = b.active;
+    }
+    if (b.active) atomicAdd(&cnt[0], 1);
+  }
+};
+
+__global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
+  const int N = a.N, M = a.num_meshes;
+  const float scale = float(a.dt * a.dt);
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  unsigned round = 0;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const NodeRange nr = warp_node_range(N);
+  const int lane = threadIdx.x & 31;
+  const int first_mesh = nr.beg < nr.end ? a.mesh_of_node[nr.beg] : -1;
+  const unsigned char* mask_apply = a.bmask + kMaskApply * M;
+  const unsigned char* mask_update = a.bmask + kMaskUpdate * M;
+  const unsigned char* mask_refresh = a.bmask + kMaskRefresh * M;
+  int counts[4];
+  int sweeps = 0;
+  auto acc_half = [&](unsigned next_round) { return a.bacc + size_t(next_round & 1u) * M * 4; };
+
+  // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess), q = 0
+  {
+    SegSum<1> ss;
+    ss.start(first_mesh);
+    for (long base = nr.beg; base < nr.end; base += 32) {
+      const long i = base + lane;
+      const bool valid = i < nr.end;
+      int m = -1;
+      float bb[1] = {0.f};
+      if (valid) {
+        m = a.mesh_of_node[i];
+        DF g[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
+          int e = a.inc_ent[q];
+          float4 f = a.g_f[4L * (e >> 2) + (e & 3)];
+          df_inc(g[0].hi, g[0].lo, f.x);
+          df_inc(g[1].hi, g[1].lo, f.y);
+          df_inc(g[2].hi, g[2].lo, f.z);
+        }
+        const bool fx = a.fixed[i] != 0;
+        const double mass = a.mass[i];
+        double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+        if (!fx) {
+          double b3[3];
+          for (int c = 0; c < 3; ++c)
+            b3[c] = mass * vi[c] + a.dt * (a.fext[3 * i + c] - (double(g[c].hi) + double(g[c].lo)));
+          for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
+          const float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
+          bb[0] = bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2];
+          a.diag[i] = mass + a.dt * (a.alpha * mass);
+          if (a.warm_dv) {
+            const float4 w = a.warm_dv[i];
+            vi[0] += double(w.x), vi[1] += double(w.y), vi[2] += double(w.z);
+          }
+        } else {
+          a.diag[i] = 0.0;
+        }
+        store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+        a.q_f[i] = zero4;
+      }
+      ss.add(valid, m, bb, acc_half(round + 1));
+    }
+    ss.flush(acc_half(round + 1));
+  }
+  if (!batch_reduce(a, round, FinBatchInit(), counts)) return;
+
+  // initial residual r = b - A v (FP64), p = r, for every mesh
+  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+  ++sweeps;
+  if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  {
+    SegSum<1> ss;
+    ss.start(first_mesh);
+    for (long base = nr.beg; base < nr.end; base += 32) {
+      const long i = base + lane;
+      const bool valid = i < nr.end;
+      int m = -1;
+      float rr[1] = {0.f};
+      if (valid) {
+        m = a.mesh_of_node[i];
+        if (a.fixed[i]) {
+          a.p_f[i] = zero4;
+          a.r_f[i] = zero4;
+        } else {
+          const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+          const double d = a.diag[i];
+          float rf[3];
+          rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+          rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+          rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+          a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
+          a.q_f[i] = zero4;
+          rr[0] = rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2];
+        }
+      }
+      ss.add(valid, m, rr, acc_half(round + 1));
+    }
+    ss.flush(acc_half(round + 1));
+  }
+  if (!batch_reduce(a, round, FinBatchStart(), counts)) return;
+  int n_active = counts[0];
+
+  for (int it = 0; n_active > 0 && it < a.max_it; ++it) {
+    // q += dt^2 K' p for the meshes still iterating
+    apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_apply);
+    ++sweeps;
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    // q = diag p + q; p.q, r.q, q.q, r.r per mesh
+    {
+      SegSum<4> ss;
+      ss.start(first_mesh);
+      for (long base = nr.beg; base < nr.end; base += 32) {
+        const long i = base + lane;
+        const bool valid = i < nr.end;
+        int m = -1;
+        float s4[4] = {0.f, 0.f, 0.f, 0.f};
+        if (valid) {
+          m = a.mesh_of_node[i];
+          if (mask_apply[m] && !a.fixed[i]) {
+            const float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
+            const float d = float(a.diag[i]);
+            const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+            s4[0] = p4.x * qx + p4.y * qy + p4.z * qz;
+            s4[1] = r4.x * qx + r4.y * qy + r4.z * qz;
+            s4[2] = qx * qx + qy * qy + qz * qz;
+            s4[3] = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z;
+          }
+        }
+        ss.add(valid, m, s4, acc_half(round + 1));
+      }
+      ss.flush(acc_half(round + 1));
+    }
+    if (!batch_reduce(a, round, FinBatchIter(), counts)) return;
+    n_active = counts[0];
+    const bool any_refresh = counts[1] > 0;
+    // v += alpha p, r -= alpha q, p = r + beta p with each mesh's scalars
+    for (long i = nr.beg + lane; i < nr.end; i += 32) {
+      const int m = a.mesh_of_node[i];
+      if (!mask_update[m] || a.fixed[i]) continue;
+      const float alpha = float(a.bm[m].alpha), beta = float(a.bm[m].beta);
+      float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
+      float4 vh = a.v_f[i], vl = a.v_lo[i];
+      const float d = float(a.diag[i]);
+      const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+      df_inc(vh.x, vl.x, alpha * p4.x);
+      df_inc(vh.y, vl.y, alpha * p4.y);
+      df_inc(vh.z, vl.z, alpha * p4.z);
+      const float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
+      a.v_f[i] = vh;
+      a.v_lo[i] = vl;
+      a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+      a.p_f[i] = make_float4(rx + beta * p4.x, ry + beta * p4.y, rz + beta * p4.z, 1.f);
+      a.q_f[i] = zero4;
+    }
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (any_refresh) {
+      // r = b - A v (residual replacement, FP64) for the meshes due
+      apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_refresh);
+      ++sweeps;
+      if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+      SegSum<1> ss;
+      ss.start(first_mesh);
+      for (long base = nr.beg; base < nr.end; base += 32) {
+        const long i = base + lane;
+        const bool valid = i < nr.end;
+        int m = -1;
+        float tr[1] = {0.f};
+        if (valid) {
+          m = a.mesh_of_node[i];
+          if (mask_refresh[m] && !a.fixed[i]) {
+            const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+            const double d = a.diag[i];
+            const float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+            const float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+            const float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+            a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+            a.q_f[i] = zero4;
+            tr[0] = rx * rx + ry * ry + rz * rz;
+          }
+        }
+        ss.add(valid, m, tr, acc_half(round + 1));
+      }
+      ss.flush(acc_half(round + 1));
+      if (!batch_reduce(a, round, FinBatchRefresh(), counts)) return;
+      n_active = counts[0];
+    }
+  }
+
+  // v back to FP64; position update; velocity change (all meshes)
+  for (long i = nr.beg + lane; i < nr.end; i += 32) {
+    if (a.fixed[i]) continue;
+    const float4 vh = a.v_f[i], vl = a.v_lo[i];
+    const double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
+    float dv[3];
+    for (int c = 0; c < 3; ++c) {
+      dv[c] = float(v3[c] - a.v[3 * i + c]);
+      a.v[3 * i + c] = v3[c];
+      a.x[3 * i + c] += v3[c] * a.dt;
+    }
+    a.dv_last[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // batch summary: the largest iteration count and relative residual, the
+    // worst status
+    int its = 0, st = ld_status(&a.sync->status), warn = 0;
+    double rel = 0.0, rel0 = 0.0;
+    for (int m = 0; m < M; ++m) {
+      BatchMesh& b = a.bm[m];
+      if (b.status == 0 && !b.converged) b.status = OTFEM_WARN_NOT_CONVERGED;
+      if (b.status < 0 && st == 0) st = b.status;
+      if (b.status > 0) warn = 1;
+      its = its > b.iterations ? its : b.iterations;
+      const double bb = b.bnorm2 > 0.0 ? b.bnorm2 : 1.0;
+      rel = fmax(rel, b.rho / bb);
+      rel0 = fmax(rel0, b.rho0 / bb);
+    }
+    a.stats->iterations = its;
+    a.stats->applies = sweeps;
+    a.stats->status = st != 0 ? st : (warn ? OTFEM_WARN_NOT_CONVERGED : 0);
+    a.stats->rr = rel;
+    a.stats->rr0 = rel0;
+    a.stats->bb = 1.0;
+  }
+}
+
 // K1, mixed: FP32 orientation and elastic forces.  Edge differences of the
 // FP64 current and model coordinates are taken in FP64, then rounded.  The
 // rows of E^-1 are -b_k (fem_compute_b.h), so F = -sum_k e'_k (x) b_k, which
@@ -1668,7 +2108,8 @@ cudaError_t build_patches(Context& c, const int32_t* tets) {
     return e;
   // kernels that stage patches may need more than the default 48 KB
   const void* fns[] = {cg_kernel<float>(), cg_kernel<double>(), reinterpret_cast<const void*>(&k_apply_sweep<float>),
-                       reinterpret_cast<const void*>(&k_apply_sweep<double>)};
+                       reinterpret_cast<const void*>(&k_apply_sweep<double>),
+                       reinterpret_cast<const void*>(&k_cg_batch)};
   for (const void* f : fns)
     if ((e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(c.apply_smem))) != cudaSuccess)
       return e;
@@ -1689,10 +2130,11 @@ void staged_tiles(Context& c) {
 }
 
 int mixed_grid_shape(Context& c, int* grid, int* block) {
-  int occ32 = 0, occ64 = 0;
+  int occ32 = 0, occ64 = 0, occb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, k_cg_mixed, kBlock, c.apply_smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, k_cg_fp64, kBlock, c.apply_smem);
-  int occ = occ32 < occ64 ? occ32 : occ64;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, k_cg_batch, kBlock, c.apply_smem);
+  int occ = std::min(occ32, std::min(occ64, occb));
   if (occ < 1) occ = 1;
   if (occ > 2) occ = 2;
   *grid = c.num_sms * occ;
@@ -1751,9 +2193,14 @@ cudaError_t autotune_apply(Context& c) {
   if ((e = cudaEventCreate(&e1)) != cudaSuccess) return e;
   const int saved = c.apply_variant;
   int best = 0;
+  if (c.num_meshes > 1) best = kApplyTets;
   for (int v = 0; v < kApplyVariants; ++v) {
     c.apply_variant = v;
     float best_ms = 1e30f;
+    if (c.num_meshes > 1 && v != kApplyTets && v != kApplyStaged) {
+      c.apply_ms[v] = 0.0;  // batches use the variants that take mesh masks
+      continue;
+    }
     for (int rep = 0; rep < 3; ++rep) {
       launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1);
       cudaEventRecord(e0, c.stream);
@@ -1765,7 +2212,7 @@ cudaError_t autotune_apply(Context& c) {
       best_ms = std::min(best_ms, ms / 4.f);
     }
     c.apply_ms[v] = best_ms;
-    if (best_ms < c.apply_ms[best]) best = v;
+    if (best_ms < c.apply_ms[best] || c.apply_ms[best] <= 0.0) best = v;
   }
   (void)saved;
   c.apply_variant = best;
@@ -1832,6 +2279,12 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
   a.warm_dv = prm.warm_start == OTFEM_WARM_START_LEARNED ? c.warm_dv : nullptr;
   a.dv_last = c.dv_last;
+  a.num_meshes = c.num_meshes;
+  a.mesh_of_node = c.mesh_of_node;
+  a.mesh_of_tet = c.mesh_of_tet;
+  a.bm = c.bmesh;
+  a.bacc = c.bacc;
+  a.bmask = c.bmask;
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
 }
 
@@ -1859,6 +2312,26 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
 // at zero, as a solver launch does.
 static cudaError_t reset_tile_tickets(Context& c) {
   return cudaMemsetAsync(&c.sync->tile_ticket, 0, sizeof(unsigned), c.stream);
+}
+
+cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params& prm) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.bacc, 0, sizeof(double) * 8 * size_t(c.num_meshes), c.stream)) != cudaSuccess) return e;
+  MixedArgs a;
+  fill_args(a, c, dt, prm);
+  void* args[] = {&a};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c.mf_grid);
+  cfg.blockDim = dim3(c.mf_block);
+  cfg.dynamicSmemBytes = c.apply_smem;
+  cfg.stream = c.stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_cg_batch), args);
 }
 
 cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps) {
