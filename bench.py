@@ -273,6 +273,143 @@ def tip_load(coord, amp, freq, d, t):
     return f
 
 
+def timed_steps(lib, capi, torch, stream, h, params, steps, forces, dt, flush_l2, stats_fn=None):
+    """Steps with per-step external forces forces(k) (host arrays), timed on
+    the device; returns seconds and per-step iteration counts."""
+    st = capi.StepStats()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    its = []
+    for k in range(steps):
+        f = forces(k)
+        capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(_dp), f.size))
+        flush_l2()
+        ev[k][0].record(stream)
+        capi.check(lib.otfem_simulate_ex(h, dt, 1, ctypes.byref(params), ctypes.byref(st)))
+        ev[k][1].record(stream)
+        capi.check(lib.otfem_last_stats(h, ctypes.byref(st)))
+        its.append(st.iterations if stats_fn is None else stats_fn())
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / 1e3, its
+
+
+def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
+    """Learned vs plain (and extrapolation) on a 64x16x16 beam under a
+    sinusoidal tip load (amplitude U[0,100] N, frequency U[0.5,5] Hz,
+    direction uniform), dt 0.01."""
+    from opentissue_gb300.fem import generate_blocks
+    from opentissue_gb300.warmstart import WarmStartNet, extrapolation_state
+    I, J, K = 64, 16, 16
+    tets, coord = generate_blocks(I, J, K, 0.1, 0.1, 0.1)
+    coord = coord + np.random.default_rng(args.seed + 5).uniform(-0.01, 0.01, coord.shape)
+    fixed = (np.arange(coord.shape[0]) < (J + 1) * (K + 1)).astype(np.uint8)
+    amp, freq = float(rng.uniform(0, 100)), float(rng.uniform(0.5, 5))
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    tip = np.arange(coord.shape[0]) >= I * (J + 1) * (K + 1)
+    w = WORKLOAD
+    extrap = WarmStartNet(capacity=0, seed=0)
+    extrap.set_state(extrapolation_state(net.state()))
+    out = {}
+    for name, mlp, warm in (("plain", None, capi.WARM_START_PREVIOUS), ("extrapolation", extrap, capi.WARM_START_LEARNED),
+                            ("learned", net, capi.WARM_START_LEARNED)):
+        h = make_handle(lib, capi, tets, coord, fixed, stream)
+        if mlp is not None:
+            mlp.attach(h)
+            if mlp is extrap:
+                capi.check(lib.otfem_set_warm_start_smoothing(h, 0))
+        mass = get_mass(lib, capi, h, coord.shape[0])
+        g = gravity(mass, fixed)
+        p = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                max_iterations=5000, refresh_period=16, warm_start=warm)
+
+        def forces(k):
+            f = g.copy()
+            f[tip] += amp * np.sin(2 * np.pi * freq * k * 0.01) * d / tip.sum()
+            return f
+        sec, its = timed_steps(lib, capi, torch, stream, h, p, args.ab_steps, forces, 0.01, flush_l2)
+        x = np.zeros((coord.shape[0], 3))
+        capi.check(lib.otfem_get_nodes(h, capi.COORD, x.ctypes.data_as(_dp), x.size))
+        out[name] = {"tet_steps_per_s": tets.shape[0] * args.ab_steps / sec, "iterations_per_step": float(np.mean(its)),
+                     "x": x}
+        if mlp is not None:
+            mlp.detach(h)
+        capi.check(lib.otfem_destroy(h))
+    extrap.close()
+    disp = np.abs(out["plain"]["x"] - coord).max()
+    res = {"workload": f"64x16x16 beam ({tets.shape[0]} tets), tip load {amp:.1f} N sin(2 pi {freq:.2f} t), "
+                       f"{args.ab_steps} steps, dt 0.01, rel. residual 1e-6"}
+    for k, v in out.items():
+        res[k] = {"tet_steps_per_s": v["tet_steps_per_s"], "iterations_per_step": v["iterations_per_step"]}
+        if k != "plain":
+            res[k]["position_difference_vs_plain"] = float(np.abs(v["x"] - out["plain"]["x"]).max() / disp)
+    res["learned_over_plain"] = out["learned"]["tet_steps_per_s"] / out["plain"]["tet_steps_per_s"]
+    return res
+
+
+def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
+    """256 beams of uneven size (nx U{8..64}, ny, nz U{3..16}), per-beam
+    material, random fixed face, gravity plus a tip force, dt 0.005, one
+    persistent launch per step: plain (constant tip force), then plain and
+    learned under a sinusoidal tip force."""
+    from opentissue_gb300.workloads import random_beams
+    beams = random_beams(args.batch_meshes, seed=args.seed)
+    descs = (capi.MeshDesc * len(beams))()
+    keep = []
+    for k, b in enumerate(beams):
+        tets = np.ascontiguousarray(b["tets"], np.int32)
+        coord = np.ascontiguousarray(b["coord"], np.float64)
+        fixed = np.ascontiguousarray(b["fixed"], np.uint8)
+        keep += [tets, coord, fixed]
+        descs[k] = capi.MeshDesc(coord.shape[0], tets.shape[0], tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                 coord.ctypes.data_as(_dp), coord.ctypes.data_as(_dp),
+                                 fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    T = sum(b["tets"].shape[0] for b in beams)
+    N = sum(b["coord"].shape[0] for b in beams)
+    fixed_all = np.concatenate([b["fixed"] for b in beams])
+    tipf = np.concatenate([b["tip_force"] for b in beams])
+    freqs = np.concatenate([np.full(b["coord"].shape[0], rng.uniform(0.5, 5)) for b in beams])
+    w = WORKLOAD
+    res = {"workload": f"{len(beams)} beams, {T} tets, {N} nodes, dt 0.005, rel. residual 1e-6"}
+    for name, warm, vary in (("plain", capi.WARM_START_PREVIOUS, False), ("plain_tip_sine", capi.WARM_START_PREVIOUS, True),
+                             ("learned_tip_sine", capi.WARM_START_LEARNED, True)):
+        h = ctypes.c_void_p()
+        t0 = time.perf_counter()
+        capi.check(lib.otfem_batch_create(descs, len(beams), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
+        e = np.array([b["young"] for b in beams])
+        nu = np.array([b["poisson"] for b in beams])
+        rho = np.array([b["density"] for b in beams])
+        capi.check(lib.otfem_batch_init(h, e.ctypes.data_as(_dp), nu.ctypes.data_as(_dp), rho.ctypes.data_as(_dp),
+                                        1e30, 0.0, 0.0))
+        setup_s = time.perf_counter() - t0
+        if warm == capi.WARM_START_LEARNED:
+            net.attach(h)
+        mass = get_mass(lib, capi, h, N)
+        g = gravity(mass, fixed_all)
+        p = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                max_iterations=5000, refresh_period=16, warm_start=warm)
+
+        def forces(k):
+            f = g + (tipf * np.sin(2 * np.pi * freqs * k * 0.005)[:, None] if vary else tipf)
+            f[fixed_all == 1] = 0.0
+            return f
+        steps = args.batch_steps
+        timed_steps(lib, capi, torch, stream, h, p, args.warmup, forces, 0.005, flush_l2)
+        sec, its = timed_steps(lib, capi, torch, stream, h, p, steps, lambda k: forces(k + args.warmup), 0.005,
+                               flush_l2)
+        M = len(beams)
+        mi = np.zeros(M, np.int32)
+        capi.check(lib.otfem_batch_stats(h, mi.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), None, None, None))
+        res[name] = {"tet_steps_per_s": T * steps / sec, "ms_per_step": 1e3 * sec / steps,
+                     "max_iterations_per_step": float(np.mean(its)),
+                     "mesh_iterations_last_step": {"mean": float(mi.mean()), "min": int(mi.min()), "max": int(mi.max())},
+                     "setup_s": round(setup_s, 2)}
+        if warm == capi.WARM_START_LEARNED:
+            net.detach(h)
+        capi.check(lib.otfem_destroy(h))
+    res["learned_over_plain_tip_sine"] = res["learned_tip_sine"]["tet_steps_per_s"] / res["plain_tip_sine"]["tet_steps_per_s"]
+    return res
+
+
 def run_ours(args, world, rank, local):
     import torch
     from opentissue_gb300 import build as ext_build
@@ -420,6 +557,12 @@ def run_ours(args, world, rank, local):
     e2e_s = dist_max(world, sum(e2e_ms) / 1e3)
     dist_barrier(world)
 
+    # ---- the other measured configurations (outside the headline timing) ---
+    extra = {}
+    if not args.no_extra:
+        extra["inference_ab_64x16x16"] = run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng)
+        extra["batch"] = run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng)
+
     total_tet_steps = T * args.steps * world
     value = total_tet_steps / r_learn["dev_s"]
     plain_value = total_tet_steps / r_plain["dev_s"]
@@ -444,7 +587,8 @@ def run_ours(args, world, rank, local):
                              "max_rel_residual": float(np.max(r_plain["res"]))},
                    "learned_over_plain": value / plain_value,
                    "position_difference_learned_vs_plain": pos_diff,
-                   "training": train_info},
+                   "training": train_info,
+                   "other_configurations": extra},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "k_cg_mixed", "peak_source": peak_note,
                      "algorithmic_bytes_per_launch": float(np.mean(cg_bytes)),
@@ -484,6 +628,10 @@ def main():
     ap.add_argument("--train-steps", type=int, default=40)
     ap.add_argument("--train-epochs", type=int, default=60)
     ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--ab-steps", type=int, default=200)
+    ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--no-extra", action="store_true")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = WORKLOADS[args.workload]

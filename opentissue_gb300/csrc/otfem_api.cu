@@ -59,7 +59,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.features, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.warm_ops, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -430,7 +430,7 @@ int otfem_batch_create(const otfem_mesh_desc* meshes, int32_t count, void* strea
   if (e == cudaSuccess) e = cudaMalloc(&c.mesh_of_tet, sizeof(int) * mot.size());
   if (e == cudaSuccess) e = cudaMalloc(&c.bmesh, sizeof(otfem::BatchMesh) * size_t(count));
   if (e == cudaSuccess) e = cudaMallocHost(&c.bmesh_host, sizeof(otfem::BatchMesh) * size_t(count));
-  if (e == cudaSuccess) e = cudaMalloc(&c.bacc, sizeof(double) * 8 * size_t(count));
+  if (e == cudaSuccess) e = cudaMalloc(&c.bacc, sizeof(double) * 16 * size_t(count));
   if (e == cudaSuccess) e = cudaMalloc(&c.bmask, 3 * size_t(count));
   if (e == cudaSuccess) e = cudaMemcpy(c.mesh_of_node, mon.data(), sizeof(int) * mon.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(c.mesh_of_tet, mot.data(), sizeof(int) * mot.size(), cudaMemcpyHostToDevice);

@@ -13,7 +13,7 @@
 namespace otfem {
 
 // Per-CTA partial sums written before a grid barrier (one slot per scalar).
-constexpr int kMaxPartials = 8;
+constexpr int kMaxPartials = 16;
 // Rows of the per-iteration CG trace kept per step.  Each row holds
 // kTraceCols doubles: rho, p.q, alpha, beta, then SM-clock stamps (cycles
 // since the kernel started, taken on CTA 0) after the apply sweep, after its
@@ -34,7 +34,7 @@ struct DeviceSync {
   int pad2[31];
   double result[2][4];       // grid-sum results, double-buffered by barrier parity
   double pad3[8];
-  double acc[2][4];          // grid-sum accumulators (FP64 reductions), by barrier parity
+  double acc[2][8];          // grid-sum accumulators (FP64 reductions), by barrier parity
   double pad4[8];
   unsigned tile_ticket;      // staged apply: monotonic tile tickets
   unsigned pad5[31];
@@ -42,7 +42,7 @@ struct DeviceSync {
 
 // Per-mesh state of a batched solve (device memory, one per mesh).
 struct BatchMesh {
-  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta;
+  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta, gamma_d, gamma_c;
   int active, restart, stalls, iterations, applies, status, converged, pad;
 };
 
@@ -140,6 +140,9 @@ struct Context {
   float4* dv_last = nullptr;      // N (w unused)
   float4* warm_dv = nullptr;      // N
   float4* warm_tmp = nullptr;     // N, allocated with smoothing passes
+  // learned start, projected: operands d = dv_prev, c = the network's
+  // correction and their products A d, A c (4N, allocated with a network)
+  float4* warm_ops = nullptr;
   int warm_smoothing = 4;         // 1-ring mean passes over the network's correction
   float* features = nullptr;      // N x kFeatureStride, allocated when collecting
   int collect = 0;
@@ -153,7 +156,7 @@ struct Context {
   int* mesh_of_tet = nullptr;                     // T
   BatchMesh* bmesh = nullptr;                     // num_meshes
   BatchMesh* bmesh_host = nullptr;                // num_meshes, pinned
-  double* bacc = nullptr;                         // 2 x num_meshes x 4 accumulators
+  double* bacc = nullptr;                         // 2 x num_meshes x 8 accumulators
   unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
@@ -228,7 +231,7 @@ cudaError_t launch_apply_operator_scratch(Context& c, int solver, double dt, dou
                                           double* y, void* scratch);
 // `sweeps` element-apply sweeps on the resident operand (no host transfer):
 // the apply kernel alone, for timing.
-cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps);
+cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps, bool masked = false);
 int mixed_grid_shape(Context& c, int* grid, int* block);
 
 }  // namespace otfem

@@ -116,8 +116,9 @@ struct MixedArgs {
   const float* tile_f;                  // staged apply tiles (see Context::tile_f)
   int tile_tets, num_tiles;
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
-  const float4* warm_dv;                // learned initial guess v + warm_dv (null: v)
-  float4* dv_last;                      // out: v_new - v_old per free node
+  const float4* warm_dv;                // learned guess v + warm_dv (null: plain start from v)
+  float4* dv_last;                      // in: dv_prev; out: v_new - v_old per free node
+  float4 *wd, *wc, *ad, *ac;            // learned start: operands d, c and products A d, A c
   // batched solve (see Context)
   int num_meshes;
   const int* mesh_of_node;
@@ -125,6 +126,7 @@ struct MixedArgs {
   BatchMesh* bm;
   double* bacc;
   unsigned char* bmask;
+  const unsigned char* sweep_mask;      // standalone sweeps of a batch (autotuner): meshes to apply
   long long spin_limit;
 };
 
@@ -351,11 +353,11 @@ struct AccOps<DF> {
 template <typename Acc, int NV, int NO, typename Fin>
 __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&out)[NO], unsigned& round,
                             Fin fin) {
-  static_assert(2 * NV <= kMaxPartials && NO <= 4 && NV <= 4, "partials too small");
+  static_assert(2 * NV <= kMaxPartials && NO <= 4 && NV <= 8, "partials too small");
   typedef AccOps<Acc> Ops;
   constexpr int kWarps = kBlock / 32;
   __shared__ Acc s_warp[kWarps][NV];
-  __shared__ double s_tot[4];
+  __shared__ double s_tot[8];
   __shared__ double s_res[4];
   __shared__ int s_flag;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -479,6 +481,32 @@ struct FinAlphaBetaExact {
     if (o[3] == 0.0 && !isfinite(t[3])) o[3] = 1.0;
     if (restart || (prev_est >= 0.0 && fabs(prev_est - t[3]) > 0.25 * t[3])) o[1] = 0.0;
   }
+};
+
+// The learned start, projected: CG starts from the point of least energy
+// x.A.x/2 - b.x on v + span{d, c} (d = dv_prev, c = the network's
+// correction).  The plane holds the plain start v (the judge of the learned
+// guess), the extrapolation v + d and the network's guess v + d + c, so the
+// start is never worse than any of them in the energy norm.  Totals: d.Ad,
+// d.Ac, c.Ac, d.r, c.r with r = b - A v; outputs gamma_d, gamma_c.
+__device__ __forceinline__ void warm_projection(const double* t, double& gd, double& gc) {
+  const double dd = t[0], dc = t[1], cc = t[2], dr = t[3], cr = t[4];
+  gd = gc = 0.0;
+  const bool okd = dd > 0.0 && isfinite(dd) && isfinite(dr);
+  const bool okc = cc > 0.0 && isfinite(cc) && isfinite(cr);
+  const double det = dd * cc - dc * dc;
+  if (okd && okc && isfinite(dc) && det > 1e-10 * dd * cc) {
+    gd = (dr * cc - cr * dc) / det;
+    gc = (cr * dd - dr * dc) / det;
+  } else {
+    // (nearly) one direction: the one that lowers the energy most, x.r^2 / x.Ax
+    const double ed = okd ? dr * dr / dd : -1.0, ec = okc ? cr * cr / cc : -1.0;
+    if (okd && ed >= ec) gd = dr / dd;
+    else if (okc) gc = cr / cc;
+  }
+}
+struct FinWarm {
+  __device__ void operator()(const double* t, double* o) const { warm_projection(t, o[0], o[1]); }
 };
 
 // Coherent (L2) load of node data written by other CTAs within the launch.
@@ -1011,37 +1039,90 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     }
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
-    // never accumulated (w = 0).  A learned warm start moves the initial
-    // guess of free nodes by the predicted velocity change.
-    if (a.warm_dv && !fx) {
-      const float4 w = a.warm_dv[i];
-      vi[0] += double(w.x), vi[1] += double(w.y), vi[2] += double(w.z);
-    }
+    // never accumulated (w = 0).
     store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     a.q_f[i] = zero4;
+    if (a.wd) {
+      // learned start: directions d = dv_prev and c = the network's correction
+      const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
+      const float fw = fx ? 0.f : 1.f;
+      a.wd[i] = make_float4(d.x, d.y, d.z, fw);
+      a.wc[i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fw);
+      a.ad[i] = zero4;
+      a.ac[i] = zero4;
+    }
   }
   double tot[1];
   if (!grid_reduce<DF, 1, 1>(a, bbsum, tot, round, FinIdentity1())) return;
   const double bnorm2 = tot[0];
   const double thresh = a.rtol * a.rtol * bnorm2;
 
-  // Initial residual r = b - A v (FP64), p = r.
+  // Initial residual r = b - A v (FP64), p = r; with the learned start also
+  // A d and A c, and the start moves to v + gamma_d d + gamma_c c.
+  int applies = 1;
   apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+  if (a.wd) {
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    apply_sweep<float>(a, a.wd, nullptr, a.ad, a.re_f, a.b_f, a.c_f, scale, smem);
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    apply_sweep<float>(a, a.wc, nullptr, a.ac, a.re_f, a.b_f, a.c_f, scale, smem);
+    applies += 2;
+  }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  double gam[2] = {0.0, 0.0};
+  if (a.wd) {
+    DF s5[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (long i = gtid; i < N; i += gstride) {
+      if (a.fixed[i]) continue;
+      const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+      const double dg = a.diag[i];
+      float rf[3];
+      rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
+      rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
+      rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
+      const float df = float(dg);
+      const float4 d = a.wd[i], c = a.wc[i], ad4 = load_acc(a.ad + i), ac4 = load_acc(a.ac + i);
+      const float adx = df * d.x + ad4.x, ady = df * d.y + ad4.y, adz = df * d.z + ad4.z;
+      const float acx = df * c.x + ac4.x, acy = df * c.y + ac4.y, acz = df * c.z + ac4.z;
+      s5[0] = df_add(s5[0], DF{d.x * adx + d.y * ady + d.z * adz, 0.f});
+      s5[1] = df_add(s5[1], DF{d.x * acx + d.y * acy + d.z * acz, 0.f});
+      s5[2] = df_add(s5[2], DF{c.x * acx + c.y * acy + c.z * acz, 0.f});
+      s5[3] = df_add(s5[3], DF{d.x * rf[0] + d.y * rf[1] + d.z * rf[2], 0.f});
+      s5[4] = df_add(s5[4], DF{c.x * rf[0] + c.y * rf[1] + c.z * rf[2], 0.f});
+      a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+      a.ad[i] = make_float4(adx, ady, adz, 0.f);
+      a.ac[i] = make_float4(acx, acy, acz, 0.f);
+    }
+    if (!grid_reduce<DF, 5, 2>(a, s5, gam, round, FinWarm())) return;
+  }
   DF rr[1] = {{0.f, 0.f}};
+  const float gd = float(gam[0]), gc = float(gam[1]);
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) {
       a.p_f[i] = zero4;
       a.r_f[i] = zero4;
       continue;
     }
-    float4 q4 = load_acc(a.q_f + i);
-    float4 vh = a.v_f[i], vl = a.v_lo[i];
-    double d = a.diag[i];
     float rf[3];
-    rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-    rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-    rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+    if (a.wd) {
+      // v += gamma_d d + gamma_c c; r -= gamma_d A d + gamma_c A c
+      const float4 d = a.wd[i], c = a.wc[i], ad4 = a.ad[i], ac4 = a.ac[i], r4 = a.r_f[i];
+      float4 vh = a.v_f[i], vl = a.v_lo[i];
+      df_inc(vh.x, vl.x, gd * d.x + gc * c.x);
+      df_inc(vh.y, vl.y, gd * d.y + gc * c.y);
+      df_inc(vh.z, vl.z, gd * d.z + gc * c.z);
+      a.v_f[i] = vh;
+      a.v_lo[i] = vl;
+      rf[0] = r4.x - (gd * ad4.x + gc * ac4.x);
+      rf[1] = r4.y - (gd * ad4.y + gc * ac4.y);
+      rf[2] = r4.z - (gd * ad4.z + gc * ac4.z);
+    } else {
+      const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+      const double d = a.diag[i];
+      rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+      rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+      rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+    }
     a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
     a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
     a.q_f[i] = zero4;
@@ -1050,7 +1131,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   if (!grid_reduce<DF, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
   double rho = tot[0];
   const double rho0 = rho;
-  int it = 0, applies = 1;
+  int it = 0;
   bool converged = rho <= thresh;
   // recurrence check and restarts (FinAlphaBetaExact); stagnation of the
   // true residual at the refreshes ends the solve unconverged
@@ -1339,6 +1420,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
 // with one FP64 atomic per value and mesh.
 
 constexpr int kMaskApply = 0, kMaskUpdate = 1, kMaskRefresh = 2;
+constexpr int kBatchSlots = 8;  // accumulators per mesh and round
 
 struct NodeRange {
   long beg, end;
@@ -1369,7 +1451,7 @@ struct SegSum {
       DF x = acc[k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x = AccOps<DF>::add(x, AccOps<DF>::shfl_down(x, o));
-      if ((threadIdx.x & 31) == 0 && cur >= 0) atomicAdd(&acc_half[4 * cur + k], AccOps<DF>::to_double(x));
+      if ((threadIdx.x & 31) == 0 && cur >= 0) atomicAdd(&acc_half[kBatchSlots * cur + k], AccOps<DF>::to_double(x));
       acc[k] = DF{0.f, 0.f};
     }
   }
@@ -1392,8 +1474,8 @@ struct SegSum {
   }
 };
 
-// Grid barrier whose last CTA runs fin(a, mesh, totals[4], counts) for every
-// mesh (totals: this round's accumulators, which it clears) and publishes
+// Grid barrier whose last CTA runs fin(a, mesh, totals[kBatchSlots], counts)
+// for every mesh (totals: this round's accumulators, which it clears) and publishes
 // the 4 integer counts the finisher accumulates (e.g. meshes still active).
 template <typename Fin>
 __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (&counts)[4]) {
@@ -1406,13 +1488,13 @@ __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0;
   __syncthreads();
   if (s_flag) {
-    double* acc = a.bacc + size_t(half) * a.num_meshes * 4;
+    double* acc = a.bacc + size_t(half) * a.num_meshes * kBatchSlots;
     for (int m = threadIdx.x; m < a.num_meshes; m += blockDim.x) {
-      double t[4];
+      double t[kBatchSlots];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        t[k] = __ldcg(acc + 4 * m + k);
-        acc[4 * m + k] = 0.0;  // for round r + 2
+      for (int k = 0; k < kBatchSlots; ++k) {
+        t[k] = __ldcg(acc + kBatchSlots * m + k);
+        acc[kBatchSlots * m + k] = 0.0;  // for round r + 2
       }
       fin(a, m, t, s_cnt);
     }
@@ -1446,6 +1528,13 @@ struct FinBatchInit {
   }
 };
 
+// totals: d.Ad, d.Ac, c.Ac, d.r, c.r (learned start, projected per mesh)
+struct FinBatchWarm {
+  __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
+    warm_projection(t, a.bm[m].gamma_d, a.bm[m].gamma_c);
+  }
+};
+
 // totals: |r0|^2 of the initial guess
 struct FinBatchStart {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
@@ -1453,7 +1542,7 @@ struct FinBatchStart {
     b.rho = b.rho0 = b.best_true = b.est = t[0];
     b.prev_est = -1.0;
     b.restart = b.stalls = b.iterations = 0;
-    b.applies = 1;
+    b.applies = a.wd ? 3 : 1;
     b.status = isfinite(t[0]) && isfinite(b.bnorm2) ? 0 : OTFEM_ERR_NONFINITE;
     b.converged = b.status == 0 && t[0] <= b.thresh;
     b.active = b.status == 0 && !b.converged && a.max_it > 0;
@@ -1493,7 +1582,9 @@ struct FinBatchIter {
     ++b.iterations;
     ++b.applies;
     mk[kMaskUpdate * M + m] = 1;
-    const bool refresh = (a.refresh > 0 && b.iterations % a.refresh == 0) || o[2] <= b.thresh;
+    // a mesh whose estimate reached the tolerance refreshes at the next
+    // multiple of 4 iterations, so the meshes share refresh sweeps
+    const bool refresh = (a.refresh > 0 && b.iterations % a.refresh == 0) || (o[2] <= b.thresh && b.iterations % 4 == 0);
     if (refresh) {
       mk[kMaskRefresh * M + m] = 1;
       ++b.applies;
@@ -1547,7 +1638,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   const unsigned char* mask_refresh = a.bmask + kMaskRefresh * M;
   int counts[4];
   int sweeps = 0;
-  auto acc_half = [&](unsigned next_round) { return a.bacc + size_t(next_round & 1u) * M * 4; };
+  auto acc_half = [&](unsigned next_round) { return a.bacc + size_t(next_round & 1u) * M * kBatchSlots; };
 
   // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess), q = 0
   {
@@ -1579,15 +1670,19 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           const float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
           bb[0] = bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2];
           a.diag[i] = mass + a.dt * (a.alpha * mass);
-          if (a.warm_dv) {
-            const float4 w = a.warm_dv[i];
-            vi[0] += double(w.x), vi[1] += double(w.y), vi[2] += double(w.z);
-          }
         } else {
           a.diag[i] = 0.0;
         }
         store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
         a.q_f[i] = zero4;
+        if (a.wd) {
+          const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
+          const float fw = fx ? 0.f : 1.f;
+          a.wd[i] = make_float4(d.x, d.y, d.z, fw);
+          a.wc[i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fw);
+          a.ad[i] = zero4;
+          a.ac[i] = zero4;
+        }
       }
       ss.add(valid, m, bb, acc_half(round + 1));
     }
@@ -1595,10 +1690,54 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   }
   if (!batch_reduce(a, round, FinBatchInit(), counts)) return;
 
-  // initial residual r = b - A v (FP64), p = r, for every mesh
+  // initial residual r = b - A v (FP64), p = r, for every mesh; with the
+  // learned start also A d, A c and each mesh's projected start
   apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   ++sweeps;
+  if (a.wd) {
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    apply_sweep<float>(a, a.wd, nullptr, a.ad, a.re_f, a.b_f, a.c_f, scale, smem);
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    apply_sweep<float>(a, a.wc, nullptr, a.ac, a.re_f, a.b_f, a.c_f, scale, smem);
+    sweeps += 2;
+  }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  if (a.wd) {
+    SegSum<5> ss;
+    ss.start(first_mesh);
+    for (long base = nr.beg; base < nr.end; base += 32) {
+      const long i = base + lane;
+      const bool valid = i < nr.end;
+      int m = -1;
+      float s5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (valid) {
+        m = a.mesh_of_node[i];
+        if (!a.fixed[i]) {
+          const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+          const double dg = a.diag[i];
+          float rf[3];
+          rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
+          rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
+          rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
+          const float df = float(dg);
+          const float4 d = a.wd[i], c = a.wc[i], ad4 = load_acc(a.ad + i), ac4 = load_acc(a.ac + i);
+          const float adx = df * d.x + ad4.x, ady = df * d.y + ad4.y, adz = df * d.z + ad4.z;
+          const float acx = df * c.x + ac4.x, acy = df * c.y + ac4.y, acz = df * c.z + ac4.z;
+          s5[0] = d.x * adx + d.y * ady + d.z * adz;
+          s5[1] = d.x * acx + d.y * acy + d.z * acz;
+          s5[2] = c.x * acx + c.y * acy + c.z * acz;
+          s5[3] = d.x * rf[0] + d.y * rf[1] + d.z * rf[2];
+          s5[4] = c.x * rf[0] + c.y * rf[1] + c.z * rf[2];
+          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+          a.ad[i] = make_float4(adx, ady, adz, 0.f);
+          a.ac[i] = make_float4(acx, acy, acz, 0.f);
+        }
+      }
+      ss.add(valid, m, s5, acc_half(round + 1));
+    }
+    ss.flush(acc_half(round + 1));
+    if (!batch_reduce(a, round, FinBatchWarm(), counts)) return;
+  }
   {
     SegSum<1> ss;
     ss.start(first_mesh);
@@ -1613,12 +1752,26 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           a.p_f[i] = zero4;
           a.r_f[i] = zero4;
         } else {
-          const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-          const double d = a.diag[i];
           float rf[3];
-          rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-          rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-          rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+          if (a.wd) {
+            const float gd = float(a.bm[m].gamma_d), gc = float(a.bm[m].gamma_c);
+            const float4 d = a.wd[i], c = a.wc[i], ad4 = a.ad[i], ac4 = a.ac[i], r4 = a.r_f[i];
+            float4 vh = a.v_f[i], vl = a.v_lo[i];
+            df_inc(vh.x, vl.x, gd * d.x + gc * c.x);
+            df_inc(vh.y, vl.y, gd * d.y + gc * c.y);
+            df_inc(vh.z, vl.z, gd * d.z + gc * c.z);
+            a.v_f[i] = vh;
+            a.v_lo[i] = vl;
+            rf[0] = r4.x - (gd * ad4.x + gc * ac4.x);
+            rf[1] = r4.y - (gd * ad4.y + gc * ac4.y);
+            rf[2] = r4.z - (gd * ad4.z + gc * ac4.z);
+          } else {
+            const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+            const double d = a.diag[i];
+            rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
+            rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
+            rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+          }
           a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
           a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
           a.q_f[i] = zero4;
@@ -1979,7 +2132,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_apply_sweep(MixedArgs a, const ty
   const R* bb = sizeof(R) == 4 ? (const R*)a.b_f : (const R*)a.b_d;
   const R* cc = sizeof(R) == 4 ? (const R*)a.c_f : (const R*)a.c_d;
   extern __shared__ __align__(16) unsigned char smem[];
-  apply_sweep<R>(a, u, ulo, q, re, bb, cc, R(a.dt * a.dt), smem);
+  apply_sweep<R>(a, u, ulo, q, re, bb, cc, R(a.dt * a.dt), smem, a.sweep_mask);
 }
 
 template <typename V4>
@@ -2193,7 +2346,13 @@ cudaError_t autotune_apply(Context& c) {
   if ((e = cudaEventCreate(&e1)) != cudaSuccess) return e;
   const int saved = c.apply_variant;
   int best = 0;
-  if (c.num_meshes > 1) best = kApplyTets;
+  if (c.num_meshes > 1) {
+    best = kApplyTets;
+    // batches time masked sweeps: every fourth mesh, as late in a step
+    std::vector<unsigned char> mask(size_t(3) * c.num_meshes, 0);
+    for (int m = 0; m < c.num_meshes; m += 4) mask[size_t(m)] = 1;
+    if ((e = cudaMemcpy(c.bmask, mask.data(), mask.size(), cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  }
   for (int v = 0; v < kApplyVariants; ++v) {
     c.apply_variant = v;
     float best_ms = 1e30f;
@@ -2202,9 +2361,9 @@ cudaError_t autotune_apply(Context& c) {
       continue;
     }
     for (int rep = 0; rep < 3; ++rep) {
-      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1);
+      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1, true);
       cudaEventRecord(e0, c.stream);
-      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 4);
+      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 4, true);
       cudaEventRecord(e1, c.stream);
       if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
       float ms = 0.f;
@@ -2277,14 +2436,20 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.tile_tets = c.tile_tets;
   a.num_tiles = c.num_tiles;
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
-  a.warm_dv = prm.warm_start == OTFEM_WARM_START_LEARNED ? c.warm_dv : nullptr;
+  const bool learned = prm.warm_start == OTFEM_WARM_START_LEARNED && c.warm_ops;
+  a.warm_dv = learned ? c.warm_dv : nullptr;
   a.dv_last = c.dv_last;
+  a.wd = learned ? c.warm_ops : nullptr;
+  a.wc = learned ? c.warm_ops + c.N : nullptr;
+  a.ad = learned ? c.warm_ops + 2L * c.N : nullptr;
+  a.ac = learned ? c.warm_ops + 3L * c.N : nullptr;
   a.num_meshes = c.num_meshes;
   a.mesh_of_node = c.mesh_of_node;
   a.mesh_of_tet = c.mesh_of_tet;
   a.bm = c.bmesh;
   a.bacc = c.bacc;
   a.bmask = c.bmask;
+  a.sweep_mask = nullptr;
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
 }
 
@@ -2317,7 +2482,8 @@ static cudaError_t reset_tile_tickets(Context& c) {
 cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params& prm) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(c.bacc, 0, sizeof(double) * 8 * size_t(c.num_meshes), c.stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.bacc, 0, sizeof(double) * 2 * kBatchSlots * size_t(c.num_meshes), c.stream)) != cudaSuccess)
+    return e;
   MixedArgs a;
   fill_args(a, c, dt, prm);
   void* args[] = {&a};
@@ -2334,11 +2500,12 @@ cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params&
   return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_cg_batch), args);
 }
 
-cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps) {
+cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps, bool masked) {
   MixedArgs a;
   otfem_solver_params prm;
   otfem_default_params(&prm);
   fill_args(a, c, dt, prm);
+  if (masked && c.num_meshes > 1) a.sweep_mask = c.bmask;
   if (cudaError_t e = reset_tile_tickets(c)) return e;
   for (int k = 0; k < sweeps; ++k) {
     if (solver == OTFEM_SOLVER_FP64)

@@ -105,6 +105,19 @@ class WarmStartNet:
         capi.check(capi.lib().otfem_set_mlp(handle, None))
 
 
+# offsets in the network state (include/otfem_gpu.h, OTFEM_MLP_STATE_SIZE)
+_W4, _B4, _MU_Y = 9536, 9728, 9731 + 36
+
+
+def extrapolation_state(state):
+    """The state with the output layer and target mean zeroed: its guess is
+    v + dv_prev, the extrapolation of the velocity the network corrects."""
+    s = np.array(state, np.float32, copy=True)
+    s[_W4:_B4 + 3] = 0.0
+    s[_MU_Y:_MU_Y + 3] = 0.0
+    return s
+
+
 def node_features(handle, num_nodes):
     """The network inputs of every node in the handle's last step (N x 18)."""
     out = np.zeros((num_nodes, 18), np.float32)
