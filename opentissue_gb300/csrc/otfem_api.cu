@@ -148,8 +148,11 @@ std::string step_key(const Context& c, double dt, bool warp, const otfem_solver_
 
 int kernels_per_step(const Context& c, const otfem_solver_params& p) {
   if (p.solver == OTFEM_SOLVER_REFERENCE) return 1 + 2 + 2 + 1 + (1 + 5 * p.max_iterations + 1) + 1;
-  const bool features = p.warm_start == OTFEM_WARM_START_LEARNED || c.collect;
-  return 2 + (c.plastic_active ? 2 : 0) + (features ? 1 : 0);
+  const bool learned = p.warm_start == OTFEM_WARM_START_LEARNED;
+  const bool features = learned || c.collect;
+  // orientation, persistent solve, status merge; plasticity; network inputs
+  // and the smoothing passes of the learned start
+  return 3 + (c.plastic_active ? 2 : 0) + (features ? 1 : 0) + (learned ? c.warm_smoothing : 0);
 }
 
 }  // namespace
@@ -599,11 +602,12 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
     c.launches += 1 + (c.plastic_active ? 2 : 0);
     if ((e = launch_warm_start(c, p)) != cudaSuccess) return cuda_fail(e, "warm start");
     if (p.warm_start == OTFEM_WARM_START_LEARNED || c.collect) c.launches += 1;
+    if (p.warm_start == OTFEM_WARM_START_LEARNED) c.launches += c.warm_smoothing;
   } else if (phase == OTFEM_PHASE_SOLVE) {
     e = c.num_meshes > 1 ? otfem::launch_batch_solve(c, dt, p) : otfem::launch_mixed_solve(c, dt, p);
     if (e != cudaSuccess) return cuda_fail(e, "solve phase");
     OT_CUDA(cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream));
-    c.launches += 1;
+    c.launches += 2;
     c.last_solver = p.solver;
   } else {
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown phase");

@@ -179,6 +179,14 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+__device__ __forceinline__ void mbar_inval(unsigned long long* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses of shared memory (made
+// visible to it by a CTA barrier) before its following bulk copies into it.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
   unsigned done;
   asm volatile(
@@ -854,7 +862,9 @@ __device__ __forceinline__ int claim_tile(const MixedArgs& a) {
 // Variant kApplyStaged (FP32): as kApplyTets, but the per-tet data (node
 // ids, rotation quaternion, b_1..b_3, c0..c2: 80 bytes per tet) arrives in
 // shared memory by bulk copies, a tile of tile_tets tets at a time and one
-// tile ahead of the computation, so no thread waits on DRAM for it.  CTAs
+// tile ahead of the computation, so no thread waits on DRAM for it.  Each
+// sweep initialises its two mbarriers and invalidates them at the end (a
+// valid mbarrier must not be initialised again).  CTAs
 // claim tiles dynamically (claim_tile), so SMs that see more memory
 // bandwidth take more tiles.  On a copy that does not complete within
 // spin_limit cycles the CTA sets OTFEM_ERR_TIMEOUT, stops, and waits (again
@@ -929,6 +939,7 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
       if (next < 0) s_more = 0;
       s_tile[sb] = next;
       if (next >= 0) {
+        fence_proxy_async_smem();
         mbar_arm(&bar[sb], tile_bytes);
         bulk_copy_g2s(stage(sb), a.tile_f + size_t(next) * kTileWords * TT, tile_bytes, &bar[sb]);
       }
@@ -939,6 +950,12 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
     // the copies of claims j and j + 1 may still be arriving
     for (int k = j; k < j + 2; ++k)
       if (s_tile[k & 1] >= 0) mbar_wait(&bar[k & 1], (k >> 1) & 1, a.spin_limit);
+  }
+  // end of the barriers' life: the next sweep initialises them afresh
+  __syncthreads();
+  if (tid == 0) {
+    mbar_inval(&bar[0]);
+    mbar_inval(&bar[1]);
   }
 }
 
@@ -2453,6 +2470,19 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.spin_limit = 4000000000LL;  // clock cycles, about two seconds
 }
 
+// After a persistent solve: an error the grid recorded (a timed-out wait, a
+// non-finite scalar) reaches the step statistics even when the kernel left
+// before writing them.
+__global__ void k_merge_status(const DeviceSync* sync, DeviceStats* stats) {
+  const int st = sync->status;
+  if (st < 0) stats->status = st;
+}
+
+static cudaError_t merge_status(Context& c) {
+  k_merge_status<<<1, 1, 0, c.stream>>>(c.sync, c.stats);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& prm) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
@@ -2470,7 +2500,8 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   const void* fn = prm.solver == OTFEM_SOLVER_FP64 ? cg_kernel<double>() : cg_kernel<float>();
-  return cudaLaunchKernelExC(&cfg, fn, args);
+  if ((e = cudaLaunchKernelExC(&cfg, fn, args)) != cudaSuccess) return e;
+  return merge_status(c);
 }
 
 // Standalone element-apply launches start the staged apply's tile tickets
@@ -2497,7 +2528,8 @@ cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params&
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_cg_batch), args);
+  if ((e = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_cg_batch), args)) != cudaSuccess) return e;
+  return merge_status(c);
 }
 
 cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps, bool masked) {
