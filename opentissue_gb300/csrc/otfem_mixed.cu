@@ -1216,7 +1216,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) trace_row(a, row, rho, 0.0, sc[0], sc[1], stamp, t_start);
     rho = sc[2];
-    if ((a.refresh > 0 && it % a.refresh == 0) || sc[2] <= thresh) {
+    const bool periodic = a.refresh > 0 && it % a.refresh == 0;
+    if (periodic || sc[2] <= thresh) {
       // r = b - A v (residual replacement, FP64); q is zero here and the
       // (hi, lo) velocity is the apply operand.
       apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
@@ -1240,11 +1241,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       restart = tot[0] > 4.0 * sc[2];
       prev_est = -1.0;
       rho = tot[0];
+      // stagnation is judged at the periodic refreshes only (16 iterations
+      // apart), not at the convergence checks in between
       if (rho < best_true) {
         best_true = rho;
         stalls = 0;
-      } else if (++stalls >= 3) {
-        break;  // at the precision floor: no progress over three refreshes
+      } else if ((periodic || a.refresh <= 0) && ++stalls >= 3) {
+        break;  // at the precision floor: no progress over three periods
       }
     }
     converged = rho <= thresh;
@@ -1624,11 +1627,12 @@ struct FinBatchRefresh {
       b.restart = t[0] > 4.0 * b.est;
       b.prev_est = -1.0;
       b.rho = t[0];
+      const bool periodic = a.refresh <= 0 || b.iterations % a.refresh == 0;
       if (t[0] < b.best_true) {
         b.best_true = t[0];
         b.stalls = 0;
-      } else if (++b.stalls >= 3) {
-        b.active = 0;  // at the precision floor
+      } else if (periodic && ++b.stalls >= 3) {
+        b.active = 0;  // at the precision floor: no progress over three periods
       }
       if (t[0] <= b.thresh) {
         b.converged = 1;
