@@ -471,16 +471,28 @@ def run_ours(args, world, rank, local):
         return {"dev_s": dev_s, "its": its, "res": res, "applies": applies, "launches": int(n1.value - n0.value),
                 "x": x, "fext": fext}
 
-    # ---- plain CG (previous velocity) and learned warm start, same trajectory
+    # ---- plain CG (previous velocity), the extrapolation v + dv_prev alone
+    # (the network with its output zeroed) and the learned warm start, each
+    # on the same trajectory
+    from opentissue_gb300.warmstart import WarmStartNet, extrapolation_state
     h_plain = make_handle(lib, capi, tets, coord, fixed, stream)
     h_learn = make_handle(lib, capi, tets, coord, fixed, stream)
+    h_extra = make_handle(lib, capi, tets, coord, fixed, stream)
     net.attach(h_learn)
+    extrap = WarmStartNet(capacity=0, seed=0)
+    extrap.set_state(extrapolation_state(net.state()))
+    extrap.attach(h_extra)
+    capi.check(lib.otfem_set_warm_start_smoothing(h_extra, 0))
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
     r_plain = timed_run(h_plain, plain)
     r_learn = timed_run(h_learn, learned)
     clocks = sampler.stop()
+    r_extra = timed_run(h_extra, learned)
+    extrap.detach(h_extra)
+    capi.check(lib.otfem_destroy(h_extra))
+    extrap.close()
     disp = np.abs(r_plain["x"] - coord).max()
     pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))
 
@@ -585,6 +597,8 @@ def run_ours(args, world, rank, local):
                              "ms_per_step": 1e3 * r_plain["dev_s"] / args.steps,
                              "iterations_per_step": float(np.mean(r_plain["its"])),
                              "max_rel_residual": float(np.max(r_plain["res"]))},
+                   "extrapolation_only": {"value": total_tet_steps / r_extra["dev_s"], "unit": "tet-steps/s",
+                                          "iterations_per_step": float(np.mean(r_extra["its"]))},
                    "learned_over_plain": value / plain_value,
                    "position_difference_learned_vs_plain": pos_diff,
                    "training": train_info,

@@ -44,6 +44,8 @@ struct DeviceSync {
 struct BatchMesh {
   double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta, gamma_d, gamma_c;
   int active, restart, stalls, iterations, applies, status, converged, pad;
+  int best_buf;  // which kept iterate (v_keep) has the smallest true residual
+  int stalled;   // stopped at the precision floor: the kept iterate is the result
 };
 
 // Statistics written by the step kernels (device memory).
@@ -143,6 +145,9 @@ struct Context {
   // learned start, projected: operands d = dv_prev, c = the network's
   // correction and their products A d, A c (4N, allocated with a network)
   float4* warm_ops = nullptr;
+  // two kept copies of the CG iterate (hi, lo) from the true-residual
+  // refreshes: a solve stopped at the precision floor returns the best one
+  float4* v_keep = nullptr;       // 4N
   int warm_smoothing = 4;         // 1-ring mean passes over the network's correction
   float* features = nullptr;      // N x kFeatureStride, allocated when collecting
   int collect = 0;
@@ -160,7 +165,7 @@ struct Context {
   unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
-  double apply_ms[4] = {0, 0, 0, 0};  // measured time of one sweep per variant
+  double apply_ms[OTFEM_NUM_APPLY_VARIANTS] = {};  // measured time of one sweep per variant
   DeviceSync* sync = nullptr;
   double* trace = nullptr;                                 // kTraceRows x kTraceCols
   DeviceStats* stats = nullptr;
@@ -205,6 +210,7 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver);
 // fastest in c.apply_variant (synchronises the stream).
 cudaError_t autotune_apply(Context& c);
 constexpr int kNumApplyVariants = OTFEM_NUM_APPLY_VARIANTS;
+static_assert(sizeof(Context::apply_ms) == sizeof(double) * kNumApplyVariants, "one time per apply variant");
 // Learned warm start: per-node inputs (v, previous dv, f_ext, 1-ring mean
 // of the 9 entries of Re) stored with this stride (floats).
 constexpr int kFeatures = 18;

@@ -119,6 +119,7 @@ struct MixedArgs {
   const float4* warm_dv;                // learned guess v + warm_dv (null: plain start from v)
   float4* dv_last;                      // in: dv_prev; out: v_new - v_old per free node
   float4 *wd, *wc, *ad, *ac;            // learned start: operands d, c and products A d, A c
+  float4* v_keep;                       // kept iterates: copy k at v_keep[2kN + i] (hi), [(2k+1)N + i] (lo)
   // batched solve (see Context)
   int num_meshes;
   const int* mesh_of_node;
@@ -1143,12 +1144,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
     a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
     a.q_f[i] = zero4;
+    a.v_keep[i] = a.v_f[i];  // the start is the first kept iterate
+    a.v_keep[N + i] = a.v_lo[i];
     rr[0] = df_add(rr[0], DF{rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2], 0.f});
   }
   if (!grid_reduce<DF, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
   double rho = tot[0];
   const double rho0 = rho;
   int it = 0;
+  int best_buf = 0;      // kept iterate with the smallest true residual
+  bool stalled = false;  // stopped at the precision floor: return the kept iterate
   bool converged = rho <= thresh;
   // recurrence check and restarts (FinAlphaBetaExact); stagnation of the
   // true residual at the refreshes ends the solve unconverged
@@ -1224,6 +1229,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       ++applies;
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       DF tr[1] = {{0.f, 0.f}};
+      const long cand = 2L * (best_buf ^ 1) * N;  // the kept copy that is not the best
       for (long i = gtid; i < N; i += gstride) {
         if (a.fixed[i]) continue;
         float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
@@ -1233,6 +1239,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
         float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
         a.r_f[i] = make_float4(rx, ry, rz, 0.f);
         a.q_f[i] = zero4;
+        a.v_keep[cand + i] = vh;
+        a.v_keep[cand + N + i] = vl;
         tr[0] = df_add(tr[0], DF{rx * rx + ry * ry + rz * rz, 0.f});
       }
       if (!grid_reduce<DF, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
@@ -1245,19 +1253,24 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       // apart), not at the convergence checks in between
       if (rho < best_true) {
         best_true = rho;
+        best_buf ^= 1;
         stalls = 0;
       } else if ((periodic || a.refresh <= 0) && ++stalls >= 3) {
-        break;  // at the precision floor: no progress over three periods
+        stalled = true;  // at the precision floor: no progress over three periods
+        rho = best_true;
+        break;
       }
     }
     converged = rho <= thresh;
   }
 
-  // v back to FP64; position_update (fem_position_update.h:25-39); the
-  // velocity change is kept for the learned warm start
+  // v back to FP64 (the kept best iterate when stopped at the floor);
+  // position_update (fem_position_update.h:25-39); the velocity change is
+  // kept for the learned warm start
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) continue;
-    float4 vh = a.v_f[i], vl = a.v_lo[i];
+    const long kb = 2L * best_buf * N;
+    float4 vh = stalled ? a.v_keep[kb + i] : a.v_f[i], vl = stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
     double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
     float dv[3];
     for (int c = 0; c < 3; ++c) {
@@ -1562,6 +1575,8 @@ struct FinBatchStart {
     b.rho = b.rho0 = b.best_true = b.est = t[0];
     b.prev_est = -1.0;
     b.restart = b.stalls = b.iterations = 0;
+    b.best_buf = 0;
+    b.stalled = 0;
     b.applies = a.wd ? 3 : 1;
     b.status = isfinite(t[0]) && isfinite(b.bnorm2) ? 0 : OTFEM_ERR_NONFINITE;
     b.converged = b.status == 0 && t[0] <= b.thresh;
@@ -1630,9 +1645,12 @@ struct FinBatchRefresh {
       const bool periodic = a.refresh <= 0 || b.iterations % a.refresh == 0;
       if (t[0] < b.best_true) {
         b.best_true = t[0];
+        b.best_buf ^= 1;
         b.stalls = 0;
       } else if (periodic && ++b.stalls >= 3) {
         b.active = 0;  // at the precision floor: no progress over three periods
+        b.stalled = 1;
+        b.rho = b.best_true;
       }
       if (t[0] <= b.thresh) {
         b.converged = 1;
@@ -1796,6 +1814,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
           a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
           a.q_f[i] = zero4;
+          a.v_keep[i] = a.v_f[i];  // the start is the first kept iterate
+          a.v_keep[N + i] = a.v_lo[i];
           rr[0] = rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2];
         }
       }
@@ -1881,6 +1901,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             const float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
             a.r_f[i] = make_float4(rx, ry, rz, 0.f);
             a.q_f[i] = zero4;
+            const long cand = 2L * (a.bm[m].best_buf ^ 1) * N;  // the kept copy that is not the best
+            a.v_keep[cand + i] = vh;
+            a.v_keep[cand + N + i] = vl;
             tr[0] = rx * rx + ry * ry + rz * rz;
           }
         }
@@ -1892,10 +1915,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     }
   }
 
-  // v back to FP64; position update; velocity change (all meshes)
+  // v back to FP64 (a mesh stopped at the floor takes its kept best
+  // iterate); position update; velocity change (all meshes)
   for (long i = nr.beg + lane; i < nr.end; i += 32) {
     if (a.fixed[i]) continue;
-    const float4 vh = a.v_f[i], vl = a.v_lo[i];
+    const BatchMesh& bmi = a.bm[a.mesh_of_node[i]];
+    const long kb = 2L * bmi.best_buf * N;
+    const float4 vh = bmi.stalled ? a.v_keep[kb + i] : a.v_f[i], vl = bmi.stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
     const double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
     float dv[3];
     for (int c = 0; c < 3; ++c) {
@@ -2460,6 +2486,7 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   const bool learned = prm.warm_start == OTFEM_WARM_START_LEARNED && c.warm_ops;
   a.warm_dv = learned ? c.warm_dv : nullptr;
   a.dv_last = c.dv_last;
+  a.v_keep = c.v_keep;
   a.wd = learned ? c.warm_ops : nullptr;
   a.wc = learned ? c.warm_ops + c.N : nullptr;
   a.ad = learned ? c.warm_ops + 2L * c.N : nullptr;
