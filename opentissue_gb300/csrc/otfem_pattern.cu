@@ -26,33 +26,82 @@ __global__ void k_count_incidence(int T, const int4* __restrict__ tets, int* cnt
   atomicAdd(cnt + n.w, 1);
 }
 
-// Exclusive scan of n ints into out[0..n] (out[n] = total) with one block:
-// each thread scans a contiguous chunk, chunk totals are scanned in shared
-// memory.  Used only at set-up.
-__global__ void k_scan_one_block(long n, const int* __restrict__ in, int* out) {
+// Exclusive scan of n ints into out[0..n] (out[n] = total), in three
+// coalesced passes: each CTA scans a tile of 1024 (warp shuffles, then the
+// warp totals), one CTA scans the tile totals, and every element gets its
+// tile's offset.  Used only at set-up.
+constexpr int kScanTile = 1024;
+
+__global__ void k_scan_tiles(long n, const int* __restrict__ in, int* out, long* tile_sums) {
+  __shared__ long warp_tot[kScanTile / 32];
+  const long i = long(blockIdx.x) * kScanTile + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long v = i < n ? in[i] : 0;
+  long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    long w = lane < kScanTile / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kScanTile / 32) warp_tot[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  const long before = warp ? warp_tot[warp - 1] : 0;
+  if (i < n) out[i] = int(before + x - v);
+  if (threadIdx.x == kScanTile - 1) tile_sums[blockIdx.x] = before + x;
+}
+
+// In place: tile_sums[k] <- sum of tiles before k; out[n] = total.
+__global__ void k_scan_tile_sums(long tiles, long* tile_sums, int* out, long n) {
   __shared__ long part[1024];
-  long chunk = (n + blockDim.x - 1) / blockDim.x;
-  long lo = threadIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
+  const long chunk = (tiles + blockDim.x - 1) / blockDim.x;
+  const long lo = threadIdx.x * chunk, hi = lo + chunk < tiles ? lo + chunk : tiles;
   long s = 0;
-  for (long i = lo; i < hi; ++i) s += in[i];
+  for (long k = lo; k < hi; ++k) s += tile_sums[k];
   part[threadIdx.x] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     long acc = 0;
-    for (int k = 0; k < (int)blockDim.x; ++k) {
-      long v = part[k];
+    for (int k = 0; k < int(blockDim.x); ++k) {
+      const long v = part[k];
       part[k] = acc;
       acc += v;
     }
-    out[n] = (int)acc;
+    out[n] = int(acc);
   }
   __syncthreads();
   long acc = part[threadIdx.x];
-  for (long i = lo; i < hi; ++i) {
-    int v = in[i];
-    out[i] = (int)acc;
+  for (long k = lo; k < hi; ++k) {
+    const long v = tile_sums[k];
+    tile_sums[k] = acc;
     acc += v;
   }
+}
+
+__global__ void k_scan_add(long n, const long* __restrict__ tile_sums, int* out) {
+  const long i = long(blockIdx.x) * kScanTile + threadIdx.x;
+  if (i < n) out[i] += int(tile_sums[blockIdx.x]);
+}
+
+cudaError_t scan_exclusive(Context& c, long n, const int* in, int* out) {
+  const long tiles = (n + kScanTile - 1) / kScanTile;
+  long* sums = nullptr;
+  cudaError_t e = cudaMallocAsync(&sums, sizeof(long) * (tiles > 0 ? tiles : 1), c.stream);
+  if (e != cudaSuccess) return e;
+  if (tiles > 0) k_scan_tiles<<<unsigned(tiles), kScanTile, 0, c.stream>>>(n, in, out, sums);
+  k_scan_tile_sums<<<1, 1024, 0, c.stream>>>(tiles, sums, out, n);
+  if (tiles > 0) k_scan_add<<<unsigned(tiles), kScanTile, 0, c.stream>>>(n, sums, out);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return cudaFreeAsync(sums, c.stream);
 }
 
 __global__ void k_fill_incidence(int T, const int4* __restrict__ tets, const int* __restrict__ ptr,
@@ -169,7 +218,7 @@ cudaError_t build_incidence(Context& c) {
   OT_TRY(cudaMallocAsync(&c.inc_ptr, sizeof(int) * (c.N + 1), c.stream));
   OT_TRY(cudaMallocAsync(&c.inc_ent, sizeof(int) * (4L * c.T + 1), c.stream));
   k_count_incidence<<<blocks_for(c.T), kThreads, 0, c.stream>>>(c.T, c.tets, cnt);
-  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.N, cnt, c.inc_ptr);
+  OT_TRY(scan_exclusive(c, c.N, cnt, c.inc_ptr));
   OT_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (c.N + 1), c.stream));
   k_fill_incidence<<<blocks_for(c.T), kThreads, 0, c.stream>>>(c.T, c.tets, c.inc_ptr, cnt, c.inc_ent);
   k_sort_incidence<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.inc_ptr, c.inc_ent);
@@ -184,7 +233,7 @@ cudaError_t build_pattern(Context& c) {
   OT_TRY(cudaMallocAsync(&cnt, sizeof(int) * (c.N + 1), c.stream));
   OT_TRY(cudaMallocAsync(&c.row_ptr, sizeof(int) * (c.N + 1), c.stream));
   k_row_unique<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, scratch, cnt);
-  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.N, cnt, c.row_ptr);
+  OT_TRY(scan_exclusive(c, c.N, cnt, c.row_ptr));
   int nnz = 0;
   OT_TRY(cudaMemcpyAsync(&nnz, c.row_ptr + c.N, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
   OT_TRY(cudaStreamSynchronize(c.stream));
@@ -199,7 +248,7 @@ cudaError_t build_pattern(Context& c) {
   OT_TRY(cudaMallocAsync(&c.bc_ent, sizeof(int) * (16L * c.T + 1), c.stream));
   k_bc_count<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, c.row_ptr,
                                                          c.cols, bc_cnt);
-  k_scan_one_block<<<1, 1024, 0, c.stream>>>(c.nnz, bc_cnt, c.bc_ptr);
+  OT_TRY(scan_exclusive(c, c.nnz, bc_cnt, c.bc_ptr));
   OT_TRY(cudaMemsetAsync(bc_cnt, 0, sizeof(int) * (c.nnz + 1), c.stream));
   k_bc_fill<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, c.row_ptr,
                                                         c.cols, c.bc_ptr, bc_cnt, c.bc_ent);
