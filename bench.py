@@ -430,6 +430,10 @@ def run_ours(args, world, rank, local):
                                 max_iterations=5000, refresh_period=16)
     learned = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
                                   max_iterations=5000, refresh_period=16, warm_start=capi.WARM_START_LEARNED)
+    # plain CG without the preconditioner: the reference's method on the GPU
+    plain_cg = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                   max_iterations=5000, refresh_period=16,
+                                   preconditioner=capi.PRECONDITIONER_NONE)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def flush_l2():
@@ -492,6 +496,9 @@ def run_ours(args, world, rank, local):
     r_extra = timed_run(h_extra, learned)
     extrap.detach(h_extra)
     capi.check(lib.otfem_destroy(h_extra))
+    h_cg = make_handle(lib, capi, tets, coord, fixed, stream)
+    r_cg = timed_run(h_cg, plain_cg)
+    capi.check(lib.otfem_destroy(h_cg))
     extrap.close()
     disp = np.abs(r_plain["x"] - coord).max()
     pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))
@@ -590,6 +597,7 @@ def run_ours(args, world, rank, local):
         "config": {"workload": WORKLOAD["name"],
                    "warm_start": "learned (node MLP + 1-ring smoothing), trained in this run",
                    "solver": "matrix-free persistent CG (OTFEM_SOLVER_MIXED), CUDA graph per step",
+                   "preconditioner": "node Jacobi (OTFEM_PRECONDITIONER_JACOBI, the default)",
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
                    "iterations_per_step": float(np.mean(r_learn["its"])),
                    "max_rel_residual": float(np.max(r_learn["res"])),
@@ -597,6 +605,9 @@ def run_ours(args, world, rank, local):
                              "ms_per_step": 1e3 * r_plain["dev_s"] / args.steps,
                              "iterations_per_step": float(np.mean(r_plain["its"])),
                              "max_rel_residual": float(np.max(r_plain["res"]))},
+                   "plain_unpreconditioned": {"value": total_tet_steps / r_cg["dev_s"], "unit": "tet-steps/s",
+                                              "iterations_per_step": float(np.mean(r_cg["its"])),
+                                              "max_rel_residual": float(np.max(r_cg["res"]))},
                    "extrapolation_only": {"value": total_tet_steps / r_extra["dev_s"], "unit": "tet-steps/s",
                                           "iterations_per_step": float(np.mean(r_extra["its"]))},
                    "learned_over_plain": value / plain_value,

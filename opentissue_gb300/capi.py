@@ -22,10 +22,11 @@ ERR_OUT_OF_MEMORY = -7
 ERR_UNSUPPORTED = -8
 
 # node fields
-COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B = range(7)
+COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B, NODE_STIFFNESS = range(8)
 # solvers
 SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
 WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
+PRECONDITIONER_NONE, PRECONDITIONER_JACOBI = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2
 NUM_APPLY_VARIANTS = 4
 # learned warm start: network state = 9731 weights + 42 normalisation values
@@ -44,6 +45,7 @@ class SolverParams(ctypes.Structure):
         ("sequential_dots", ctypes.c_int),
         ("warm_start", ctypes.c_int),
         ("graph", ctypes.c_int),
+        ("preconditioner", ctypes.c_int),
     ]
 
 

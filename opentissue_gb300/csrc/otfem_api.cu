@@ -59,7 +59,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.warm_ops, c.v_keep, c.features, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.warm_ops, c.v_keep, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -82,11 +82,14 @@ double* node_field(Context& c, int field) {
     case OTFEM_MASS: return c.mass;
     case OTFEM_F0: return c.f0;
     case OTFEM_B: return c.last_solver == OTFEM_SOLVER_REFERENCE ? c.b : c.bvec;
+    case OTFEM_NODE_STIFFNESS: return c.node_k;
     default: return nullptr;
   }
 }
 
-int64_t field_count(Context& c, int field) { return field == OTFEM_MASS ? int64_t(c.N) : 3 * int64_t(c.N); }
+int64_t field_count(Context& c, int field) {
+  return field == OTFEM_MASS || field == OTFEM_NODE_STIFFNESS ? int64_t(c.N) : 3 * int64_t(c.N);
+}
 
 int check_params(const Context& c, const otfem_solver_params& p) {
   if (p.solver < OTFEM_SOLVER_REFERENCE || p.solver > OTFEM_SOLVER_FP64)
@@ -97,6 +100,8 @@ int check_params(const Context& c, const otfem_solver_params& p) {
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
   if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
+  if (p.preconditioner != OTFEM_PRECONDITIONER_NONE && p.preconditioner != OTFEM_PRECONDITIONER_JACOBI)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown preconditioner");
   if (c.num_meshes > 1 && p.solver != OTFEM_SOLVER_MIXED)
     return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes steps with OTFEM_SOLVER_MIXED (one CG per mesh)");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && p.solver != OTFEM_SOLVER_MIXED)
@@ -140,9 +145,9 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
 
 std::string step_key(const Context& c, double dt, bool warp, const otfem_solver_params& p) {
   char buf[320];
-  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d|%p|%d|%d", p.solver, dt, int(warp), p.mass_damping,
+  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d|%d|%p|%d|%d", p.solver, dt, int(warp), p.mass_damping,
            p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots, p.warm_start,
-           static_cast<void*>(c.mlp), c.collect, c.warm_smoothing);
+           p.preconditioner, static_cast<void*>(c.mlp), c.collect, c.warm_smoothing);
   return buf;
 }
 
@@ -170,6 +175,7 @@ void otfem_default_params(otfem_solver_params* p) {
   p->sequential_dots = 0;
   p->warm_start = OTFEM_WARM_START_PREVIOUS;
   p->graph = 1;
+  p->preconditioner = OTFEM_PRECONDITIONER_JACOBI;
 }
 
 const char* otfem_last_error(void) { return g_last_error.c_str(); }
@@ -254,6 +260,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.b_d, 9 * T);
   OT_ALLOC(c.c_d, 3 * T);
   OT_ALLOC(c.diag, N);
+  OT_ALLOC(c.node_k, N);
   OT_ALLOC(c.r, 3 * N);
   OT_ALLOC(c.p, 3 * N);
   OT_ALLOC(c.bvec, 3 * N);

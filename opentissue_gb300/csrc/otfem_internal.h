@@ -14,6 +14,8 @@ namespace otfem {
 
 // Per-CTA partial sums written before a grid barrier (one slot per scalar).
 constexpr int kMaxPartials = 16;
+// Doubles between consecutive grid-sum accumulators (one 128-byte line each).
+constexpr int kAccStride = 16;
 // Rows of the per-iteration CG trace kept per step.  Each row holds
 // kTraceCols doubles: rho, p.q, alpha, beta, then SM-clock stamps (cycles
 // since the kernel started, taken on CTA 0) after the apply sweep, after its
@@ -32,10 +34,10 @@ struct DeviceSync {
   unsigned int pad1[31];
   int status;                // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
   int pad2[31];
-  double result[2][4];       // grid-sum results, double-buffered by barrier parity
-  double pad3[8];
-  double acc[2][8];          // grid-sum accumulators (FP64 reductions), by barrier parity
-  double pad4[8];
+  double result[2][8];       // grid-sum results, double-buffered by barrier parity
+  double pad3[16];
+  double acc[3][8][kAccStride];  // grid-sum accumulators (FP64 reductions): three rotating
+                                 // sets of 8 values, each value on its own 128-byte line
   unsigned tile_ticket;      // staged apply: monotonic tile tickets
   unsigned pad5[31];
 };
@@ -112,6 +114,7 @@ struct Context {
   float *re_f = nullptr, *b_f = nullptr, *c_f = nullptr;  // 9T, 9T, 3T
   double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
   double* diag = nullptr;                                 // N: m(1+dt*alpha)
+  double* node_k = nullptr;  // N: tr(sum_e Ke_ii) / 3 over the node's tets (Jacobi preconditioner), from init
   double *r = nullptr, *p = nullptr, *bvec = nullptr;    // 3N
   float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N (p_f/v_f: high part, w = free flag)
   float4 *p_lo = nullptr, *v_lo = nullptr;                // N: low parts, x - double(float(x))
@@ -148,7 +151,7 @@ struct Context {
   // two kept copies of the CG iterate (hi, lo) from the true-residual
   // refreshes: a solve stopped at the precision floor returns the best one
   float4* v_keep = nullptr;       // 4N
-  int warm_smoothing = 4;         // 1-ring mean passes over the network's correction
+  int warm_smoothing = 2;         // 1-ring mean passes over the network's correction
   float* features = nullptr;      // N x kFeatureStride, allocated when collecting
   int collect = 0;
   bool features_valid = false;    // c.features hold the inputs of the last step

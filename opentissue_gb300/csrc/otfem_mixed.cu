@@ -82,6 +82,8 @@ struct MixedArgs {
   double* r;
   double* p;
   double* diag;
+  const double* node_k;  // tr(sum_e Ke_ii) / 3 per node (Jacobi preconditioner)
+  int precond;           // 1: CG preconditioned by the node scalars 1 / (diag + dt^2 node_k)
   // FP32 apply
   const float* re_f;
   const float* b_f;
@@ -271,10 +273,14 @@ __device__ __forceinline__ bool arrive(DeviceSync* s, unsigned round) {
   return ticket + 1u == round * gridDim.x;
 }
 
-// Thread 0 only: wait until round `round` is released; false on timeout.
+// Thread 0 only: wait until round `round` is released; false on timeout or
+// when another CTA has recorded an error (checked every 64 polls, off the
+// fast path).
 __device__ __forceinline__ bool wait_released(DeviceSync* s, unsigned round, long long spin_limit) {
   long long start = clock64();
+  unsigned polls = 0;
   while (int(ld_acquire(&s->gen) - round) < 0) {
+    if ((++polls & 63u) == 0u && ld_status(&s->status) != 0) return false;
     if (clock64() - start > spin_limit) {
       atomicCAS(&s->status, 0, OTFEM_ERR_TIMEOUT);
       return false;
@@ -283,17 +289,34 @@ __device__ __forceinline__ bool wait_released(DeviceSync* s, unsigned round, lon
   return true;
 }
 
+// Thread 0 only, the last CTA of round `round`: clears the accumulator set
+// of round - 1 (read by every CTA before it arrived here; used again by
+// round + 2) and releases the round.
+__device__ __forceinline__ void release_round(DeviceSync* s, unsigned round) {
+  double* acc = &s->acc[(round + 2u) % 3u][0][0];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k * kAccStride] = 0.0;
+  st_release(&s->gen, round);
+}
+
+// Thread 0 only: one grid synchronisation.  The status word is read before
+// arriving (its latency overlaps the arrival); a CTA that finds an error
+// leaves without arriving, and the others notice the error while they wait
+// or at their next synchronisation.
+__device__ __forceinline__ bool sync_round(DeviceSync* s, unsigned round, long long spin_limit) {
+  if (ld_status(&s->status) != 0) return false;
+  if (arrive(s, round)) {
+    release_round(s, round);
+    return true;
+  }
+  return wait_released(s, round, spin_limit);
+}
+
 __device__ bool grid_barrier(DeviceSync* s, long long spin_limit, unsigned& round) {
   __shared__ int ok;
   ++round;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int good = 1;
-    if (arrive(s, round)) st_release(&s->gen, round);
-    else good = wait_released(s, round, spin_limit) ? 1 : 0;
-    if (ld_status(&s->status) != 0) good = 0;
-    ok = good;
-  }
+  if (threadIdx.x == 0) ok = sync_round(s, round, spin_limit) ? 1 : 0;
   __syncthreads();
   return ok != 0;
 }
@@ -331,6 +354,7 @@ struct AccOps<double> {
   static __device__ __forceinline__ double add(double a, double b) { return a + b; }
   static __device__ __forceinline__ double shfl_down(double a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
   static __device__ __forceinline__ double to_double(double a) { return a; }
+  static __device__ __forceinline__ double shfl_xor(double a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
   static __device__ __forceinline__ double from_double(double a) { return a; }
   static __device__ __forceinline__ double zero() { return 0.0; }
 };
@@ -340,6 +364,9 @@ struct AccOps<DF> {
   static __device__ __forceinline__ DF shfl_down(DF a, int o) {
     return DF{__shfl_down_sync(0xffffffffu, a.hi, o), __shfl_down_sync(0xffffffffu, a.lo, o)};
   }
+  static __device__ __forceinline__ DF shfl_xor(DF a, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+  }
   static __device__ __forceinline__ double to_double(DF a) { return double(a.hi) + double(a.lo); }
   static __device__ __forceinline__ DF from_double(double a) {
     float h = float(a);
@@ -348,37 +375,76 @@ struct AccOps<DF> {
   static __device__ __forceinline__ DF zero() { return DF{0.f, 0.f}; }
 };
 
+// Warp sums of NV values per lane by a reduce-scatter butterfly: with the
+// values padded to P = 2^S, each of the first S exchange steps (lane
+// distance 16, 8, ...) sends half of the remaining values to the partner
+// lane and adds the other half, so lane groups of 32 / P end up with one
+// value each, which the remaining steps sum over the group.  That is P - 1 +
+// 5 - S additions per lane instead of 5 NV.  Returns the value index this
+// lane holds (its warp total) or -1 when the lane holds no total to publish.
+template <typename Acc, int NV>
+__device__ __forceinline__ int warp_totals(const Acc (&val)[NV], Acc& total) {
+  typedef AccOps<Acc> Ops;
+  static_assert(NV >= 1 && NV <= 8, "1..8 values");
+  constexpr int S = NV > 4 ? 3 : NV > 2 ? 2 : NV > 1 ? 1 : 0;
+  constexpr int P = 1 << S;
+  const int lane = threadIdx.x & 31;
+  Acc x[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) x[k] = k < NV ? val[k] : Ops::zero();
+#pragma unroll
+  for (int lvl = 0; lvl < S; ++lvl) {
+    const int o = 16 >> lvl;
+    const int h = P >> (lvl + 1);
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const Acc send = upper ? x[j] : x[j + h];
+      const Acc keep = upper ? x[j + h] : x[j];
+      x[j] = Ops::add(keep, Ops::shfl_xor(send, o));
+    }
+  }
+#pragma unroll
+  for (int o = 16 >> S; o > 0; o >>= 1) x[0] = Ops::add(x[0], Ops::shfl_xor(x[0], o));
+  total = x[0];
+  const int idx = lane >> (5 - S);
+  return (lane & ((32 >> S) - 1)) == 0 && idx < NV ? idx : -1;
+}
+
 // Sums NV per-thread values over the grid: warp shuffles, then the warp
-// totals (NV warps in parallel, one value each), then the CTA totals.  With
-// a.ordered_sums the CTA totals go to per-CTA partials that the last CTA to
-// arrive adds up in CTA order (a fixed order); otherwise each CTA adds its
-// totals into FP64 accumulators with atomic reductions and the last CTA only
-// reads them (a shorter critical path; sums in arrival order).  The last CTA turns the NV totals into NO outputs with
-// fin(totals, outputs), and every thread of every CTA receives the outputs.
-// Includes a grid barrier.  Partials, accumulators and results alternate
-// between two halves by round parity: those of round r are consumed (and the
-// accumulators cleared) by the last CTA of r before it releases r, so the
-// writes of round r + 2 cannot overtake them.
+// totals (NV warps in parallel, one value each), then the CTA totals, and
+// gives every thread of every CTA the NO outputs of fin(totals, outputs).
+// Includes a grid synchronisation.
+//  * Default: each CTA adds its totals into FP64 accumulators with atomic
+//    reductions (sums in arrival order; each value on its own 128-byte line),
+//    and after the release every CTA reads the totals and runs fin itself,
+//    so nothing but the release sits between the last arrival and the next
+//    phase.  Accumulator sets rotate over three rounds: the set of round r
+//    is read by every CTA before it arrives at round r + 1, whose last CTA
+//    clears it for round r + 3 (release_round).
+//  * a.ordered_sums: the CTA totals go to per-CTA partials that the last CTA
+//    to arrive adds up in CTA order (a fixed order), runs fin and publishes
+//    the outputs; partials and outputs alternate between two halves by round
+//    parity, so the writes of round r + 2 cannot overtake the reads of r.
 template <typename Acc, int NV, int NO, typename Fin>
 __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&out)[NO], unsigned& round,
                             Fin fin) {
-  static_assert(2 * NV <= kMaxPartials && NO <= 4 && NV <= 8, "partials too small");
+  static_assert(2 * NV <= kMaxPartials && NO <= 8 && NV <= 8, "partials too small");
   typedef AccOps<Acc> Ops;
   constexpr int kWarps = kBlock / 32;
   __shared__ Acc s_warp[kWarps][NV];
   __shared__ double s_tot[8];
-  __shared__ double s_res[4];
+  __shared__ double s_res[8];
   __shared__ int s_flag;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   ++round;
   const int half = int(round & 1u);
   double* part = a.partials + half * (kMaxPartials / 2) * gridDim.x;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    Acc x = val[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-    if (lane == 0) s_warp[warp][k] = x;
+  double* acc = &a.sync->acc[round % 3u][0][0];
+  {
+    Acc x;
+    const int k = warp_totals<Acc, NV>(val, x);
+    if (k >= 0) s_warp[warp][k] = x;
   }
   __syncthreads();
   if (warp < NV) {
@@ -388,34 +454,55 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
     for (int o = kWarps / 2; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
     if (lane == 0) {
       if (a.ordered_sums) part[warp * gridDim.x + blockIdx.x] = Ops::to_double(x);
-      else atomicAdd(&a.sync->acc[half][warp], Ops::to_double(x));
+      else atomicAdd(acc + warp * kAccStride, Ops::to_double(x));
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
-  __syncthreads();
-  if (s_flag) {
-    if (a.ordered_sums) {
-      // one partial per thread (gridDim.x <= blockDim.x), then a fixed-order tree
+  if (!a.ordered_sums) {
+    if (threadIdx.x == 0) s_flag = sync_round(a.sync, round, a.spin_limit) ? 1 : 0;
+    __syncthreads();
+    const bool good = s_flag != 0;
+    if (good && threadIdx.x < NV) s_tot[threadIdx.x] = __ldcg(acc + threadIdx.x * kAccStride);
+    __syncthreads();
+    if (good && threadIdx.x == 0) {
+      double tot[NV], res[NO];
 #pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        Acc x = threadIdx.x < gridDim.x ? Ops::from_double(__ldcg(part + k * gridDim.x + threadIdx.x)) : Ops::zero();
+      for (int k = 0; k < NV; ++k) tot[k] = s_tot[k];
+      fin(tot, res);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-        if (lane == 0) s_warp[warp][k] = x;
-      }
-      __syncthreads();
-      if (warp < NV) {
-        Acc x = lane < kWarps ? s_warp[lane][warp] : Ops::zero();
-#pragma unroll
-        for (int o = kWarps / 2; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
-        if (lane == 0) s_tot[warp] = Ops::to_double(x);
-      }
-      __syncthreads();
-    } else if (threadIdx.x < NV) {
-      s_tot[threadIdx.x] = __ldcg(&a.sync->acc[half][threadIdx.x]);
-      a.sync->acc[half][threadIdx.x] = 0.0;  // for round r + 2
+      for (int k = 0; k < NO; ++k) s_res[k] = res[k];
     }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NO; ++k) out[k] = s_res[k];
+    __syncthreads();
+    return good;
+  }
+  if (threadIdx.x == 0) {
+    // 2: last CTA, 1: wait for the release, 0: an error is recorded
+    if (ld_status(&a.sync->status) != 0) s_flag = 0;
+    else s_flag = arrive(a.sync, round) ? 2 : 1;
+  }
+  __syncthreads();
+  if (s_flag == 2) {
+    // one partial per thread (gridDim.x <= blockDim.x), then a fixed-order tree
+    Acc pv[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      pv[k] = threadIdx.x < gridDim.x ? Ops::from_double(__ldcg(part + k * gridDim.x + threadIdx.x)) : Ops::zero();
+    {
+      Acc x;
+      const int k = warp_totals<Acc, NV>(pv, x);
+      if (k >= 0) s_warp[warp][k] = x;
+    }
+    __syncthreads();
+    if (warp < NV) {
+      Acc x = lane < kWarps ? s_warp[lane][warp] : Ops::zero();
+#pragma unroll
+      for (int o = kWarps / 2; o > 0; o >>= 1) x = Ops::add(x, Ops::shfl_down(x, o));
+      if (lane == 0) s_tot[warp] = Ops::to_double(x);
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
       double tot[NV], res[NO];
 #pragma unroll
@@ -425,12 +512,10 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
         s_res[k] = res[k];
         a.sync->result[half][k] = res[k];
       }
-      st_release(&a.sync->gen, round);
-      if (ld_status(&a.sync->status) != 0) s_flag = 0;
+      release_round(a.sync, round);
     }
-  } else if (threadIdx.x == 0) {
-    int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
-    if (ld_status(&a.sync->status) != 0) ok = 0;
+  } else if (threadIdx.x == 0 && s_flag == 1) {
+    const int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
     if (ok)
       for (int k = 0; k < NO; ++k) s_res[k] = __ldcg(&a.sync->result[half][k]);
     s_flag = ok;
@@ -446,51 +531,72 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
 struct FinIdentity1 {
   __device__ void operator()(const double* t, double* o) const { o[0] = t[0]; }
 };
-
-// The CG scalars from (p.q, r.q, q.q) and rho = r.r of the current r:
-// alpha = rho / p.q, ||r - alpha q||^2 = rho - 2 alpha r.q + alpha^2 q.q
-// (so beta is known before the vector update, which then updates v, r and p
-// in one pass), beta = that / rho.  outputs: alpha, beta, rho_est, flag
-// (0 ok, 1 non-finite system, 2 finite breakdown).  With four totals the
-// fourth is the exact r.r (and `rho` is ignored); the estimate of the new
-// r.r then only sets beta, whose error is relative to rho.
-struct FinAlphaBeta {
-  double rho;
+struct FinIdentity2 {
   __device__ void operator()(const double* t, double* o) const {
-    const double pq = t[0];
-    // two independent reciprocals instead of two dependent divisions
-    const double inv_pq = 1.0 / pq, inv_rho = 1.0 / rho;
-    double alpha = rho * inv_pq;
-    double est = rho - 2.0 * alpha * t[1] + alpha * alpha * t[2];
-    if (est < 0.0) est = 0.0;
-    double beta = est * inv_rho;
-    double flag = 0.0;
-    if (!isfinite(pq) || !isfinite(rho) || !isfinite(t[1]) || !isfinite(t[2])) flag = 1.0;
-    else if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) flag = 2.0;
-    o[0] = alpha;
-    o[1] = beta;
-    o[2] = est;
-    o[3] = flag;
+    o[0] = t[0];
+    o[1] = t[1];
   }
 };
 
-// The same with the exact r.r as the fourth total.  The previous
-// iteration's estimate of this r.r (prev_est < 0: none) checks the
-// recurrence: when they disagree by more than a quarter, or on `restart`,
-// beta = 0 restarts the search direction from the residual (steepest
-// descent, which cannot grow the error), instead of letting an inaccurate
-// recurrence near the precision floor amplify itself.
-struct FinAlphaBetaExact {
+// Preconditioned CG (z = S r, S the node scalars; S = I without the
+// preconditioner) with both CG scalars from one grid sum.  Totals: p.q,
+// z.q, q.Sq, the exact r.z, r.q, q.q and the exact r.r of the current r.
+// alpha = r.z / p.q; the new r' = r - alpha q has
+//   r'.z' = r.z - 2 alpha z.q + alpha^2 q.Sq   (sets beta = r'.z' / r.z)
+//   r'.r' = r.r - 2 alpha r.q + alpha^2 q.q    (the convergence estimate)
+// so the vector update can form p' = z' + beta p in the same pass.  Outputs:
+// alpha, beta, the r'.r' estimate, flag (0 ok, 1 non-finite system, 2 finite
+// breakdown), the r'.z' estimate.  The previous iteration's r'.z' estimate
+// (prev_est < 0: none) checks the recurrence against the exact r.z: when they
+// disagree by more than a quarter, or on `restart`, beta = 0 restarts the
+// search direction from z (preconditioned steepest descent, which cannot grow
+// the error) instead of letting an inaccurate recurrence near the precision
+// floor amplify itself.
+__device__ __forceinline__ void pcg_scalars(const double* t, double prev_est, bool restart, double* o) {
+  const double pq = t[0], zq = t[1], qsq = t[2], rz = t[3], rq = t[4], qq = t[5], rr = t[6];
+  // independent reciprocals instead of dependent divisions
+  const double inv_pq = 1.0 / pq, inv_rz = 1.0 / rz;
+  const double alpha = rz * inv_pq;
+  double est_z = rz - 2.0 * alpha * zq + alpha * alpha * qsq;
+  double est_r = rr - 2.0 * alpha * rq + alpha * alpha * qq;
+  if (est_z < 0.0) est_z = 0.0;
+  if (est_r < 0.0) est_r = 0.0;
+  double beta = est_z * inv_rz;
+  double flag = 0.0;
+  bool finite = true;
+  for (int k = 0; k < 7; ++k) finite = finite && isfinite(t[k]);
+  if (!finite) flag = 1.0;
+  else if (!(pq > 0.0) || !isfinite(alpha) || !isfinite(beta)) flag = 2.0;
+  if (restart || (prev_est >= 0.0 && fabs(prev_est - rz) > 0.25 * rz)) beta = 0.0;
+  o[0] = alpha;
+  o[1] = beta;
+  o[2] = est_r;
+  o[3] = flag;
+  o[4] = est_z;
+}
+struct FinPcg {
   double prev_est;
   bool restart;
+  __device__ void operator()(const double* t, double* o) const { pcg_scalars(t, prev_est, restart, o); }
+};
+
+// The same for the FP64 solver, whose exact r.z (t_rz) and r.r come from the
+// grid sum after the vector update: totals p.q, z.q, q.Sq, r.q, q.q; outputs
+// alpha, beta, the r'.r' estimate, flag.
+struct FinPcgFp64 {
+  double rz, rr;
   __device__ void operator()(const double* t, double* o) const {
-    FinAlphaBeta f;
-    f.rho = t[3];
-    f(t, o);
-    if (o[3] == 0.0 && !isfinite(t[3])) o[3] = 1.0;
-    if (restart || (prev_est >= 0.0 && fabs(prev_est - t[3]) > 0.25 * t[3])) o[1] = 0.0;
+    const double u[7] = {t[0], t[1], t[2], rz, t[3], t[4], rr};
+    double w[5];
+    pcg_scalars(u, -1.0, false, w);
+    for (int k = 0; k < 4; ++k) o[k] = w[k];
   }
 };
+
+// Jacobi scalar of a free node whose mass term is dg (1 without the preconditioner).
+__device__ __forceinline__ double jacobi_scale(const MixedArgs& a, long i, double dg) {
+  return a.precond ? 1.0 / (dg + a.dt * a.dt * a.node_k[i]) : 1.0;
+}
 
 // The learned start, projected: CG starts from the point of least energy
 // x.A.x/2 - b.x on v + span{d, c} (d = dv_prev, c = the network's
@@ -1044,6 +1150,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     bool fx = a.fixed[i] != 0;
     double m = a.mass[i];
     double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+    float sp = 0.f;
     if (!fx) {
       double b3[3];
       for (int c = 0; c < 3; ++c)
@@ -1051,10 +1158,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
       float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
       bbsum[0] = df_add(bbsum[0], DF{bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2], 0.f});
-      a.diag[i] = m + a.dt * (a.alpha * m);
+      const double dg = m + a.dt * (a.alpha * m);
+      a.diag[i] = dg;
+      sp = float(jacobi_scale(a, i, dg));
     } else {
       a.diag[i] = 0.0;
     }
+    // r.w carries the node's preconditioner scalar through the solve
+    a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
     // never accumulated (w = 0).
@@ -1107,7 +1218,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       s5[2] = df_add(s5[2], DF{c.x * acx + c.y * acy + c.z * acz, 0.f});
       s5[3] = df_add(s5[3], DF{d.x * rf[0] + d.y * rf[1] + d.z * rf[2], 0.f});
       s5[4] = df_add(s5[4], DF{c.x * rf[0] + c.y * rf[1] + c.z * rf[2], 0.f});
-      a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+      a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
       a.ad[i] = make_float4(adx, ady, adz, 0.f);
       a.ac[i] = make_float4(acx, acy, acz, 0.f);
     }
@@ -1121,6 +1232,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       a.r_f[i] = zero4;
       continue;
     }
+    const float sp = a.r_f[i].w;
     float rf[3];
     if (a.wd) {
       // v += gamma_d d + gamma_c c; r -= gamma_d A d + gamma_c A c
@@ -1141,8 +1253,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
       rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
     }
-    a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
-    a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
+    a.r_f[i] = make_float4(rf[0], rf[1], rf[2], sp);
+    a.p_f[i] = make_float4(sp * rf[0], sp * rf[1], sp * rf[2], 1.f);  // p = z = S r
     a.q_f[i] = zero4;
     a.v_keep[i] = a.v_f[i];  // the start is the first kept iterate
     a.v_keep[N + i] = a.v_lo[i];
@@ -1155,7 +1267,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   int best_buf = 0;      // kept iterate with the smallest true residual
   bool stalled = false;  // stopped at the precision floor: return the kept iterate
   bool converged = rho <= thresh;
-  // recurrence check and restarts (FinAlphaBetaExact); stagnation of the
+  // recurrence check and restarts (FinPcg); stagnation of the
   // true residual at the refreshes ends the solve unconverged
   double prev_est = -1.0, best_true = rho0;
   bool restart = false;
@@ -1168,22 +1280,27 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
-    // q = diag p + q; p.q, r.q, q.q and the exact r.r of the current r
-    DF s4[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    // q = diag p + q; the totals of FinPcg (r.w = the node's scalar s)
+    DF s7[7] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float d = float(a.diag[i]);
       float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
-      s4[0] = df_add(s4[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
-      s4[1] = df_add(s4[1], DF{r4.x * qx + r4.y * qy + r4.z * qz, 0.f});
-      s4[2] = df_add(s4[2], DF{qx * qx + qy * qy + qz * qz, 0.f});
-      s4[3] = df_add(s4[3], DF{r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, 0.f});
+      const float rq = r4.x * qx + r4.y * qy + r4.z * qz, qq = qx * qx + qy * qy + qz * qz;
+      const float rr2 = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, sp = r4.w;
+      s7[0] = df_add(s7[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
+      s7[1] = df_add(s7[1], DF{sp * rq, 0.f});
+      s7[2] = df_add(s7[2], DF{sp * qq, 0.f});
+      s7[3] = df_add(s7[3], DF{sp * rr2, 0.f});
+      s7[4] = df_add(s7[4], DF{rq, 0.f});
+      s7[5] = df_add(s7[5], DF{qq, 0.f});
+      s7[6] = df_add(s7[6], DF{rr2, 0.f});
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
-    double sc[4];
-    if (!grid_reduce<DF, 4, 4>(a, s4, sc, round, FinAlphaBetaExact{prev_est, restart})) return;
-    prev_est = sc[2];
+    double sc[5];
+    if (!grid_reduce<DF, 7, 5>(a, s7, sc, round, FinPcg{prev_est, restart})) return;
+    prev_est = sc[4];
     restart = false;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
     if (sc[3] != 0.0) {
@@ -1207,10 +1324,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       df_inc(vh.y, vl.y, alpha * p4.y);
       df_inc(vh.z, vl.z, alpha * p4.z);
       float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
+      const float sp = r4.w;
       a.v_f[i] = vh;
       a.v_lo[i] = vl;
-      a.r_f[i] = make_float4(rx, ry, rz, 0.f);
-      a.p_f[i] = make_float4(rx + beta * p4.x, ry + beta * p4.y, rz + beta * p4.z, 1.f);
+      a.r_f[i] = make_float4(rx, ry, rz, sp);
+      a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
       a.q_f[i] = zero4;
     }
     if (tracer) stamp[4] = double(cycles_now() - t_start);
@@ -1237,7 +1355,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
         float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
         float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
         float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
-        a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+        a.r_f[i] = make_float4(rx, ry, rz, a.r_f[i].w);
         a.q_f[i] = zero4;
         a.v_keep[cand + i] = vh;
         a.v_keep[cand + N + i] = vl;
@@ -1332,7 +1450,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
 
   apply_sweep<double>(a, vv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-  double rr[1] = {0.0};
+  double rr[2] = {0.0, 0.0};
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) {
       pv[i] = zero4;
@@ -1342,15 +1460,19 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     V4 q4 = load_acc(qv + i);
     double qa[3] = {q4.x, q4.y, q4.z};
     double d = a.diag[i];
+    const double sp = jacobi_scale(a, i, d);
     double ri[3];
     for (int c = 0; c < 3; ++c) ri[c] = a.bvec[3 * i + c] - (d * a.v[3 * i + c] + qa[c]);
-    for (int c = 0; c < 3; ++c) a.r[3 * i + c] = ri[c], a.p[3 * i + c] = ri[c];
-    pv[i] = make_double4(ri[0], ri[1], ri[2], 1.0);
+    for (int c = 0; c < 3; ++c) a.r[3 * i + c] = ri[c], a.p[3 * i + c] = sp * ri[c];  // p = z = S r
+    pv[i] = make_double4(sp * ri[0], sp * ri[1], sp * ri[2], 1.0);
     qv[i] = zero4;
-    rr[0] += ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
+    const double r2 = ri[0] * ri[0] + ri[1] * ri[1] + ri[2] * ri[2];
+    rr[0] += r2;
+    rr[1] += sp * r2;
   }
-  if (!grid_reduce<double, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
-  double rho = tot[0];
+  double tot2[2];
+  if (!grid_reduce<double, 2, 2>(a, rr, tot2, round, FinIdentity2())) return;
+  double rho = tot2[0], rz = tot2[1];
   const double rho0 = rho;
   int it = 0, applies = 1;
   bool converged = rho <= thresh;
@@ -1361,23 +1483,28 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
-    double s3[3] = {0.0, 0.0, 0.0};
+    double s5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
       double qi[3] = {d * a.p[3 * i] + q4.x, d * a.p[3 * i + 1] + q4.y, d * a.p[3 * i + 2] + q4.z};
+      double pq = 0.0, rq = 0.0, qq = 0.0;
       for (int c = 0; c < 3; ++c) {
-        s3[0] += a.p[3 * i + c] * qi[c];
-        s3[1] += a.r[3 * i + c] * qi[c];
-        s3[2] += qi[c] * qi[c];
+        pq += a.p[3 * i + c] * qi[c];
+        rq += a.r[3 * i + c] * qi[c];
+        qq += qi[c] * qi[c];
       }
+      const double sp = jacobi_scale(a, i, d);
+      s5[0] += pq;
+      s5[1] += sp * rq;
+      s5[2] += sp * qq;
+      s5[3] += rq;
+      s5[4] += qq;
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
     double sc[4];
-    FinAlphaBeta fin;
-    fin.rho = rho;
-    if (!grid_reduce<double, 3, 4>(a, s3, sc, round, fin)) return;
+    if (!grid_reduce<double, 5, 4>(a, s5, sc, round, FinPcgFp64{rz, rho})) return;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
     if (sc[3] != 0.0) {
       if (sc[3] == 1.0 && blockIdx.x == 0 && threadIdx.x == 0)
@@ -1387,11 +1514,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     const double alpha = sc[0], beta = sc[1];
     const int row = it;
     ++it;
-    double rn[1] = {0.0};
+    double rn[2] = {0.0, 0.0};
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
+      const double sp = jacobi_scale(a, i, d);
       double pn[3], vn[3];
       const double qq[3] = {q4.x, q4.y, q4.z};
       for (int c = 0; c < 3; ++c) {
@@ -1402,7 +1530,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
         a.v[3 * i + c] = vn[c];
         a.r[3 * i + c] = ri;
         rn[0] += ri * ri;
-        pn[c] = ri + beta * pi;
+        rn[1] += sp * ri * ri;
+        pn[c] = sp * ri + beta * pi;
         a.p[3 * i + c] = pn[c];
       }
       pv[i] = make_double4(pn[0], pn[1], pn[2], 1.0);
@@ -1410,28 +1539,32 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
       qv[i] = zero4;
     }
     if (tracer) stamp[4] = double(cycles_now() - t_start);
-    if (!grid_reduce<double, 1, 1>(a, rn, tot, round, FinIdentity1())) return;
+    if (!grid_reduce<double, 2, 2>(a, rn, tot2, round, FinIdentity2())) return;
     if (tracer) trace_row(a, row, rho, 0.0, alpha, beta, stamp, t_start);
-    rho = tot[0];
+    rho = tot2[0];
+    rz = tot2[1];
     if ((a.refresh > 0 && it % a.refresh == 0) || rho <= thresh) {
       apply_sweep<double>(a, vv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
       ++applies;
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-      double tr[1] = {0.0};
+      double tr[2] = {0.0, 0.0};
       for (long i = gtid; i < N; i += gstride) {
         if (a.fixed[i]) continue;
         V4 q4 = load_acc(qv + i);
         double d = a.diag[i];
+        const double sp = jacobi_scale(a, i, d);
         const double qa[3] = {q4.x, q4.y, q4.z};
         for (int c = 0; c < 3; ++c) {
           double ri = a.bvec[3 * i + c] - (d * a.v[3 * i + c] + qa[c]);
           a.r[3 * i + c] = ri;
           tr[0] += ri * ri;
+          tr[1] += sp * ri * ri;
         }
         qv[i] = zero4;
       }
-      if (!grid_reduce<double, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
-      rho = tot[0];
+      if (!grid_reduce<double, 2, 2>(a, tr, tot2, round, FinIdentity2())) return;
+      rho = tot2[0];
+      rz = tot2[1];
     }
     converged = rho <= thresh;
   }
@@ -1479,14 +1612,11 @@ struct SegSum {
     for (int k = 0; k < NV; ++k) acc[k] = DF{0.f, 0.f};
   }
   __device__ __forceinline__ void flush(double* acc_half) {
+    DF x;
+    const int k = warp_totals<DF, NV>(acc, x);
+    if (k >= 0 && cur >= 0) atomicAdd(&acc_half[kBatchSlots * cur + k], AccOps<DF>::to_double(x));
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      DF x = acc[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x = AccOps<DF>::add(x, AccOps<DF>::shfl_down(x, o));
-      if ((threadIdx.x & 31) == 0 && cur >= 0) atomicAdd(&acc_half[kBatchSlots * cur + k], AccOps<DF>::to_double(x));
-      acc[k] = DF{0.f, 0.f};
-    }
+    for (int j = 0; j < NV; ++j) acc[j] = DF{0.f, 0.f};
   }
   // adds each valid lane's values to the sums of its mesh m (m >= cur)
   __device__ __forceinline__ void add(bool valid, int m, const float (&v)[NV], double* acc_half) {
@@ -1517,10 +1647,14 @@ __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (
   ++round;
   const int half = int(round & 1u);
   __syncthreads();
-  if (threadIdx.x == 0) s_flag = arrive(a.sync, round) ? 1 : 0;
+  if (threadIdx.x == 0) {
+    // 2: last CTA, 1: wait for the release, 0: an error is recorded
+    if (ld_status(&a.sync->status) != 0) s_flag = 0;
+    else s_flag = arrive(a.sync, round) ? 2 : 1;
+  }
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0;
   __syncthreads();
-  if (s_flag) {
+  if (s_flag == 2) {
     double* acc = a.bacc + size_t(half) * a.num_meshes * kBatchSlots;
     for (int m = threadIdx.x; m < a.num_meshes; m += blockDim.x) {
       double t[kBatchSlots];
@@ -1534,12 +1668,10 @@ __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (
     __syncthreads();
     if (threadIdx.x == 0) {
       for (int k = 0; k < 4; ++k) a.sync->result[half][k] = double(s_cnt[k]);
-      st_release(&a.sync->gen, round);
-      if (ld_status(&a.sync->status) != 0) s_flag = 0;
+      release_round(a.sync, round);
     }
-  } else if (threadIdx.x == 0) {
-    int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
-    if (ld_status(&a.sync->status) != 0) ok = 0;
+  } else if (threadIdx.x == 0 && s_flag == 1) {
+    const int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
     if (ok)
       for (int k = 0; k < 4; ++k) s_cnt[k] = int(__ldcg(&a.sync->result[half][k]));
     s_flag = ok;
@@ -1589,7 +1721,7 @@ struct FinBatchStart {
   }
 };
 
-// totals: p.q, r.q, q.q and the exact r.r of the meshes in the sweep
+// totals: those of FinPcg for the meshes in the sweep
 struct FinBatchIter {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
     BatchMesh& b = a.bm[m];
@@ -1598,11 +1730,8 @@ struct FinBatchIter {
     mk[kMaskUpdate * M + m] = 0;
     mk[kMaskRefresh * M + m] = 0;
     if (!mk[kMaskApply * M + m]) return;
-    double o[4];
-    FinAlphaBetaExact fin;
-    fin.prev_est = b.prev_est;
-    fin.restart = b.restart != 0;
-    fin(t, o);
+    double o[5];
+    pcg_scalars(t, b.prev_est, b.restart != 0, o);
     if (o[3] != 0.0) {
       // 1: NaN/Inf in this mesh's system (an error); 2: finite breakdown
       if (o[3] == 1.0) b.status = OTFEM_ERR_NONFINITE;
@@ -1612,7 +1741,8 @@ struct FinBatchIter {
     }
     b.alpha = o[0];
     b.beta = o[1];
-    b.est = b.rho = b.prev_est = o[2];
+    b.est = b.rho = o[2];
+    b.prev_est = o[4];
     b.restart = 0;
     ++b.iterations;
     ++b.applies;
@@ -1701,6 +1831,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
         const bool fx = a.fixed[i] != 0;
         const double mass = a.mass[i];
         double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+        float sp = 0.f;
         if (!fx) {
           double b3[3];
           for (int c = 0; c < 3; ++c)
@@ -1708,10 +1839,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
           const float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
           bb[0] = bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2];
-          a.diag[i] = mass + a.dt * (a.alpha * mass);
+          const double dg = mass + a.dt * (a.alpha * mass);
+          a.diag[i] = dg;
+          sp = float(jacobi_scale(a, i, dg));
         } else {
           a.diag[i] = 0.0;
         }
+        a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
         store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
         a.q_f[i] = zero4;
         if (a.wd) {
@@ -1767,7 +1901,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           s5[2] = c.x * acx + c.y * acy + c.z * acz;
           s5[3] = d.x * rf[0] + d.y * rf[1] + d.z * rf[2];
           s5[4] = c.x * rf[0] + c.y * rf[1] + c.z * rf[2];
-          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
+          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
           a.ad[i] = make_float4(adx, ady, adz, 0.f);
           a.ac[i] = make_float4(acx, acy, acz, 0.f);
         }
@@ -1791,6 +1925,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           a.p_f[i] = zero4;
           a.r_f[i] = zero4;
         } else {
+          const float sp = a.r_f[i].w;
           float rf[3];
           if (a.wd) {
             const float gd = float(a.bm[m].gamma_d), gc = float(a.bm[m].gamma_c);
@@ -1811,8 +1946,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
             rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
           }
-          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], 0.f);
-          a.p_f[i] = make_float4(rf[0], rf[1], rf[2], 1.f);
+          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], sp);
+          a.p_f[i] = make_float4(sp * rf[0], sp * rf[1], sp * rf[2], 1.f);  // p = z = S r
           a.q_f[i] = zero4;
           a.v_keep[i] = a.v_f[i];  // the start is the first kept iterate
           a.v_keep[N + i] = a.v_lo[i];
@@ -1831,28 +1966,31 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_apply);
     ++sweeps;
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    // q = diag p + q; p.q, r.q, q.q, r.r per mesh
+    // q = diag p + q; the totals of FinPcg per mesh
     {
-      SegSum<4> ss;
+      SegSum<7> ss;
       ss.start(first_mesh);
       for (long base = nr.beg; base < nr.end; base += 32) {
         const long i = base + lane;
         const bool valid = i < nr.end;
         int m = -1;
-        float s4[4] = {0.f, 0.f, 0.f, 0.f};
+        float s7[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (valid) {
           m = a.mesh_of_node[i];
           if (mask_apply[m] && !a.fixed[i]) {
             const float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
             const float d = float(a.diag[i]);
             const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
-            s4[0] = p4.x * qx + p4.y * qy + p4.z * qz;
-            s4[1] = r4.x * qx + r4.y * qy + r4.z * qz;
-            s4[2] = qx * qx + qy * qy + qz * qz;
-            s4[3] = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z;
+            s7[0] = p4.x * qx + p4.y * qy + p4.z * qz;
+            s7[4] = r4.x * qx + r4.y * qy + r4.z * qz;
+            s7[5] = qx * qx + qy * qy + qz * qz;
+            s7[6] = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z;
+            s7[1] = r4.w * s7[4];
+            s7[2] = r4.w * s7[5];
+            s7[3] = r4.w * s7[6];
           }
         }
-        ss.add(valid, m, s4, acc_half(round + 1));
+        ss.add(valid, m, s7, acc_half(round + 1));
       }
       ss.flush(acc_half(round + 1));
     }
@@ -1872,10 +2010,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       df_inc(vh.y, vl.y, alpha * p4.y);
       df_inc(vh.z, vl.z, alpha * p4.z);
       const float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
+      const float sp = r4.w;
       a.v_f[i] = vh;
       a.v_lo[i] = vl;
-      a.r_f[i] = make_float4(rx, ry, rz, 0.f);
-      a.p_f[i] = make_float4(rx + beta * p4.x, ry + beta * p4.y, rz + beta * p4.z, 1.f);
+      a.r_f[i] = make_float4(rx, ry, rz, sp);
+      a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
       a.q_f[i] = zero4;
     }
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
@@ -1899,7 +2038,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             const float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
             const float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
             const float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
-            a.r_f[i] = make_float4(rx, ry, rz, 0.f);
+            a.r_f[i] = make_float4(rx, ry, rz, a.r_f[i].w);
             a.q_f[i] = zero4;
             const long cand = 2L * (a.bm[m].best_buf ^ 1) * N;  // the kept copy that is not the best
             a.v_keep[cand + i] = vh;
@@ -2160,6 +2299,25 @@ __global__ void k_prepare(int T, const int4* __restrict__ tets, const double* __
   tile_f[tile_word(tile_tets, t, 7)] = 1.f;
 }
 
+// Node stiffness scale of the Jacobi preconditioner: k_i = sum over the
+// node's tets of tr(Ke_ii) / 3.  For the node's B-vector b the element apply
+// gives, in the tet frame, Ke_ii[a][a] = (c0 + c1) b_a^2 + c2 (|b|^2 - b_a^2),
+// so tr(Ke_ii) = (c0 + c1 + 2 c2) |b|^2; the rotation Re Ke_ii Re^T keeps the
+// trace, so k does not change from step to step.  Sums in ascending tet order.
+__global__ void k_node_stiffness(int N, int T, const int* __restrict__ inc_ptr, const int* __restrict__ inc_ent,
+                                 const double* __restrict__ Bv, const double* __restrict__ c_d, double* node_k) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double k = 0.0;
+  for (int q = inc_ptr[i]; q < inc_ptr[i + 1]; ++q) {
+    const int e = inc_ent[q], t = e >> 2, slot = e & 3;
+    const double* b = Bv + 12L * t + 3 * slot;
+    const double c = c_d[t] + c_d[(long)T + t] + 2.0 * c_d[2L * T + t];
+    k += c * (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+  }
+  node_k[i] = k / 3.0;
+}
+
 // Standalone y = A x (diagnostics and the apply-only measurement): pack, one
 // element-apply sweep, finalize.
 template <typename V4>
@@ -2352,6 +2510,9 @@ cudaError_t mixed_prepare(Context& c) {
   if (e != cudaSuccess) return e;
   k_prepare<<<nb, 256, 0, c.stream>>>(c.T, c.tets, c.Bv, c.D, c.V, c.b_f, c.c_f, c.b_d, c.c_d, c.tile_f,
                                       c.tile_tets);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  const int nn = c.N > 0 ? (c.N + 255) / 256 : 1;
+  k_node_stiffness<<<nn, 256, 0, c.stream>>>(c.N, c.T, c.inc_ptr, c.inc_ent, c.Bv, c.c_d, c.node_k);
   return cudaGetLastError();
 }
 
@@ -2454,6 +2615,8 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.r = c.r;
   a.p = c.p;
   a.diag = c.diag;
+  a.node_k = c.node_k;
+  a.precond = prm.preconditioner == OTFEM_PRECONDITIONER_JACOBI ? 1 : 0;
   a.re_f = c.re_f;
   a.b_f = c.b_f;
   a.c_f = c.c_f;

@@ -76,7 +76,7 @@ class GpuMesh:
         capi.check(self.lib.otfem_set_nodes(self.h, field, a.ctypes.data_as(_dp), a.size))
 
     def get(self, field):
-        out = np.zeros(self.N if field == capi.MASS else (self.N, 3))
+        out = np.zeros(self.N if field in (capi.MASS, capi.NODE_STIFFNESS) else (self.N, 3))
         capi.check(self.lib.otfem_get_nodes(self.h, field, out.ctypes.data_as(_dp), out.size))
         return out
 

@@ -39,11 +39,12 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.otfem_abi_version() == 4
+    assert lib.otfem_abi_version() == 5
     p = capi.default_params()
     assert p.solver == capi.SOLVER_REFERENCE
     assert p.mass_damping == 2.0 and p.min_iterations == 20 and p.max_iterations == 20
     assert p.rtol == 1e-6 and p.refresh_period == 16 and p.graph == 1
+    assert p.preconditioner == capi.PRECONDITIONER_JACOBI
 
 
 def _create(lib, tets, coord):

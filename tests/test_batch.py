@@ -89,7 +89,7 @@ def params(**kw):
     return capi.default_params(**base)
 
 
-def run_batch(beams, steps, variant=None):
+def run_batch(beams, steps, variant=None, **kw):
     b = Batch(beams)
     if variant is not None:
         capi.check(b.lib.otfem_set_apply_variant(b.h, variant))
@@ -99,7 +99,7 @@ def run_batch(beams, steps, variant=None):
     for _ in range(steps):
         b.set(capi.F_EXTERNAL, f)
         st = capi.StepStats()
-        capi.check(b.lib.otfem_simulate_ex(b.h, DT, 1, ctypes.byref(params()), ctypes.byref(st)))
+        capi.check(b.lib.otfem_simulate_ex(b.h, DT, 1, ctypes.byref(params(**kw)), ctypes.byref(st)))
         out.append((b.per_mesh(b.get(capi.COORD)), b.stats(), st))
     return b, out
 
@@ -176,6 +176,22 @@ def test_batch_apply_variants_agree(gpu):
     for k, bm in enumerate(beams):
         disp = np.abs(res[0][k] - bm["coord"]).max()
         assert np.abs(res[0][k] - res[1][k]).max() <= 1e-4 * disp
+
+
+def test_batch_preconditioner_same_answer_fewer_iterations(gpu):
+    beams = random_beams(4, seed=35, nx=(10, 16), nyz=(3, 5))
+    res, its = {}, {}
+    for pre in (capi.PRECONDITIONER_NONE, capi.PRECONDITIONER_JACOBI):
+        b, out = run_batch(beams, 3, preconditioner=pre)
+        res[pre] = out[-1][0]
+        its[pre] = np.sum([o[1][0] for o in out])
+        for _, (it, st, rel, _), _ in out:
+            assert np.all(st == capi.OK) and np.all(rel <= 1e-6)
+        b.close()
+    for k, bm in enumerate(beams):
+        disp = np.abs(res[0][k] - bm["coord"]).max()
+        assert np.abs(res[0][k] - res[1][k]).max() <= 1e-4 * disp
+    assert its[capi.PRECONDITIONER_JACOBI] < 0.9 * its[capi.PRECONDITIONER_NONE], its
 
 
 def test_batch_rejects_other_solvers_and_variants(gpu):

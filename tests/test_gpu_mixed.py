@@ -26,8 +26,10 @@ def rel_pos_err(x, x_ref, x_init):
 
 
 def test_mixed_vs_reference_converged_golden(gpu):
+    """Plain CG (the reference's method) takes the reference's iteration
+    counts; the Jacobi-preconditioned default reaches the same positions."""
     g = golden("converged")
-    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 20, params=mixed())
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 20, params=mixed(preconditioner=capi.PRECONDITIONER_NONE))
     for s in (1, 5, 20):
         x, v, st = out[s - 1]
         err = rel_pos_err(x, g[f"x_{s}"], g["coord"])
@@ -36,11 +38,65 @@ def test_mixed_vs_reference_converged_golden(gpu):
         assert st.status == capi.OK
         assert st.rel_residual <= 1e-6
         assert abs(st.iterations - int(it_ref)) <= max(6, 0.2 * it_ref)
+    _, outp = run_gpu(g["tets"], g["coord"], g["fixed"], 20, params=mixed())
+    for s in (1, 5, 20):
+        assert rel_pos_err(outp[s - 1][0], g[f"x_{s}"], g["coord"]) < POS_TOL, s
+    for _, _, st in outp:
+        assert st.status == capi.OK and st.rel_residual <= 1e-6
+
+
+def test_node_stiffness_is_the_trace_of_the_assembled_diagonal(gpu, oracle):
+    """OTFEM_NODE_STIFFNESS = tr(K_ii) / 3 of the oracle's assembled
+    (rotated) stiffness matrix, for every node."""
+    tets, coord, fixed = beam(6, 3, 4, jitter_seed=5)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    k = m.get(capi.NODE_STIFFNESS)
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*MATERIAL)
+    mass = o.get(oracle.MASS)
+    for _ in range(2):  # non-identity orientations in the assembled K
+        o.set(oracle.F_EXTERNAL, gravity_force(mass, fixed) * 50.0)
+        o.simulate(0.01, True)
+    rp, cols = o.k_pattern()
+    K = o.k_values()
+    diag = np.array([K[q] for i in range(len(rp) - 1) for q in range(rp[i], rp[i + 1]) if cols[q] == i])
+    ref = np.trace(diag, axis1=1, axis2=2) / 3.0
+    assert np.allclose(k, ref, rtol=1e-10, atol=0.0)
+    o.close()
+    m.close()
+
+
+@pytest.mark.parametrize("solver", [capi.SOLVER_MIXED, capi.SOLVER_FP64])
+def test_jacobi_preconditioner_same_answer_fewer_iterations(gpu, oracle, solver):
+    tets, coord, fixed = beam(24, 6, 6, jitter_seed=9)
+    _, ref = run_oracle(oracle, tets, coord, fixed, 4, converged=True, rtol=1e-11)
+    its = {}
+    for pre in (capi.PRECONDITIONER_NONE, capi.PRECONDITIONER_JACOBI):
+        _, out = run_gpu(tets, coord, fixed, 4, params=mixed(solver=solver, preconditioner=pre))
+        for s in range(4):
+            x, _, st = out[s]
+            assert st.status == capi.OK and st.rel_residual <= 1e-6
+            assert rel_pos_err(x, ref[s][0], coord) < POS_TOL, (pre, s)
+        its[pre] = np.mean([st.iterations for _, _, st in out])
+    assert its[capi.PRECONDITIONER_JACOBI] < 0.85 * its[capi.PRECONDITIONER_NONE], its
+
+
+def test_unknown_preconditioner_is_rejected(gpu):
+    tets, coord, fixed = beam(3, 2, 2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    rc, _ = m.step(0.01, True, mixed(preconditioner=7), check=False)
+    assert rc == capi.ERR_INVALID_ARGUMENT
+    m.close()
 
 
 def test_fp64_matrix_free_vs_reference(gpu):
+    """Plain CG in FP64 follows the reference's CG iterates: both stop at
+    rel. residual 1e-6 on nearly the same iterate."""
     g = golden("converged")
-    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 5, params=mixed(solver=capi.SOLVER_FP64))
+    _, out = run_gpu(g["tets"], g["coord"], g["fixed"], 5,
+                     params=mixed(solver=capi.SOLVER_FP64, preconditioner=capi.PRECONDITIONER_NONE))
     x, v, st = out[4]
     assert rel_pos_err(x, g["x_5"], g["coord"]) < 1e-7
     assert st.rel_residual <= 1e-6
