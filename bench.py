@@ -293,11 +293,10 @@ def timed_steps(lib, capi, torch, stream, h, params, steps, forces, dt, flush_l2
 
 
 def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
-    """Learned vs plain (and extrapolation) on a 64x16x16 beam under a
-    sinusoidal tip load (amplitude U[0,100] N, frequency U[0.5,5] Hz,
-    direction uniform), dt 0.01."""
+    """Learned vs plain CG (and the Jacobi and projected ablations) on a
+    64x16x16 beam under a sinusoidal tip load (amplitude U[0,100] N,
+    frequency U[0.5,5] Hz, direction uniform), dt 0.01."""
     from opentissue_gb300.fem import generate_blocks
-    from opentissue_gb300.warmstart import WarmStartNet, extrapolation_state
     I, J, K = 64, 16, 16
     tets, coord = generate_blocks(I, J, K, 0.1, 0.1, 0.1)
     coord = coord + np.random.default_rng(args.seed + 5).uniform(-0.01, 0.01, coord.shape)
@@ -307,20 +306,18 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
     d /= np.linalg.norm(d)
     tip = np.arange(coord.shape[0]) >= I * (J + 1) * (K + 1)
     w = WORKLOAD
-    extrap = WarmStartNet(capacity=0, seed=0)
-    extrap.set_state(extrapolation_state(net.state()))
     out = {}
-    for name, mlp, warm in (("plain", None, capi.WARM_START_PREVIOUS), ("extrapolation", extrap, capi.WARM_START_LEARNED),
-                            ("learned", net, capi.WARM_START_LEARNED)):
+    arms = (("plain", None, dict(preconditioner=capi.PRECONDITIONER_NONE)), ("plain_jacobi", None, {}),
+            ("projected", None, dict(warm_start=capi.WARM_START_PROJECTED)),
+            ("learned", net, dict(warm_start=capi.WARM_START_LEARNED)))
+    for name, mlp, kw in arms:
         h = make_handle(lib, capi, tets, coord, fixed, stream)
         if mlp is not None:
             mlp.attach(h)
-            if mlp is extrap:
-                capi.check(lib.otfem_set_warm_start_smoothing(h, 0))
         mass = get_mass(lib, capi, h, coord.shape[0])
         g = gravity(mass, fixed)
         p = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                max_iterations=5000, refresh_period=16, warm_start=warm)
+                                max_iterations=5000, refresh_period=16, **kw)
 
         def forces(k):
             f = g.copy()
@@ -334,7 +331,6 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
         if mlp is not None:
             mlp.detach(h)
         capi.check(lib.otfem_destroy(h))
-    extrap.close()
     disp = np.abs(out["plain"]["x"] - coord).max()
     res = {"workload": f"64x16x16 beam ({tets.shape[0]} tets), tip load {amp:.1f} N sin(2 pi {freq:.2f} t), "
                        f"{args.ab_steps} steps, dt 0.01, rel. residual 1e-6"}
@@ -343,6 +339,7 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
         if k != "plain":
             res[k]["position_difference_vs_plain"] = float(np.abs(v["x"] - out["plain"]["x"]).max() / disp)
     res["learned_over_plain"] = out["learned"]["tet_steps_per_s"] / out["plain"]["tet_steps_per_s"]
+    res["learned_over_projected"] = out["learned"]["tet_steps_per_s"] / out["projected"]["tet_steps_per_s"]
     return res
 
 
@@ -426,14 +423,14 @@ def run_ours(args, world, rank, local):
     tets, coord, fixed = build_mesh()
     T, N = tets.shape[0], coord.shape[0]
     n_free = int((fixed == 0).sum())
-    plain = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                max_iterations=5000, refresh_period=16)
-    learned = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                  max_iterations=5000, refresh_period=16, warm_start=capi.WARM_START_LEARNED)
-    # plain CG without the preconditioner: the reference's method on the GPU
-    plain_cg = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                   max_iterations=5000, refresh_period=16,
-                                   preconditioner=capi.PRECONDITIONER_NONE)
+    def solver_params(**kw):
+        return capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
+                                   max_iterations=5000, refresh_period=16, **kw)
+    # plain CG: the reference's method (no preconditioner, previous-velocity start) on the GPU
+    plain = solver_params(preconditioner=capi.PRECONDITIONER_NONE)
+    plain_jacobi = solver_params()
+    projected = solver_params(warm_start=capi.WARM_START_PROJECTED)
+    learned = solver_params(warm_start=capi.WARM_START_LEARNED)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def flush_l2():
@@ -441,13 +438,14 @@ def run_ours(args, world, rank, local):
             flush.fill_(1.0)
 
     def timed_run(h, params):
-        """W warm-up steps, then K steps timed on the device (L2 flushed
-        before each); the workload's gravity load."""
+        """The lead-in steps of the trajectory from rest and W warm-up steps,
+        then K steps timed on the device (L2 flushed before each); the
+        workload's gravity load."""
         mass = get_mass(lib, capi, h, N)
         fext = gravity(mass, fixed)
         capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, fext.ctypes.data_as(_dp), fext.size))
         stats = capi.StepStats()
-        for _ in range(args.warmup):
+        for _ in range(args.lead_in + args.warmup):
             capi.check(lib.otfem_simulate_ex(h, w["dt"], 1, ctypes.byref(params), None))
         torch.cuda.synchronize()
         n0 = ctypes.c_int64()
@@ -475,31 +473,23 @@ def run_ours(args, world, rank, local):
         return {"dev_s": dev_s, "its": its, "res": res, "applies": applies, "launches": int(n1.value - n0.value),
                 "x": x, "fext": fext}
 
-    # ---- plain CG (previous velocity), the extrapolation v + dv_prev alone
-    # (the network with its output zeroed) and the learned warm start, each
-    # on the same trajectory
-    from opentissue_gb300.warmstart import WarmStartNet, extrapolation_state
+    # ---- plain CG (the reference's method), Jacobi-preconditioned CG, the
+    # projected start without the network and the learned start, each on the
+    # same trajectory
     h_plain = make_handle(lib, capi, tets, coord, fixed, stream)
     h_learn = make_handle(lib, capi, tets, coord, fixed, stream)
-    h_extra = make_handle(lib, capi, tets, coord, fixed, stream)
     net.attach(h_learn)
-    extrap = WarmStartNet(capacity=0, seed=0)
-    extrap.set_state(extrapolation_state(net.state()))
-    extrap.attach(h_extra)
-    capi.check(lib.otfem_set_warm_start_smoothing(h_extra, 0))
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
     r_plain = timed_run(h_plain, plain)
     r_learn = timed_run(h_learn, learned)
     clocks = sampler.stop()
-    r_extra = timed_run(h_extra, learned)
-    extrap.detach(h_extra)
-    capi.check(lib.otfem_destroy(h_extra))
-    h_cg = make_handle(lib, capi, tets, coord, fixed, stream)
-    r_cg = timed_run(h_cg, plain_cg)
-    capi.check(lib.otfem_destroy(h_cg))
-    extrap.close()
+    ablations = {}
+    for name, prm in (("plain_jacobi", plain_jacobi), ("projected", projected)):
+        h_ab = make_handle(lib, capi, tets, coord, fixed, stream)
+        ablations[name] = timed_run(h_ab, prm)
+        capi.check(lib.otfem_destroy(h_ab))
     disp = np.abs(r_plain["x"] - coord).max()
     pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))
 
@@ -595,22 +585,26 @@ def run_ours(args, world, rank, local):
         "dtype": "f32 element apply, f64 CG vectors and reductions, bf16/f32 warm-start network",
         "data": "synthetic",
         "config": {"workload": WORKLOAD["name"],
-                   "warm_start": "learned (node MLP + 1-ring smoothing), trained in this run",
+                   "warm_start": "learned (node MLP on 1-ring mean inputs, trained in this run) in the projected search space",
                    "solver": "matrix-free persistent CG (OTFEM_SOLVER_MIXED), CUDA graph per step",
                    "preconditioner": "node Jacobi (OTFEM_PRECONDITIONER_JACOBI, the default)",
+                   "search_space": f"v + span{{network correction, last {learned.warm_history} velocity changes}}",
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
+                   "trajectory": f"timed steps {args.lead_in + args.warmup + 1}..{args.lead_in + args.warmup + args.steps} "
+                                 f"of the beam's motion from rest (every arm), after {args.lead_in} untimed lead-in "
+                                 f"and {args.warmup} warm-up steps",
                    "iterations_per_step": float(np.mean(r_learn["its"])),
                    "max_rel_residual": float(np.max(r_learn["res"])),
-                   "plain": {"value": plain_value, "unit": "tet-steps/s",
+                   "plain": {"method": "CG, no preconditioner, previous-velocity start (the reference's)",
+                             "value": plain_value, "unit": "tet-steps/s",
                              "ms_per_step": 1e3 * r_plain["dev_s"] / args.steps,
                              "iterations_per_step": float(np.mean(r_plain["its"])),
                              "max_rel_residual": float(np.max(r_plain["res"]))},
-                   "plain_unpreconditioned": {"value": total_tet_steps / r_cg["dev_s"], "unit": "tet-steps/s",
-                                              "iterations_per_step": float(np.mean(r_cg["its"])),
-                                              "max_rel_residual": float(np.max(r_cg["res"]))},
-                   "extrapolation_only": {"value": total_tet_steps / r_extra["dev_s"], "unit": "tet-steps/s",
-                                          "iterations_per_step": float(np.mean(r_extra["its"]))},
+                   "ablations": {k: {"value": total_tet_steps / r["dev_s"], "unit": "tet-steps/s",
+                                     "iterations_per_step": float(np.mean(r["its"])),
+                                     "max_rel_residual": float(np.max(r["res"]))} for k, r in ablations.items()},
                    "learned_over_plain": value / plain_value,
+                   "learned_over_projected": ablations["projected"]["dev_s"] / r_learn["dev_s"],
                    "position_difference_learned_vs_plain": pos_diff,
                    "training": train_info,
                    "other_configurations": extra},
@@ -645,6 +639,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--lead-in", type=int, default=10,
+                    help="untimed steps of the trajectory before the warm-up (the velocity history fills)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -76,8 +76,18 @@ enum {
 
 enum {
   OTFEM_WARM_START_PREVIOUS = 0, /* CG starts from the previous velocity (reference) */
-  OTFEM_WARM_START_LEARNED = 1   /* CG starts from v + MLP-predicted dv */
+  /* CG starts from the point of least energy x.A.x/2 - b.x on v + span{the
+   * network's correction, the last max(warm_history, 1) velocity changes};
+   * the network predicts v + dv (otfem_set_mlp) */
+  OTFEM_WARM_START_LEARNED = 1,
+  /* CG starts from the point of least energy on v + span{the last
+   * warm_history velocity changes} (projection onto previous solutions);
+   * one extra element-apply per vector and step */
+  OTFEM_WARM_START_PROJECTED = 2
 };
+
+/* Velocity changes kept for the projected and learned starts. */
+#define OTFEM_MAX_WARM_HISTORY 8
 
 enum {
   OTFEM_PRECONDITIONER_NONE = 0,   /* plain CG (the reference's method) */
@@ -100,10 +110,13 @@ typedef struct otfem_solver_params {
                                thread (bit-identical to the reference), 0 = parallel tree.
                                matrix-free: 1 = grid sums of the CTA totals in CTA order,
                                0 = FP64 atomic accumulation of them (faster) */
-  int warm_start;           /* OTFEM_WARM_START_* */
+  int warm_start;           /* OTFEM_WARM_START_* (matrix-free solvers of one mesh; a batch
+                               takes PREVIOUS or LEARNED with one velocity change) */
   int graph;                /* 1 = replay the step from a CUDA graph (default) */
   int preconditioner;       /* matrix-free: OTFEM_PRECONDITIONER_* (default JACOBI);
                                the reference solver ignores it */
+  int warm_history;         /* projected and learned starts: previous velocity changes in the
+                               search space, 0..OTFEM_MAX_WARM_HISTORY (default 4) */
 } otfem_solver_params;
 
 typedef struct otfem_step_stats {
@@ -265,11 +278,12 @@ OTFEM_API int otfem_mlp_predict(otfem_mlp m, const float* x, int64_t n, float* y
  * The network must outlive its use and must not be trained while steps
  * that use it are in flight. */
 OTFEM_API int otfem_set_mlp(otfem_handle h, otfem_mlp m);
-/* Passes (0..64, default 2) of 1-ring mean aggregation over the network's
+/* Passes (0..64, default 0) of 1-ring mean aggregation over the network's
  * correction net(inputs) before it enters the initial guess: each pass
  * replaces a node's correction by the mean over its tets of the tet's node
- * mean.  (The network's per-node errors are rough; the smoothed correction
- * leaves a smaller initial residual.) */
+ * mean.  (Smoothing lowers the initial residual of the network's guess on
+ * its own; inside the projected search space it changes nothing measurable
+ * and costs one node pass each.) */
 OTFEM_API int otfem_set_warm_start_smoothing(otfem_handle h, int32_t passes);
 
 /* ---- host staging (no counterpart in the reference) ---------------------- */

@@ -25,7 +25,8 @@ ERR_UNSUPPORTED = -8
 COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B, NODE_STIFFNESS = range(8)
 # solvers
 SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
-WARM_START_PREVIOUS, WARM_START_LEARNED = 0, 1
+WARM_START_PREVIOUS, WARM_START_LEARNED, WARM_START_PROJECTED = 0, 1, 2
+MAX_WARM_HISTORY = 8
 PRECONDITIONER_NONE, PRECONDITIONER_JACOBI = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2
 NUM_APPLY_VARIANTS = 4
@@ -46,6 +47,7 @@ class SolverParams(ctypes.Structure):
         ("warm_start", ctypes.c_int),
         ("graph", ctypes.c_int),
         ("preconditioner", ctypes.c_int),
+        ("warm_history", ctypes.c_int),
     ]
 
 

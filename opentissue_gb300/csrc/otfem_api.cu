@@ -66,7 +66,8 @@ void free_all(Context& c) {
     if (p) cudaFree(p);
   if (c.stats_host) cudaFreeHost(c.stats_host);
   if (c.bmesh_host) cudaFreeHost(c.bmesh_host);
-  void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.bmesh, c.bacc, c.bmask};
+  void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.bmesh, c.bacc, c.bmask,
+                   c.warm_hist, c.warm_prod, c.warm_part};
   for (void* p : batch)
     if (p) cudaFree(p);
   if (c.graph) cudaGraphExecDestroy(c.graph);
@@ -98,17 +99,41 @@ int check_params(const Context& c, const otfem_solver_params& p) {
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "iteration counts must be non-negative");
   if (p.solver != OTFEM_SOLVER_REFERENCE && !(p.rtol >= 0.0))
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
-  if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED)
+  if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED &&
+      p.warm_start != OTFEM_WARM_START_PROJECTED)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
+  if (p.warm_history < 0 || p.warm_history > OTFEM_MAX_WARM_HISTORY)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "warm_history out of range");
   if (p.preconditioner != OTFEM_PRECONDITIONER_NONE && p.preconditioner != OTFEM_PRECONDITIONER_JACOBI)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown preconditioner");
   if (c.num_meshes > 1 && p.solver != OTFEM_SOLVER_MIXED)
     return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes steps with OTFEM_SOLVER_MIXED (one CG per mesh)");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && p.solver != OTFEM_SOLVER_MIXED)
     return fail(OTFEM_ERR_UNSUPPORTED, "the learned warm start runs with OTFEM_SOLVER_MIXED");
+  if (p.warm_start == OTFEM_WARM_START_PROJECTED && (p.solver != OTFEM_SOLVER_MIXED || c.num_meshes > 1))
+    return fail(OTFEM_ERR_UNSUPPORTED, "the projected start runs with OTFEM_SOLVER_MIXED on one mesh");
+  if (p.warm_start == OTFEM_WARM_START_PROJECTED && p.warm_history < 1)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "the projected start needs warm_history >= 1");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && !c.mlp)
     return fail(OTFEM_ERR_NOT_INITIALIZED, "learned warm start without a network (otfem_set_mlp)");
   return OTFEM_OK;
+}
+
+// The projected and learned starts of one mesh search previous velocity
+// changes: their history, the products and sums are allocated (the history
+// zeroed) by the first step that needs them; from then on every mixed step
+// of the mesh records its velocity change.
+cudaError_t ensure_history(Context& c, const otfem_solver_params& p) {
+  const bool needs = p.solver == OTFEM_SOLVER_MIXED && c.num_meshes <= 1 &&
+                     (p.warm_start == OTFEM_WARM_START_PROJECTED || p.warm_start == OTFEM_WARM_START_LEARNED);
+  if (!needs || c.warm_hist) return cudaSuccess;
+  const size_t n = size_t(c.N > 0 ? c.N : 1);
+  cudaError_t e;
+  if ((e = cudaMalloc(&c.warm_hist, sizeof(float4) * 2 * otfem::kMaxHistory * n)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c.warm_prod, sizeof(float4) * (otfem::kMaxWarmDirs + 1) * n)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&c.warm_part, sizeof(double) * otfem::kMaxWarmSums * size_t(c.mf_grid))) != cudaSuccess)
+    return e;
+  return cudaMemsetAsync(c.warm_hist, 0, sizeof(float4) * 2 * otfem::kMaxHistory * n, c.stream);
 }
 
 // After the orientation phase of a matrix-free step: the network inputs of
@@ -145,9 +170,10 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
 
 std::string step_key(const Context& c, double dt, bool warp, const otfem_solver_params& p) {
   char buf[320];
-  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d|%d|%p|%d|%d", p.solver, dt, int(warp), p.mass_damping,
-           p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots, p.warm_start,
-           p.preconditioner, static_cast<void*>(c.mlp), c.collect, c.warm_smoothing);
+  snprintf(buf, sizeof(buf), "%d|%a|%d|%a|%d|%d|%a|%d|%d|%d|%d|%d|%p|%p|%d|%d", p.solver, dt, int(warp),
+           p.mass_damping, p.min_iterations, p.max_iterations, p.rtol, p.refresh_period, p.sequential_dots,
+           p.warm_start, p.preconditioner, p.warm_history, static_cast<void*>(c.mlp),
+           static_cast<void*>(c.warm_hist), c.collect, c.warm_smoothing);
   return buf;
 }
 
@@ -176,6 +202,7 @@ void otfem_default_params(otfem_solver_params* p) {
   p->warm_start = OTFEM_WARM_START_PREVIOUS;
   p->graph = 1;
   p->preconditioner = OTFEM_PRECONDITIONER_JACOBI;
+  p->warm_history = 4;
 }
 
 const char* otfem_last_error(void) { return g_last_error.c_str(); }
@@ -368,6 +395,8 @@ static int init_impl(Context& c, double young, double poisson, double density, d
   // no velocity history yet (learned warm start)
   OT_CUDA(cudaMemsetAsync(c.dv_last, 0, sizeof(float4) * size_t(c.N), c.stream));
   OT_CUDA(cudaMemsetAsync(c.warm_dv, 0, sizeof(float4) * size_t(c.N), c.stream));
+  if (c.warm_hist)
+    OT_CUDA(cudaMemsetAsync(c.warm_hist, 0, sizeof(float4) * 2 * otfem::kMaxHistory * size_t(c.N), c.stream));
   // choose the element-apply variant for this mesh
   if ((e = otfem::autotune_apply(c)) != cudaSuccess) return cuda_fail(e, "autotune");
   std::vector<double> vol(size_t(c.T));
@@ -560,6 +589,8 @@ int otfem_simulate_ex(otfem_handle h, double dt, int warp, const otfem_solver_pa
   else otfem_default_params(&p);
   int rc = check_params(c, p);
   if (rc != OTFEM_OK) return rc;
+  cudaError_t e0 = ensure_history(c, p);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "warm-start history");
   bool use_warp = warp != 0;
   cudaError_t e;
   if (p.graph) {
@@ -604,6 +635,8 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
   int rc = check_params(c, p);
   if (rc != OTFEM_OK) return rc;
   if (p.solver == OTFEM_SOLVER_REFERENCE) return fail(OTFEM_ERR_UNSUPPORTED, "phases exist for the matrix-free solvers");
+  cudaError_t e0 = ensure_history(c, p);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "warm-start history");
   cudaError_t e;
   if (phase == OTFEM_PHASE_ORIENT) {
     if ((e = otfem::launch_mixed_orient(c, dt, warp != 0, p.solver)) != cudaSuccess) return cuda_fail(e, "orient phase");

@@ -16,6 +16,12 @@ namespace otfem {
 constexpr int kMaxPartials = 16;
 // Doubles between consecutive grid-sum accumulators (one 128-byte line each).
 constexpr int kAccStride = 16;
+// Projected start: velocity changes kept, and the grid sums of its Gram
+// system (pairs of up to kMaxHistory + 1 directions, and their right-hand
+// sides).
+constexpr int kMaxHistory = OTFEM_MAX_WARM_HISTORY;
+constexpr int kMaxWarmDirs = kMaxHistory + 1;
+constexpr int kMaxWarmSums = kMaxWarmDirs * (kMaxWarmDirs + 1) / 2 + kMaxWarmDirs;
 // Rows of the per-iteration CG trace kept per step.  Each row holds
 // kTraceCols doubles: rho, p.q, alpha, beta, then SM-clock stamps (cycles
 // since the kernel started, taken on CTA 0) after the apply sweep, after its
@@ -40,6 +46,7 @@ struct DeviceSync {
                                  // sets of 8 values, each value on its own 128-byte line
   unsigned tile_ticket;      // staged apply: monotonic tile tickets
   unsigned pad5[31];
+  double wacc[kMaxWarmSums];  // projected start: Gram system totals (FP64 reductions)
 };
 
 // Per-mesh state of a batched solve (device memory, one per mesh).
@@ -121,6 +128,7 @@ struct Context {
   float4* r_f = nullptr;                                   // N: mixed-solver residual
   float4* g_f = nullptr;                                   // 4T: mixed elastic node forces
   bool re_f32_pending = false;  // the FP64 m_Re copy lags the FP32 orientations
+  bool quat_in_g_f = false;     // g_f[4t + k].w holds quaternion component k of tet t (mixed orientation)
   double4* q_d = nullptr;                                  // N (FP64 apply accumulator)
   double4 *p_d4 = nullptr, *v_d4 = nullptr;               // N (FP64 apply operands)
   double* partials = nullptr;                              // kMaxPartials * max grid
@@ -145,13 +153,23 @@ struct Context {
   float4* dv_last = nullptr;      // N (w unused)
   float4* warm_dv = nullptr;      // N
   float4* warm_tmp = nullptr;     // N, allocated with smoothing passes
-  // learned start, projected: operands d = dv_prev, c = the network's
-  // correction and their products A d, A c (4N, allocated with a network)
+  // learned start of a batch, projected: operands d = dv_prev, c = the
+  // network's correction and their products A d, A c (4N, allocated with a
+  // network)
   float4* warm_ops = nullptr;
+  // projected and learned starts of one mesh (allocated by the first step
+  // that uses them): the velocity-change history as a difference basis
+  // (D_0 = the last change, D_j = its j-th backward difference; (hi, lo)
+  // float pairs, hi.w = 1 on free nodes), the products of the search
+  // directions with A, the network's correction as a direction, and per-CTA
+  // partial sums of the Gram system
+  float4* warm_hist = nullptr;    // 2 kMaxHistory x N: hi parts, then lo parts
+  float4* warm_prod = nullptr;    // (kMaxWarmDirs + 1) x N: products, then the correction
+  double* warm_part = nullptr;    // kMaxWarmSums x max grid
   // two kept copies of the CG iterate (hi, lo) from the true-residual
   // refreshes: a solve stopped at the precision floor returns the best one
   float4* v_keep = nullptr;       // 4N
-  int warm_smoothing = 2;         // 1-ring mean passes over the network's correction
+  int warm_smoothing = 0;         // 1-ring mean passes over the network's correction
   float* features = nullptr;      // N x kFeatureStride, allocated when collecting
   int collect = 0;
   bool features_valid = false;    // c.features hold the inputs of the last step
@@ -225,6 +243,23 @@ cudaError_t launch_node_features(Context& c, bool predict);
 // Staged-apply tiles: at most kTileMaxTets tets of kTileWords 32-bit words.
 constexpr int kTileMaxTets = 512;
 constexpr int kTileWords = 20;
+
+// Rotation of a unit quaternion (x, y, z, w), row-major.
+__device__ __forceinline__ void quaternion_to_rotation(float4 q, float* R) {
+  const float xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
+  const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+  const float xw = q.x * q.w, yw = q.y * q.w, zw = q.z * q.w;
+  R[0] = 1.f - 2.f * (yy + zz), R[1] = 2.f * (xy - zw), R[2] = 2.f * (xz + yw);
+  R[3] = 2.f * (xy + zw), R[4] = 1.f - 2.f * (xx + zz), R[5] = 2.f * (yz - xw);
+  R[6] = 2.f * (xz - yw), R[7] = 2.f * (yz + xw), R[8] = 1.f - 2.f * (xx + yy);
+}
+
+// Word w of tet t in the staged-apply tiles (Context::tile_f).
+__device__ __forceinline__ long tile_word(int tile_tets, int t, int w) {
+  const int tile = t / tile_tets;
+  return (long(tile) * kTileWords + w) * tile_tets + (t - tile * tile_tets);
+}
+
 // Writes m_Re (FP64) from the FP32 orientations of the last mixed step.
 cudaError_t sync_orientations(Context& c);
 cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params& p);

@@ -120,7 +120,14 @@ struct MixedArgs {
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
   const float4* warm_dv;                // learned guess v + warm_dv (null: plain start from v)
   float4* dv_last;                      // in: dv_prev; out: v_new - v_old per free node
-  float4 *wd, *wc, *ad, *ac;            // learned start: operands d, c and products A d, A c
+  float4 *wd, *wc, *ad, *ac;            // learned start of a batch: operands d, c and products A d, A c
+  // projected / learned start of one mesh (see Context::warm_hist)
+  float4* hist;                         // difference basis: hi parts (8 x N), then lo parts (8 x N); null: none
+  float4* wprod;                        // products A W_j (slots 0..8), the network's correction (slot 9)
+  double* wpart;                        // per-CTA partial sums of the Gram system (ordered sums)
+  int hist_k;                           // basis vectors searched this step
+  int hist_rec;                         // basis vectors the step records
+  int nwarm;                            // search directions this step (0: start from v)
   float4* v_keep;                       // kept iterates: copy k at v_keep[2kN + i] (hi), [(2k+1)N + i] (lo)
   // batched solve (see Context)
   int num_meshes;
@@ -230,20 +237,6 @@ __device__ __forceinline__ float4 rotation_to_quaternion(const float* R) {
   }
   const float n = rsqrtf(x * x + y * y + z * z + w * w);
   return make_float4(x * n, y * n, z * n, w * n);
-}
-__device__ __forceinline__ void quaternion_to_rotation(float4 q, float* R) {
-  const float xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
-  const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
-  const float xw = q.x * q.w, yw = q.y * q.w, zw = q.z * q.w;
-  R[0] = 1.f - 2.f * (yy + zz), R[1] = 2.f * (xy - zw), R[2] = 2.f * (xz + yw);
-  R[3] = 2.f * (xy + zw), R[4] = 1.f - 2.f * (xx + zz), R[5] = 2.f * (yz - xw);
-  R[6] = 2.f * (xz - yw), R[7] = 2.f * (yz + xw), R[8] = 1.f - 2.f * (xx + yy);
-}
-
-// Word w of tet t in the staged-apply tiles.
-__device__ __forceinline__ long tile_word(int tile_tets, int t, int w) {
-  const int tile = t / tile_tets;
-  return (long(tile) * kTileWords + w) * tile_tets + (t - tile * tile_tets);
 }
 
 // Grid barriers and grid reductions.  Every CTA passes the same sequence of
@@ -620,9 +613,6 @@ __device__ __forceinline__ void warm_projection(const double* t, double& gd, dou
     else if (okc) gc = cr / cc;
   }
 }
-struct FinWarm {
-  __device__ void operator()(const double* t, double* o) const { warm_projection(t, o[0], o[1]); }
-};
 
 // Coherent (L2) load of node data written by other CTAs within the launch.
 __device__ __forceinline__ float4 load_acc(const float4* p) { return __ldcg(p); }
@@ -976,8 +966,8 @@ __device__ __forceinline__ int claim_tile(const MixedArgs& a) {
 // bandwidth take more tiles.  On a copy that does not complete within
 // spin_limit cycles the CTA sets OTFEM_ERR_TIMEOUT, stops, and waits (again
 // bounded) for the copies it still has in flight before returning.
-__device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
-                             unsigned char* smem, const unsigned char* mask) {
+template <typename Body>
+__device__ void staged_sweep(const MixedArgs& a, unsigned char* smem, const unsigned char* mask, Body body) {
   const int TT = a.tile_tets;
   const unsigned tile_bytes = unsigned(TT) * kTileWords * sizeof(float);
   auto stage = [smem](int sb) { return reinterpret_cast<float*>(smem + sb * kStageBytes); };
@@ -1011,31 +1001,7 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
     if (tile < 0) break;
     const bool ok = mbar_wait(&bar[sb], (j >> 1) & 1, a.spin_limit);
     const int t = tile * TT + tid;
-    if (ok && tid < TT && t < a.T && (!mask || mask[a.mesh_of_tet[t]])) {
-      const float* w = stage(sb);
-      const int nn[4] = {__float_as_int(w[tid]), __float_as_int(w[TT + tid]), __float_as_int(w[2 * TT + tid]),
-                         __float_as_int(w[3 * TT + tid])};
-      float4 wv[4], lo[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) wv[k] = u4[nn[k]];
-      if (ulo) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) lo[k] = ulo[nn[k]];
-      } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) lo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      float Re[9], b[9];
-      quaternion_to_rotation(make_float4(w[4 * TT + tid], w[5 * TT + tid], w[6 * TT + tid], w[7 * TT + tid]), Re);
-#pragma unroll
-      for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT + tid];
-      float du[3][3], f[4][3];
-      tet_differences<float>(wv, lo, du);
-      element_apply<float>(Re, b, w[17 * TT + tid], w[18 * TT + tid], w[19 * TT + tid], scale, du, f);
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (wv[k].w != 0) red_add(q4 + nn[k], f[k][0], f[k][1], f[k][2]);
-    }
+    if (ok && tid < TT && t < a.T && (!mask || mask[a.mesh_of_tet[t]])) body(stage(sb), TT, tid);
     // every thread is done with buffer sb: refill it with the next claim
     if (__syncthreads_or(!ok)) {
       failed = true;
@@ -1066,6 +1032,83 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
   }
 }
 
+// A staged tile's words for tet `tid`: node ids, rotation, B-vectors, constants.
+struct StagedTet {
+  int nn[4];
+  float Re[9], b[9], c0, c1, c2;
+  __device__ __forceinline__ StagedTet(const float* w, int TT, int tid) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) nn[k] = __float_as_int(w[k * TT + tid]);
+    quaternion_to_rotation(make_float4(w[4 * TT + tid], w[5 * TT + tid], w[6 * TT + tid], w[7 * TT + tid]), Re);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT + tid];
+    c0 = w[17 * TT + tid];
+    c1 = w[18 * TT + tid];
+    c2 = w[19 * TT + tid];
+  }
+};
+
+// q += dt^2 K_e u for one tet (FP32; u with an optional lo part).
+__device__ __forceinline__ void tet_apply(const float* Re, const float* b, float c0, float c1, float c2, float scale,
+                                          const int (&nn)[4], const float4* u4, const float4* ulo, float4* q4) {
+  float4 wv[4], lo[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) wv[k] = u4[nn[k]];
+  if (ulo) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) lo[k] = ulo[nn[k]];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) lo[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  float du[3][3], f[4][3];
+  tet_differences<float>(wv, lo, du);
+  element_apply<float>(Re, b, c0, c1, c2, scale, du, f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (wv[k].w != 0) red_add(q4 + nn[k], f[k][0], f[k][1], f[k][2]);
+}
+
+__device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                             unsigned char* smem, const unsigned char* mask) {
+  staged_sweep(a, smem, mask, [&](const float* w, int TT, int tid) {
+    const StagedTet e(w, TT, tid);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
+  });
+}
+
+// Search direction j of the projected start: basis vector j of the
+// velocity-change history, then the network's correction.
+__device__ __forceinline__ const float4* warm_dir(const MixedArgs& a, int j) {
+  return j < a.hist_k ? a.hist + size_t(j) * a.N : a.wprod + size_t(kMaxWarmDirs) * a.N;
+}
+
+// Projected start: A W_j for every search direction in one pass over the
+// tets, whose data is loaded (staged) once for all directions.
+__device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char* smem) {
+  staged_sweep(a, smem, nullptr, [&](const float* w, int TT, int tid) {
+    const StagedTet e(w, TT, tid);
+    for (int j = 0; j < a.nwarm; ++j)
+      tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
+  });
+}
+__device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
+  const int T = a.T;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+    const int4 n = a.tets[t];
+    const int nn[4] = {n.x, n.y, n.z, n.w};
+    float Re[9], b[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      Re[k] = a.re_f[(long)k * T + t];
+      b[k] = a.b_f[(long)k * T + t];
+    }
+    const float c0 = a.c_f[t], c1 = a.c_f[T + t], c2 = a.c_f[2L * T + t];
+    for (int j = 0; j < a.nwarm; ++j)
+      tet_apply(Re, b, c0, c1, c2, scale, nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
+  }
+}
+
 // One element-apply sweep with the mesh's variant.  `mask` (batched solves
 // only, variants kApplyTets and kApplyStaged) selects the meshes whose tets
 // take part.
@@ -1084,6 +1127,141 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
     apply_tets<R>(a, u4, ulo, q4, re, bb, cc, scale, mask);
   else if (a.apply_variant == kApplyGather) apply_patches_gather<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
   else apply_patches<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
+}
+
+// Projected start: A W_j for every search direction (products into
+// a.wprod).  Tets and staged variants do all directions in one pass; the
+// patch variants sweep once per direction.
+__device__ bool apply_directions(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round) {
+  if (a.apply_variant == kApplyStaged) {
+    apply_staged_dirs(a, scale, smem);
+    return true;
+  }
+  if (a.apply_variant == kApplyTets) {
+    apply_tets_dirs(a, scale);
+    return true;
+  }
+  for (int j = 0; j < a.nwarm; ++j) {
+    if (j > 0 && !grid_barrier(a.sync, a.spin_limit, round)) return false;
+    apply_sweep<float>(a, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N, a.re_f, a.b_f, a.c_f, scale, smem);
+  }
+  return true;
+}
+
+// Grid sums of nv <= kMaxWarmSums values per free node (value m of node i:
+// val(i, m)) for the projected start; every CTA receives the totals in
+// tot[].  Each thread accumulates (hi, lo) pairs for chunks of 8 values,
+// warp butterflies and the CTA sum follow, then FP64: atomic reductions
+// into sync->wacc (zero at launch), or with a.ordered_sums per-CTA partials
+// that every CTA adds up in CTA order.
+template <typename Val>
+__device__ bool grid_sum_wide(const MixedArgs& a, int nv, Val val, double* tot, unsigned& round) {
+  constexpr int kWarps = kBlock / 32;
+  __shared__ DF s_w[kWarps][kMaxWarmSums];
+  __shared__ int s_ok;
+  const long gstride = (long)gridDim.x * blockDim.x;
+  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int warp = threadIdx.x >> 5;
+  for (int c0 = 0; c0 < nv; c0 += 8) {
+    DF acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = DF{0.f, 0.f};
+    for (long i = gtid; i < a.N; i += gstride) {
+      if (a.fixed[i]) continue;
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (c0 + k < nv) acc[k] = df_add(acc[k], DF{val(i, c0 + k), 0.f});
+    }
+    DF x;
+    const int k = warp_totals<DF, 8>(acc, x);
+    if (k >= 0 && c0 + k < nv) s_w[warp][c0 + k] = x;
+  }
+  __syncthreads();
+  for (int m = threadIdx.x; m < nv; m += blockDim.x) {
+    DF t = DF{0.f, 0.f};
+    for (int w = 0; w < kWarps; ++w) t = df_add(t, s_w[w][m]);
+    const double d = AccOps<DF>::to_double(t);
+    if (a.ordered_sums) a.wpart[size_t(m) * gridDim.x + blockIdx.x] = d;
+    else atomicAdd(&a.sync->wacc[m], d);
+  }
+  __syncthreads();
+  ++round;
+  if (threadIdx.x == 0) s_ok = sync_round(a.sync, round, a.spin_limit) ? 1 : 0;
+  __syncthreads();
+  const bool ok = s_ok != 0;
+  if (ok) {
+    for (int m = threadIdx.x; m < nv; m += blockDim.x) {
+      if (a.ordered_sums) {
+        double t = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(a.wpart + size_t(m) * gridDim.x + b);
+        tot[m] = t;
+      } else {
+        tot[m] = __ldcg(&a.sync->wacc[m]);
+      }
+    }
+  }
+  __syncthreads();
+  return ok;
+}
+
+// The projected start's coefficients: the least-energy point of v + span{W_j}
+// solves G g = h with G_ij = W_i.A W_j and h_i = W_i.(b - A v).  `tot` holds
+// G's upper triangle row by row, then h.  Directions are taken in order
+// (the newest velocity change first); one whose A-norm is not positive and
+// finite, or that lies (nearly) in the span of the ones before it (Cholesky
+// pivot of the unit-diagonal G below 1e-9), gets g_j = 0.
+__device__ void warm_solve(const double* tot, int n, double* g) {
+  double L[kMaxWarmDirs][kMaxWarmDirs], sc[kMaxWarmDirs], y[kMaxWarmDirs];
+  bool act[kMaxWarmDirs];
+  auto G = [&](int i, int j) {
+    if (i > j) {
+      const int t = i;
+      i = j;
+      j = t;
+    }
+    return tot[i * n - i * (i - 1) / 2 + (j - i)];
+  };
+  const double* h = tot + n * (n + 1) / 2;
+  for (int i = 0; i < n; ++i) {
+    const double d = G(i, i);
+    act[i] = d > 0.0 && isfinite(d) && isfinite(h[i]);
+    sc[i] = act[i] ? rsqrt(d) : 0.0;
+    g[i] = 0.0;
+  }
+  for (int j = 0; j < n; ++j) {
+    if (!act[j]) continue;
+    double piv = 1.0;
+    for (int k = 0; k < j; ++k)
+      if (act[k]) piv -= L[j][k] * L[j][k];
+    if (!(piv > 1e-9)) {
+      act[j] = false;
+      continue;
+    }
+    L[j][j] = sqrt(piv);
+    const double inv = 1.0 / L[j][j];
+    for (int i = j + 1; i < n; ++i) {
+      if (!act[i]) continue;
+      double t = G(i, j) * sc[i] * sc[j];
+      for (int k = 0; k < j; ++k)
+        if (act[k]) t -= L[i][k] * L[j][k];
+      L[i][j] = t * inv;
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    if (!act[j]) continue;
+    double t = h[j] * sc[j];
+    for (int k = 0; k < j; ++k)
+      if (act[k]) t -= L[j][k] * y[k];
+    y[j] = t / L[j][j];
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    if (!act[j]) continue;
+    double t = y[j];
+    for (int i = j + 1; i < n; ++i)
+      if (act[i]) t -= L[i][j] * g[i];
+    g[j] = t / L[j][j];
+  }
+  for (int j = 0; j < n; ++j) g[j] = act[j] && isfinite(g[j]) ? g[j] * sc[j] : 0.0;
 }
 
 template <typename V4, typename R>
@@ -1107,6 +1285,33 @@ __device__ __forceinline__ void trace_row(const MixedArgs& a, int row, double rh
   tr[3] = beta;
   for (int k = 0; k < 5; ++k) tr[4 + k] = stamp[k];
   tr[9] = double(cycles_now() - t_start);
+}
+
+// The velocity-change history as a difference basis: D_0 = the newest change,
+// D_j = the j-th backward difference of the last changes (new D_j = new
+// D_{j-1} - old D_{j-1}), kept as (hi, lo) float pairs.  The basis spans the
+// same space as the last kMaxHistory changes, but for a smooth trajectory its
+// vectors are far from parallel, so their Gram system stays well conditioned
+// in FP32; the pairs keep the differences exact to ~1e-14 of each level.
+__device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long i, const double (&dv)[3]) {
+  const long N = a.N;
+  float hi[3], lo[3];
+  for (int c = 0; c < 3; ++c) {
+    hi[c] = float(dv[c]);
+    lo[c] = float(dv[c] - double(hi[c]));
+  }
+  for (int j = 0; j < a.hist_rec; ++j) {
+    const float4 oh = a.hist[size_t(j) * N + i], ol = a.hist[size_t(kMaxHistory + j) * N + i];
+    a.hist[size_t(j) * N + i] = make_float4(hi[0], hi[1], hi[2], 1.f);
+    a.hist[size_t(kMaxHistory + j) * N + i] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    // next level: this level's new value minus its old one
+    const float ohc[3] = {oh.x, oh.y, oh.z}, olc[3] = {ol.x, ol.y, ol.z};
+    for (int c = 0; c < 3; ++c) {
+      const DF d = df_add(DF{hi[c], lo[c]}, DF{-ohc[c], -olc[c]});
+      hi[c] = d.hi;
+      lo[c] = d.lo;
+    }
+  }
 }
 
 __device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int applies, bool converged, double rho,
@@ -1171,14 +1376,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     // never accumulated (w = 0).
     store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
     a.q_f[i] = zero4;
-    if (a.wd) {
-      // learned start: directions d = dv_prev and c = the network's correction
-      const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
-      const float fw = fx ? 0.f : 1.f;
-      a.wd[i] = make_float4(d.x, d.y, d.z, fw);
-      a.wc[i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fw);
-      a.ad[i] = zero4;
-      a.ac[i] = zero4;
+    if (a.nwarm) {
+      // learned start: the network's correction c = its dv - dv_prev is the
+      // last search direction
+      if (a.nwarm > a.hist_k) {
+        const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
+        a.wprod[size_t(kMaxWarmDirs) * N + i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fx ? 0.f : 1.f);
+      }
+      for (int j = 0; j < a.nwarm; ++j) a.wprod[size_t(j) * N + i] = zero4;
     }
   }
   double tot[1];
@@ -1186,21 +1391,22 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const double bnorm2 = tot[0];
   const double thresh = a.rtol * a.rtol * bnorm2;
 
-  // Initial residual r = b - A v (FP64), p = r; with the learned start also
-  // A d and A c, and the start moves to v + gamma_d d + gamma_c c.
+  // Initial residual r = b - A v (FP64), p = S r.  Projected and learned
+  // starts: also A W_j for the search directions W_j, and the start moves to
+  // the least-energy point v + sum_j g_j W_j (warm_solve), whose residual is
+  // r - sum_j g_j A W_j.
   int applies = 1;
   apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
-  if (a.wd) {
+  if (a.nwarm) {
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    apply_sweep<float>(a, a.wd, nullptr, a.ad, a.re_f, a.b_f, a.c_f, scale, smem);
-    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    apply_sweep<float>(a, a.wc, nullptr, a.ac, a.re_f, a.b_f, a.c_f, scale, smem);
-    applies += 2;
+    if (!apply_directions(a, scale, smem, round)) return;
+    applies += a.nwarm;
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-  double gam[2] = {0.0, 0.0};
-  if (a.wd) {
-    DF s5[5] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  __shared__ double s_gam[kMaxWarmDirs];
+  if (a.nwarm) {
+    const int nw = a.nwarm;
+    // r = b - A v; A W_j += diag W_j (the mass term)
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
@@ -1209,23 +1415,34 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
       rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
       rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
-      const float df = float(dg);
-      const float4 d = a.wd[i], c = a.wc[i], ad4 = load_acc(a.ad + i), ac4 = load_acc(a.ac + i);
-      const float adx = df * d.x + ad4.x, ady = df * d.y + ad4.y, adz = df * d.z + ad4.z;
-      const float acx = df * c.x + ac4.x, acy = df * c.y + ac4.y, acz = df * c.z + ac4.z;
-      s5[0] = df_add(s5[0], DF{d.x * adx + d.y * ady + d.z * adz, 0.f});
-      s5[1] = df_add(s5[1], DF{d.x * acx + d.y * acy + d.z * acz, 0.f});
-      s5[2] = df_add(s5[2], DF{c.x * acx + c.y * acy + c.z * acz, 0.f});
-      s5[3] = df_add(s5[3], DF{d.x * rf[0] + d.y * rf[1] + d.z * rf[2], 0.f});
-      s5[4] = df_add(s5[4], DF{c.x * rf[0] + c.y * rf[1] + c.z * rf[2], 0.f});
       a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-      a.ad[i] = make_float4(adx, ady, adz, 0.f);
-      a.ac[i] = make_float4(acx, acy, acz, 0.f);
+      const float df = float(dg);
+      for (int j = 0; j < nw; ++j) {
+        const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
+        a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
+      }
     }
-    if (!grid_reduce<DF, 5, 2>(a, s5, gam, round, FinWarm())) return;
+    // Gram system: W_i.A W_j (i <= j) row by row, then W_i.r
+    __shared__ signed char s_pi[kMaxWarmSums], s_pj[kMaxWarmSums];
+    __shared__ double s_tot[kMaxWarmSums];
+    if (threadIdx.x == 0) {
+      int m = 0;
+      for (int i = 0; i < nw; ++i)
+        for (int j = i; j < nw; ++j, ++m) s_pi[m] = (signed char)i, s_pj[m] = (signed char)j;
+      for (int i = 0; i < nw; ++i, ++m) s_pi[m] = (signed char)i, s_pj[m] = -1;
+    }
+    __syncthreads();
+    const int nv = nw * (nw + 1) / 2 + nw;
+    auto gram = [&](long i, int m) -> float {
+      const float4 w = warm_dir(a, s_pi[m])[i];
+      const float4 q = s_pj[m] >= 0 ? a.wprod[size_t(s_pj[m]) * N + i] : a.r_f[i];
+      return w.x * q.x + w.y * q.y + w.z * q.z;
+    };
+    if (!grid_sum_wide(a, nv, gram, s_tot, round)) return;
+    if (threadIdx.x == 0) warm_solve(s_tot, nw, s_gam);
+    __syncthreads();
   }
   DF rr[1] = {{0.f, 0.f}};
-  const float gd = float(gam[0]), gc = float(gam[1]);
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) {
       a.p_f[i] = zero4;
@@ -1234,18 +1451,26 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     }
     const float sp = a.r_f[i].w;
     float rf[3];
-    if (a.wd) {
-      // v += gamma_d d + gamma_c c; r -= gamma_d A d + gamma_c A c
-      const float4 d = a.wd[i], c = a.wc[i], ad4 = a.ad[i], ac4 = a.ac[i], r4 = a.r_f[i];
+    if (a.nwarm) {
+      // v += sum_j g_j W_j (exact two-sums); r -= sum_j g_j A W_j
+      const float4 r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
-      df_inc(vh.x, vl.x, gd * d.x + gc * c.x);
-      df_inc(vh.y, vl.y, gd * d.y + gc * c.y);
-      df_inc(vh.z, vl.z, gd * d.z + gc * c.z);
+      rf[0] = r4.x;
+      rf[1] = r4.y;
+      rf[2] = r4.z;
+      for (int j = 0; j < a.nwarm; ++j) {
+        const float g = float(s_gam[j]);
+        if (g == 0.f) continue;
+        const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
+        df_inc(vh.x, vl.x, g * w.x);
+        df_inc(vh.y, vl.y, g * w.y);
+        df_inc(vh.z, vl.z, g * w.z);
+        rf[0] -= g * aw.x;
+        rf[1] -= g * aw.y;
+        rf[2] -= g * aw.z;
+      }
       a.v_f[i] = vh;
       a.v_lo[i] = vl;
-      rf[0] = r4.x - (gd * ad4.x + gc * ac4.x);
-      rf[1] = r4.y - (gd * ad4.y + gc * ac4.y);
-      rf[2] = r4.z - (gd * ad4.z + gc * ac4.z);
     } else {
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
       const double d = a.diag[i];
@@ -1384,19 +1609,20 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
 
   // v back to FP64 (the kept best iterate when stopped at the floor);
   // position_update (fem_position_update.h:25-39); the velocity change is
-  // kept for the learned warm start
+  // kept for the warm starts
   for (long i = gtid; i < N; i += gstride) {
     if (a.fixed[i]) continue;
     const long kb = 2L * best_buf * N;
     float4 vh = stalled ? a.v_keep[kb + i] : a.v_f[i], vl = stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
     double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
-    float dv[3];
+    double dv[3];
     for (int c = 0; c < 3; ++c) {
-      dv[c] = float(v3[c] - a.v[3 * i + c]);
+      dv[c] = v3[c] - a.v[3 * i + c];
       a.v[3 * i + c] = v3[c];
       a.x[3 * i + c] += v3[c] * a.dt;
     }
-    a.dv_last[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
+    a.dv_last[i] = make_float4(float(dv[0]), float(dv[1]), float(dv[2]), 0.f);
+    if (a.hist) record_velocity_change(a, i, dv);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
 }
@@ -2188,8 +2414,11 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
     for (int a = 0; a < 3; ++a) f[k + 1][a] = S[a][0] * b[3 * k] + S[a][1] * b[3 * k + 1] + S[a][2] * b[3 * k + 2];
 #pragma unroll
   for (int a = 0; a < 3; ++a) f[0][a] = -(f[1][a] + f[2][a] + f[3][a]);
+  // w of the four entries: the tet's quaternion (x, y, z, w), read by the
+  // network inputs (one 64-byte line per tet instead of four tile words)
+  const float qv[4] = {quat.x, quat.y, quat.z, quat.w};
 #pragma unroll
-  for (int k = 0; k < 4; ++k) g_f[4L * t + k] = make_float4(f[k][0], f[k][1], f[k][2], 0.f);
+  for (int k = 0; k < 4; ++k) g_f[4L * t + k] = make_float4(f[k][0], f[k][1], f[k][2], qv[k]);
 }
 
 __global__ void k_identity_f32(int T, float* re_f, float* tile_f, int tile_tets) {
@@ -2524,10 +2753,12 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
     k_orient_rhs<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.E, c.V, c.Bv, c.D, c.Re,
                                            c.re_f, c.re_d, c.elastic_force, c.tile_f, c.tile_tets);
     c.re_f32_pending = false;
+    c.quat_in_g_f = false;
   } else {
     k_orient_rhs_f32<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.b_f, c.c_f, c.re_f,
                                                c.g_f, c.tile_f, c.tile_tets);
     c.re_f32_pending = true;
+    c.quat_in_g_f = true;
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // add_plasticity_force (fem_simulate.h:102) runs between the assembly and
@@ -2646,14 +2877,26 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.tile_tets = c.tile_tets;
   a.num_tiles = c.num_tiles;
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
-  const bool learned = prm.warm_start == OTFEM_WARM_START_LEARNED && c.warm_ops;
+  const bool single = c.num_meshes <= 1;
+  const bool learned =
+      prm.warm_start == OTFEM_WARM_START_LEARNED && (single ? c.warm_hist != nullptr : c.warm_ops != nullptr);
   a.warm_dv = learned ? c.warm_dv : nullptr;
   a.dv_last = c.dv_last;
   a.v_keep = c.v_keep;
-  a.wd = learned ? c.warm_ops : nullptr;
-  a.wc = learned ? c.warm_ops + c.N : nullptr;
-  a.ad = learned ? c.warm_ops + 2L * c.N : nullptr;
-  a.ac = learned ? c.warm_ops + 3L * c.N : nullptr;
+  const bool batch_learned = learned && !single;
+  a.wd = batch_learned ? c.warm_ops : nullptr;
+  a.wc = batch_learned ? c.warm_ops + c.N : nullptr;
+  a.ad = batch_learned ? c.warm_ops + 2L * c.N : nullptr;
+  a.ac = batch_learned ? c.warm_ops + 3L * c.N : nullptr;
+  a.hist = single ? c.warm_hist : nullptr;
+  a.wprod = c.warm_prod;
+  a.wpart = c.warm_part;
+  a.hist_k = 0;
+  if (a.hist && prm.warm_start == OTFEM_WARM_START_PROJECTED) a.hist_k = prm.warm_history;
+  if (a.hist && learned) a.hist_k = std::max(prm.warm_history, 1);
+  a.nwarm = a.hist_k + (a.hist && learned ? 1 : 0);
+  // a step records the levels it searches (all of them when it searches none)
+  a.hist_rec = a.hist ? (a.hist_k > 0 ? a.hist_k : kMaxHistory) : 0;
   a.num_meshes = c.num_meshes;
   a.mesh_of_node = c.mesh_of_node;
   a.mesh_of_tet = c.mesh_of_tet;

@@ -225,7 +225,10 @@ struct FeatureArgs {
   const double* fext;
   const int* inc_ptr;
   const int* inc_ent;
-  const float* re_f;       // 9 x T (SoA)
+  const float* re_f;       // 9 x T (SoA); used when tile_f is null
+  const float* tile_f;     // the tets' rotations as quaternions (tile words 4..7), or null
+  int tile_tets;
+  const float4* quat_g;    // or the quaternions in the w of the mixed force entries (g_f), or null
   float* features;         // N x kFeatureStride or null
   float4* warm_dv;         // null: features only
   const __nv_bfloat16* packed;
@@ -259,8 +262,22 @@ __global__ void __launch_bounds__(32 * kFeatWarps) k_node_features(FeatureArgs a
     const int q0 = a.inc_ptr[i], q1 = a.inc_ptr[i + 1];
     for (int q = q0; q < q1; ++q) {
       const int t = a.inc_ent[q] >> 2;
+      if (a.quat_g || a.tile_f) {
+        // the tet's rotation from its quaternion (the FP32 rotation of the
+        // matrix-free solvers is rebuilt the same way)
+        const float4 qt =
+            a.quat_g ? make_float4(a.quat_g[4L * t].w, a.quat_g[4L * t + 1].w, a.quat_g[4L * t + 2].w,
+                                   a.quat_g[4L * t + 3].w)
+                     : make_float4(a.tile_f[tile_word(a.tile_tets, t, 4)], a.tile_f[tile_word(a.tile_tets, t, 5)],
+                                   a.tile_f[tile_word(a.tile_tets, t, 6)], a.tile_f[tile_word(a.tile_tets, t, 7)]);
+        float R[9];
+        quaternion_to_rotation(qt, R);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) f[9 + k] += a.re_f[long(k) * a.T + t];
+        for (int k = 0; k < 9; ++k) f[9 + k] += R[k];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) f[9 + k] += a.re_f[long(k) * a.T + t];
+      }
     }
     if (q1 > q0) {
       const float inv = 1.f / float(q1 - q0);
@@ -758,6 +775,9 @@ cudaError_t launch_node_features(Context& c, bool predict) {
   a.inc_ptr = c.inc_ptr;
   a.inc_ent = c.inc_ent;
   a.re_f = c.re_f;
+  a.tile_f = c.tile_f;
+  a.tile_tets = c.tile_tets;
+  a.quat_g = c.quat_in_g_f ? c.g_f : nullptr;
   a.features = c.collect ? c.features : nullptr;
   a.warm_dv = predict ? c.warm_dv : nullptr;
   a.packed = predict ? c.mlp->packed : nullptr;

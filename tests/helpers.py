@@ -170,3 +170,29 @@ def run_oracle(po, tets, coord, fixed, steps, material=MATERIAL, dt=0.01, warp=T
             it, rr = 20, None
         out.append((m.get(po.COORD), m.get(po.VELOCITY), it, rr))
     return m, out
+
+
+def tip_load(coord, I, J, K, amp, freq, direction, t):
+    """A sinusoidal load spread over the free end face of an I x J x K beam."""
+    n = coord.shape[0]
+    tip = np.arange(n) >= I * (J + 1) * (K + 1)
+    f = np.zeros((n, 3))
+    f[tip] = amp * np.sin(2 * np.pi * freq * t) * np.asarray(direction) / tip.sum()
+    return f
+
+
+def run_loaded(m, dims, steps, params, amp, freq, direction, net=None, dt=0.01):
+    """Gravity plus a tip load; returns the iteration counts and positions per step."""
+    I, J, K = dims
+    mass = m.get(capi.MASS)
+    its, xs = [], []
+    for s in range(steps):
+        f = gravity_force(mass, m.fixed) + tip_load(m.coord, I, J, K, amp, freq, direction, s * dt)
+        m.set(capi.F_EXTERNAL, f)
+        _, st = m.step(dt, True, params)
+        assert st.rel_residual <= 1e-6
+        its.append(st.iterations)
+        xs.append(m.get(capi.COORD))
+        if net is not None:
+            net.add_samples(m.h)
+    return np.array(its), xs

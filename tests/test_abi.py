@@ -45,6 +45,7 @@ def test_abi_version_and_defaults(lib):
     assert p.mass_damping == 2.0 and p.min_iterations == 20 and p.max_iterations == 20
     assert p.rtol == 1e-6 and p.refresh_period == 16 and p.graph == 1
     assert p.preconditioner == capi.PRECONDITIONER_JACOBI
+    assert p.warm_history == 4 and capi.MAX_WARM_HISTORY == 8
 
 
 def _create(lib, tets, coord):

@@ -6,7 +6,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from helpers import GpuMesh, beam, gravity_force
+from helpers import GpuMesh, beam, gravity_force, run_loaded
 from oracle import mlp_oracle as mo
 from opentissue_gb300 import capi
 
@@ -188,30 +188,6 @@ def test_learned_start_needs_a_network(gpu):
 
 
 # ---- the warm start in the solver ---------------------------------------------
-
-
-def tip_load(coord, I, J, K, amp, freq, direction, t):
-    n = coord.shape[0]
-    tip = np.arange(n) >= I * (J + 1) * (K + 1)
-    f = np.zeros((n, 3))
-    f[tip] = amp * np.sin(2 * np.pi * freq * t) * np.asarray(direction) / tip.sum()
-    return f
-
-
-def run_loaded(m, dims, steps, params, amp, freq, direction, net=None, dt=0.01):
-    I, J, K = dims
-    mass = m.get(capi.MASS)
-    its, xs = [], []
-    for s in range(steps):
-        f = gravity_force(mass, m.fixed) + tip_load(m.coord, I, J, K, amp, freq, direction, s * dt)
-        m.set(capi.F_EXTERNAL, f)
-        _, st = m.step(dt, True, params)
-        assert st.rel_residual <= 1e-6
-        its.append(st.iterations)
-        xs.append(m.get(capi.COORD))
-        if net is not None:
-            net.add_samples(m.h)
-    return np.array(its), xs
 
 
 @pytest.mark.gpu

@@ -1,0 +1,102 @@
+"""Projected start (OTFEM_WARM_START_PROJECTED): CG starts from the least-energy
+point of v + span{the last warm_history velocity changes}.  It changes where
+CG starts, not where it stops: every step still ends at rel. residual 1e-6,
+so the positions match the plain start's to that tolerance."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import GpuMesh, beam, run_loaded
+from opentissue_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (24, 6, 6)
+LOAD = (75.0, 2.2, (0.0, -0.8, -0.6))
+
+
+def params(**kw):
+    base = dict(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6)
+    base.update(kw)
+    return capi.default_params(**base)
+
+
+def run(p, steps=40, variant=None):
+    tets, coord, fixed = beam(*DIMS, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    if variant is not None:
+        capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
+    its, xs = run_loaded(m, DIMS, steps, p, *LOAD)
+    m.close()
+    return its, xs, coord
+
+
+def same_positions(xs, ref, coord, tol=1e-5):
+    for s, (a, b) in enumerate(zip(xs, ref)):
+        disp = np.abs(b - coord).max()
+        assert np.abs(a - b).max() <= tol * disp, s
+
+
+def test_projected_start_same_answer_fewer_iterations(gpu):
+    its0, x0, coord = run(params())
+    its2, x2, _ = run(params(warm_start=capi.WARM_START_PROJECTED, warm_history=2))
+    its8, x8, _ = run(params(warm_start=capi.WARM_START_PROJECTED, warm_history=8))
+    same_positions(x2, x0, coord)
+    same_positions(x8, x0, coord)
+    # once the history has filled, each further vector cuts iterations
+    plain, two, eight = its0[10:].mean(), its2[10:].mean(), its8[10:].mean()
+    assert two < 0.85 * plain, (plain, two)
+    assert eight < 0.5 * plain, (plain, eight)
+    assert eight < two
+
+
+@pytest.mark.parametrize("variant", range(capi.NUM_APPLY_VARIANTS))
+def test_projected_start_every_apply_variant(gpu, variant):
+    """The tets and staged variants apply A to all directions in one pass,
+    the patch variants once per direction: all give the same start."""
+    its0, x0, coord = run(params(), steps=16, variant=variant)
+    its, x, _ = run(params(warm_start=capi.WARM_START_PROJECTED), steps=16, variant=variant)
+    same_positions(x, x0, coord)
+    assert its[10:].mean() < 0.7 * its0[10:].mean(), (variant, its0, its)
+
+
+def test_projected_start_with_ordered_sums(gpu):
+    """sequential_dots = 1: the Gram system is summed in CTA order."""
+    its0, x0, coord = run(params(sequential_dots=1), steps=16)
+    its, x, _ = run(params(sequential_dots=1, warm_start=capi.WARM_START_PROJECTED), steps=16)
+    same_positions(x, x0, coord)
+    assert its[10:].mean() < 0.7 * its0[10:].mean()
+
+
+def test_history_restarts_at_init(gpu):
+    """otfem_init clears the history: the first projected step after it
+    starts from v, like the plain start."""
+    tets, coord, fixed = beam(*DIMS, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    p = params(warm_start=capi.WARM_START_PROJECTED)
+    run_loaded(m, DIMS, 12, p, *LOAD)
+    m.init()
+    m.set(capi.COORD, coord)
+    m.set(capi.VELOCITY, np.zeros_like(coord))
+    its_a, _ = run_loaded(m, DIMS, 1, p, *LOAD)
+    m.close()
+    its_b, _, _ = run(params(), steps=1)
+    assert abs(int(its_a[0]) - int(its_b[0])) <= 1, (its_a, its_b)
+
+
+def test_projected_start_parameter_checks(gpu):
+    tets, coord, fixed = beam(3, 2, 2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    rc, _ = m.step(0.01, True, params(warm_start=capi.WARM_START_PROJECTED, warm_history=0), check=False)
+    assert rc == capi.ERR_INVALID_ARGUMENT
+    rc, _ = m.step(0.01, True, params(warm_start=capi.WARM_START_PROJECTED, warm_history=9), check=False)
+    assert rc == capi.ERR_INVALID_ARGUMENT
+    rc, _ = m.step(0.01, True, params(solver=capi.SOLVER_FP64, warm_start=capi.WARM_START_PROJECTED), check=False)
+    assert rc == capi.ERR_UNSUPPORTED
+    rc, _ = m.step(0.01, True, params(warm_start=3), check=False)
+    assert rc == capi.ERR_INVALID_ARGUMENT
+    m.close()
