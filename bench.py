@@ -50,11 +50,13 @@ WORKLOADS = {
 }
 WORKLOAD = WORKLOADS["beam128"]
 METRIC = "tet-steps/sec at rel. residual 1e-6: learned warm-start vs plain CG, 1 GB300"
-# algorithmic bytes of one element-apply sweep: per tet 4 int32 connectivity,
-# Re 9 fp32, B 9 fp32, V*D 3 fp32 = 100 B; per free node read p 12 B, write
-# A p 12 B, diagonal 4 B = 28 B.  Per CG iteration the FP64 vectors add
-# 5 x 24 B per free node.
-BYTES_PER_TET_APPLY = 100
+# algorithmic bytes of one element-apply sweep: per tet the 20 words of its
+# tile (4 int32 connectivity, rotation quaternion 4 fp32, B 9 fp32, V*D 3
+# fp32) = 80 B for the tets and staged variants (the patch variants read Re
+# as 9 fp32: 100 B); per free node read p 12 B, write A p 12 B, diagonal
+# 4 B = 28 B.  Per CG iteration the node phases read p, q, r (fp32), the
+# (hi, lo) velocity and the diagonal and write them back: 120 B per free node.
+BYTES_PER_TET_APPLY = {0: 100, 1: 100, 2: 80, 3: 80}
 BYTES_PER_NODE_APPLY = 28
 BYTES_PER_NODE_ITER = 120
 L2_FLUSH_BYTES = 512 << 20
@@ -496,6 +498,9 @@ def run_ours(args, world, rank, local):
     # ---- roofline: the persistent CG kernel timed on its own ---------------
     cg_ms, cg_bytes, cg_applies = [], [], []
     stats = capi.StepStats()
+    variant = ctypes.c_int32()
+    capi.check(lib.otfem_tuning(h_plain, ctypes.byref(variant), None))
+    tet_bytes = BYTES_PER_TET_APPLY[int(variant.value)]
     for k in range(max(3, min(args.steps, 10))):
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         flush_l2()
@@ -507,7 +512,7 @@ def run_ours(args, world, rank, local):
         capi.check(lib.otfem_last_stats(h_plain, ctypes.byref(stats)))
         cg_ms.append(e1.elapsed_time(e2))
         cg_applies.append(stats.applies)
-        cg_bytes.append(stats.applies * (BYTES_PER_TET_APPLY * T + BYTES_PER_NODE_APPLY * n_free)
+        cg_bytes.append(stats.applies * (tet_bytes * T + BYTES_PER_NODE_APPLY * n_free)
                         + stats.iterations * BYTES_PER_NODE_ITER * n_free)
     cg_s = np.array(cg_ms) / 1e3
     achieved = float(np.mean(np.array(cg_bytes) / cg_s)) / 1e9
@@ -529,8 +534,6 @@ def run_ours(args, world, rank, local):
         traffic = None
 
     # ---- the element-apply sweep alone (the stiffness apply) ----------------
-    variant = ctypes.c_int32()
-    capi.check(lib.otfem_tuning(h_plain, ctypes.byref(variant), None))
     sweep_ms = []
     for k in range(10):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -540,7 +543,7 @@ def run_ours(args, world, rank, local):
         e1.record(stream)
         torch.cuda.synchronize()
         sweep_ms.append(e0.elapsed_time(e1))
-    sweep_bytes = BYTES_PER_TET_APPLY * T + BYTES_PER_NODE_APPLY * n_free
+    sweep_bytes = tet_bytes * T + BYTES_PER_NODE_APPLY * n_free
     sweep_gbs = sweep_bytes / (float(np.median(sweep_ms)) * 1e-3) / 1e9
 
     # ---- end to end through the C ABI with host buffers (learned) ----------

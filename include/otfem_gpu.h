@@ -319,12 +319,17 @@ OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt
  * state unspecified until the next step. */
 OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t sweeps);
 /* Convergence history of the last matrix-free step, one row of 10 doubles per
- * CG iteration (at most 256 rows): the squared residual norm before the
- * iteration, p.Ap, alpha, beta, then six GPU-timer stamps in ns since the
- * kernel started (taken by the first CTA): apply sweep done, its barrier
- * passed, reduction phase done, reduction complete, update phase done,
- * update reduction complete. */
+ * CG iteration (at most 256 rows): the squared residual norm (its estimate)
+ * before the iteration, p.Ap (0 where the solver does not form it), alpha,
+ * beta, then six stamps in SM clock cycles since the kernel started (taken by
+ * the first CTA): apply sweep done, its barrier passed, reduction phase done,
+ * reduction complete, update phase done, update synchronised. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
+/* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 5 stamps in SM
+ * clock cycles since the kernel started (first CTA): b and |b| done, the
+ * initial residual's element sweeps (and the search directions') done, the
+ * start ready (projection solved), CG loop done, position update done. */
+OTFEM_API int otfem_solver_phases(otfem_handle h, double* out);
 /* The element-apply variant the autotuner chose for this mesh at otfem_init
  * (0: patches with shared-memory atomics, 1: patches with a deterministic
  * per-node gather, 2: one tet per thread with global reductions, 3: as 2 with

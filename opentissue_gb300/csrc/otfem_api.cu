@@ -305,7 +305,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.p_d4, N);
   OT_ALLOC(c.v_d4, N);
   OT_ALLOC(c.sync, 1);
-  OT_ALLOC(c.trace, size_t(otfem::kTraceCols) * otfem::kTraceRows);
+  OT_ALLOC(c.trace, size_t(otfem::kTraceCols) * (otfem::kTraceRows + 1));  // + the phase stamps
   OT_ALLOC(c.stats, 1);
   if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
@@ -810,6 +810,15 @@ int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* r
   if (n > 0)
     OT_CUDA(cudaMemcpy(out, c.trace, sizeof(double) * otfem::kTraceCols * size_t(n), cudaMemcpyDeviceToHost));
   *rows = n;
+  return OTFEM_OK;
+}
+
+int otfem_solver_phases(otfem_handle h, double* out) {
+  if (!h || !out) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  OT_CUDA(cudaMemcpy(out, c.trace + size_t(otfem::kTraceCols) * otfem::kTraceRows, sizeof(double) * 5,
+                     cudaMemcpyDeviceToHost));
   return OTFEM_OK;
 }
 

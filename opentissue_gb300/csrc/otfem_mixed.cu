@@ -1077,6 +1077,19 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
   });
 }
 
+// Tets variant in FP32: one tet per thread, grid-stride, its words read
+// straight from the tiles (node ids, quaternion, B-vectors, constants: 80 B).
+__device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                                 const unsigned char* mask) {
+  const int T = a.T, TT = a.tile_tets;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+    if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
+    const int tile = t / TT;
+    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
+  }
+}
+
 // Search direction j of the projected start: basis vector j of the
 // velocity-change history, then the network's correction.
 __device__ __forceinline__ const float4* warm_dir(const MixedArgs& a, int j) {
@@ -1093,19 +1106,12 @@ __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char
   });
 }
 __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
-  const int T = a.T;
+  const int T = a.T, TT = a.tile_tets;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
-    const int4 n = a.tets[t];
-    const int nn[4] = {n.x, n.y, n.z, n.w};
-    float Re[9], b[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      Re[k] = a.re_f[(long)k * T + t];
-      b[k] = a.b_f[(long)k * T + t];
-    }
-    const float c0 = a.c_f[t], c1 = a.c_f[T + t], c2 = a.c_f[2L * T + t];
+    const int tile = t / TT;
+    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     for (int j = 0; j < a.nwarm; ++j)
-      tet_apply(Re, b, c0, c1, c2, scale, nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
+      tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
   }
 }
 
@@ -1120,6 +1126,10 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
   if constexpr (sizeof(R) == 4) {
     if (a.apply_variant == kApplyStaged) {
       apply_staged(a, u4, ulo, q4, scale, smem, mask);
+      return;
+    }
+    if (a.apply_variant == kApplyTets || mask) {
+      apply_tets_tiled(a, u4, ulo, q4, scale, mask);
       return;
     }
   }
@@ -1314,6 +1324,12 @@ __device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long 
   }
 }
 
+// Phase stamps of the last mixed solve (first CTA; SM clock cycles since the
+// kernel started), after the trace rows.
+__device__ __forceinline__ void phase_stamp(const MixedArgs& a, int k, long long t_start) {
+  a.trace[kTraceCols * kTraceRows + k] = double(cycles_now() - t_start);
+}
+
 __device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int applies, bool converged, double rho,
                                              double rho0, double bnorm2) {
   int st = ld_status(&a.sync->status);
@@ -1388,6 +1404,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   }
   double tot[1];
   if (!grid_reduce<DF, 1, 1>(a, bbsum, tot, round, FinIdentity1())) return;
+  if (tracer) phase_stamp(a, 0, t_start);
   const double bnorm2 = tot[0];
   const double thresh = a.rtol * a.rtol * bnorm2;
 
@@ -1403,6 +1420,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     applies += a.nwarm;
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  if (tracer) phase_stamp(a, 1, t_start);
   __shared__ double s_gam[kMaxWarmDirs];
   if (a.nwarm) {
     const int nw = a.nwarm;
@@ -1486,6 +1504,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     rr[0] = df_add(rr[0], DF{rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2], 0.f});
   }
   if (!grid_reduce<DF, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
+  if (tracer) phase_stamp(a, 2, t_start);
   double rho = tot[0];
   const double rho0 = rho;
   int it = 0;
@@ -1607,6 +1626,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     converged = rho <= thresh;
   }
 
+  if (tracer) phase_stamp(a, 3, t_start);
   // v back to FP64 (the kept best iterate when stopped at the floor);
   // position_update (fem_position_update.h:25-39); the velocity change is
   // kept for the warm starts
@@ -1624,6 +1644,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     a.dv_last[i] = make_float4(float(dv[0]), float(dv[1]), float(dv[2]), 0.f);
     if (a.hist) record_velocity_change(a, i, dv);
   }
+  if (tracer) phase_stamp(a, 4, t_start);
   if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
 }
 
@@ -2975,7 +2996,10 @@ cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps, b
   otfem_default_params(&prm);
   fill_args(a, c, dt, prm);
   if (masked && c.num_meshes > 1) a.sweep_mask = c.bmask;
-  if (cudaError_t e = reset_tile_tickets(c)) return e;
+  // tile tickets matter to the staged variant only (the measured launches
+  // are then the sweeps alone)
+  if (c.apply_variant == kApplyStaged)
+    if (cudaError_t e = reset_tile_tickets(c)) return e;
   for (int k = 0; k < sweeps; ++k) {
     if (solver == OTFEM_SOLVER_FP64)
       k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
