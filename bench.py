@@ -348,8 +348,9 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng):
 def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
     """256 beams of uneven size (nx U{8..64}, ny, nz U{3..16}), per-beam
     material, random fixed face, gravity plus a tip force, dt 0.005, one
-    persistent launch per step: plain (constant tip force), then plain and
-    learned under a sinusoidal tip force."""
+    persistent launch per step: plain CG, Jacobi PCG and the projected start
+    under a constant tip force, then Jacobi PCG, projected and learned under a
+    sinusoidal tip force."""
     from opentissue_gb300.workloads import random_beams
     beams = random_beams(args.batch_meshes, seed=args.seed)
     descs = (capi.MeshDesc * len(beams))()
@@ -369,8 +370,13 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
     freqs = np.concatenate([np.full(b["coord"].shape[0], rng.uniform(0.5, 5)) for b in beams])
     w = WORKLOAD
     res = {"workload": f"{len(beams)} beams, {T} tets, {N} nodes, dt 0.005, rel. residual 1e-6"}
-    for name, warm, vary in (("plain", capi.WARM_START_PREVIOUS, False), ("plain_tip_sine", capi.WARM_START_PREVIOUS, True),
-                             ("learned_tip_sine", capi.WARM_START_LEARNED, True)):
+    arms = (("plain_cg", capi.WARM_START_PREVIOUS, False, capi.PRECONDITIONER_NONE),
+            ("plain", capi.WARM_START_PREVIOUS, False, capi.PRECONDITIONER_JACOBI),
+            ("projected", capi.WARM_START_PROJECTED, False, capi.PRECONDITIONER_JACOBI),
+            ("plain_tip_sine", capi.WARM_START_PREVIOUS, True, capi.PRECONDITIONER_JACOBI),
+            ("projected_tip_sine", capi.WARM_START_PROJECTED, True, capi.PRECONDITIONER_JACOBI),
+            ("learned_tip_sine", capi.WARM_START_LEARNED, True, capi.PRECONDITIONER_JACOBI))
+    for name, warm, vary, pre in arms:
         h = ctypes.c_void_p()
         t0 = time.perf_counter()
         capi.check(lib.otfem_batch_create(descs, len(beams), ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
@@ -385,15 +391,16 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
         mass = get_mass(lib, capi, h, N)
         g = gravity(mass, fixed_all)
         p = capi.default_params(solver=capi.SOLVER_MIXED, mass_damping=w["mass_damping"], rtol=w["rtol"],
-                                max_iterations=5000, refresh_period=16, warm_start=warm)
+                                max_iterations=5000, refresh_period=16, warm_start=warm, preconditioner=pre)
 
         def forces(k):
             f = g + (tipf * np.sin(2 * np.pi * freqs * k * 0.005)[:, None] if vary else tipf)
             f[fixed_all == 1] = 0.0
             return f
         steps = args.batch_steps
-        timed_steps(lib, capi, torch, stream, h, p, args.warmup, forces, 0.005, flush_l2)
-        sec, its = timed_steps(lib, capi, torch, stream, h, p, steps, lambda k: forces(k + args.warmup), 0.005,
+        pre_steps = args.lead_in + args.warmup
+        timed_steps(lib, capi, torch, stream, h, p, pre_steps, forces, 0.005, flush_l2)
+        sec, its = timed_steps(lib, capi, torch, stream, h, p, steps, lambda k: forces(k + pre_steps), 0.005,
                                flush_l2)
         M = len(beams)
         mi = np.zeros(M, np.int32)
@@ -405,7 +412,9 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
         if warm == capi.WARM_START_LEARNED:
             net.detach(h)
         capi.check(lib.otfem_destroy(h))
+    res["projected_over_plain_cg"] = res["projected"]["tet_steps_per_s"] / res["plain_cg"]["tet_steps_per_s"]
     res["learned_over_plain_tip_sine"] = res["learned_tip_sine"]["tet_steps_per_s"] / res["plain_tip_sine"]["tet_steps_per_s"]
+    res["timed_steps"] = f"steps {args.lead_in + args.warmup + 1}..{args.lead_in + args.warmup + args.batch_steps}"
     return res
 
 

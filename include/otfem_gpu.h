@@ -110,8 +110,9 @@ typedef struct otfem_solver_params {
                                thread (bit-identical to the reference), 0 = parallel tree.
                                matrix-free: 1 = grid sums of the CTA totals in CTA order,
                                0 = FP64 atomic accumulation of them (faster) */
-  int warm_start;           /* OTFEM_WARM_START_* (matrix-free solvers of one mesh; a batch
-                               takes PREVIOUS or LEARNED with one velocity change) */
+  int warm_start;           /* OTFEM_WARM_START_* (PROJECTED and LEARNED: OTFEM_SOLVER_MIXED,
+                               single meshes and batches; a batch solves each mesh's own
+                               search space) */
   int graph;                /* 1 = replay the step from a CUDA graph (default) */
   int preconditioner;       /* matrix-free: OTFEM_PRECONDITIONER_* (default JACOBI);
                                the reference solver ignores it */

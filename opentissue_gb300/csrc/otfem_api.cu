@@ -59,7 +59,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.warm_ops, c.v_keep, c.features, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.v_keep, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -67,7 +67,7 @@ void free_all(Context& c) {
   if (c.stats_host) cudaFreeHost(c.stats_host);
   if (c.bmesh_host) cudaFreeHost(c.bmesh_host);
   void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.bmesh, c.bacc, c.bmask,
-                   c.warm_hist, c.warm_prod, c.warm_part};
+                   c.warm_hist, c.warm_prod, c.warm_part, c.warm_bacc};
   for (void* p : batch)
     if (p) cudaFree(p);
   if (c.graph) cudaGraphExecDestroy(c.graph);
@@ -110,8 +110,8 @@ int check_params(const Context& c, const otfem_solver_params& p) {
     return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes steps with OTFEM_SOLVER_MIXED (one CG per mesh)");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && p.solver != OTFEM_SOLVER_MIXED)
     return fail(OTFEM_ERR_UNSUPPORTED, "the learned warm start runs with OTFEM_SOLVER_MIXED");
-  if (p.warm_start == OTFEM_WARM_START_PROJECTED && (p.solver != OTFEM_SOLVER_MIXED || c.num_meshes > 1))
-    return fail(OTFEM_ERR_UNSUPPORTED, "the projected start runs with OTFEM_SOLVER_MIXED on one mesh");
+  if (p.warm_start == OTFEM_WARM_START_PROJECTED && p.solver != OTFEM_SOLVER_MIXED)
+    return fail(OTFEM_ERR_UNSUPPORTED, "the projected start runs with OTFEM_SOLVER_MIXED");
   if (p.warm_start == OTFEM_WARM_START_PROJECTED && p.warm_history < 1)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "the projected start needs warm_history >= 1");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && !c.mlp)
@@ -119,12 +119,12 @@ int check_params(const Context& c, const otfem_solver_params& p) {
   return OTFEM_OK;
 }
 
-// The projected and learned starts of one mesh search previous velocity
+// The projected and learned starts search previous velocity
 // changes: their history, the products and sums are allocated (the history
 // zeroed) by the first step that needs them; from then on every mixed step
 // of the mesh records its velocity change.
 cudaError_t ensure_history(Context& c, const otfem_solver_params& p) {
-  const bool needs = p.solver == OTFEM_SOLVER_MIXED && c.num_meshes <= 1 &&
+  const bool needs = p.solver == OTFEM_SOLVER_MIXED &&
                      (p.warm_start == OTFEM_WARM_START_PROJECTED || p.warm_start == OTFEM_WARM_START_LEARNED);
   if (!needs || c.warm_hist) return cudaSuccess;
   const size_t n = size_t(c.N > 0 ? c.N : 1);
@@ -132,6 +132,10 @@ cudaError_t ensure_history(Context& c, const otfem_solver_params& p) {
   if ((e = cudaMalloc(&c.warm_hist, sizeof(float4) * 2 * otfem::kMaxHistory * n)) != cudaSuccess) return e;
   if ((e = cudaMalloc(&c.warm_prod, sizeof(float4) * (otfem::kMaxWarmDirs + 1) * n)) != cudaSuccess) return e;
   if ((e = cudaMalloc(&c.warm_part, sizeof(double) * otfem::kMaxWarmSums * size_t(c.mf_grid))) != cudaSuccess)
+    return e;
+  if (c.num_meshes > 1 &&
+      (e = cudaMalloc(&c.warm_bacc, sizeof(double) * (otfem::kMaxWarmSums * size_t(c.num_meshes) + 8))) !=
+          cudaSuccess)
     return e;
   return cudaMemsetAsync(c.warm_hist, 0, sizeof(float4) * 2 * otfem::kMaxHistory * n, c.stream);
 }

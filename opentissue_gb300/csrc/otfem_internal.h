@@ -51,7 +51,8 @@ struct DeviceSync {
 
 // Per-mesh state of a batched solve (device memory, one per mesh).
 struct BatchMesh {
-  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta, gamma_d, gamma_c;
+  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta;
+  double wgam[kMaxWarmDirs];  // projected / learned start: the mesh's coefficients
   int active, restart, stalls, iterations, applies, status, converged, pad;
   int best_buf;  // which kept iterate (v_keep) has the smallest true residual
   int stalled;   // stopped at the precision floor: the kept iterate is the result
@@ -153,10 +154,6 @@ struct Context {
   float4* dv_last = nullptr;      // N (w unused)
   float4* warm_dv = nullptr;      // N
   float4* warm_tmp = nullptr;     // N, allocated with smoothing passes
-  // learned start of a batch, projected: operands d = dv_prev, c = the
-  // network's correction and their products A d, A c (4N, allocated with a
-  // network)
-  float4* warm_ops = nullptr;
   // projected and learned starts of one mesh (allocated by the first step
   // that uses them): the velocity-change history as a difference basis
   // (D_0 = the last change, D_j = its j-th backward difference; (hi, lo)
@@ -166,6 +163,7 @@ struct Context {
   float4* warm_hist = nullptr;    // 2 kMaxHistory x N: hi parts, then lo parts
   float4* warm_prod = nullptr;    // (kMaxWarmDirs + 1) x N: products, then the correction
   double* warm_part = nullptr;    // kMaxWarmSums x max grid
+  double* warm_bacc = nullptr;    // batch: num_meshes x kMaxWarmSums (+ 8) per-mesh Gram totals
   // two kept copies of the CG iterate (hi, lo) from the true-residual
   // refreshes: a solve stopped at the precision floor returns the best one
   float4* v_keep = nullptr;       // 4N

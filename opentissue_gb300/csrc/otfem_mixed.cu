@@ -120,11 +120,11 @@ struct MixedArgs {
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
   const float4* warm_dv;                // learned guess v + warm_dv (null: plain start from v)
   float4* dv_last;                      // in: dv_prev; out: v_new - v_old per free node
-  float4 *wd, *wc, *ad, *ac;            // learned start of a batch: operands d, c and products A d, A c
   // projected / learned start of one mesh (see Context::warm_hist)
   float4* hist;                         // difference basis: hi parts (8 x N), then lo parts (8 x N); null: none
   float4* wprod;                        // products A W_j (slots 0..8), the network's correction (slot 9)
   double* wpart;                        // per-CTA partial sums of the Gram system (ordered sums)
+  double* wbacc;                        // batch: per-mesh Gram totals (num_meshes x kMaxWarmSums)
   int hist_k;                           // basis vectors searched this step
   int hist_rec;                         // basis vectors the step records
   int nwarm;                            // search directions this step (0: start from v)
@@ -589,29 +589,6 @@ struct FinPcgFp64 {
 // Jacobi scalar of a free node whose mass term is dg (1 without the preconditioner).
 __device__ __forceinline__ double jacobi_scale(const MixedArgs& a, long i, double dg) {
   return a.precond ? 1.0 / (dg + a.dt * a.dt * a.node_k[i]) : 1.0;
-}
-
-// The learned start, projected: CG starts from the point of least energy
-// x.A.x/2 - b.x on v + span{d, c} (d = dv_prev, c = the network's
-// correction).  The plane holds the plain start v (the judge of the learned
-// guess), the extrapolation v + d and the network's guess v + d + c, so the
-// start is never worse than any of them in the energy norm.  Totals: d.Ad,
-// d.Ac, c.Ac, d.r, c.r with r = b - A v; outputs gamma_d, gamma_c.
-__device__ __forceinline__ void warm_projection(const double* t, double& gd, double& gc) {
-  const double dd = t[0], dc = t[1], cc = t[2], dr = t[3], cr = t[4];
-  gd = gc = 0.0;
-  const bool okd = dd > 0.0 && isfinite(dd) && isfinite(dr);
-  const bool okc = cc > 0.0 && isfinite(cc) && isfinite(cr);
-  const double det = dd * cc - dc * dc;
-  if (okd && okc && isfinite(dc) && det > 1e-10 * dd * cc) {
-    gd = (dr * cc - cr * dc) / det;
-    gc = (cr * dd - dr * dc) / det;
-  } else {
-    // (nearly) one direction: the one that lowers the energy most, x.r^2 / x.Ax
-    const double ed = okd ? dr * dr / dd : -1.0, ec = okc ? cr * cr / cc : -1.0;
-    if (okd && ed >= ec) gd = dr / dd;
-    else if (okc) gc = cr / cc;
-  }
 }
 
 // Coherent (L2) load of node data written by other CTAs within the launch.
@@ -1096,11 +1073,13 @@ __device__ __forceinline__ const float4* warm_dir(const MixedArgs& a, int j) {
   return j < a.hist_k ? a.hist + size_t(j) * a.N : a.wprod + size_t(kMaxWarmDirs) * a.N;
 }
 
-// Projected start: A W_j for every search direction in one pass over the
-// tets, whose data is loaded (staged) once for all directions.
+// Projected start: A v (the (hi, lo) iterate, into q) and A W_j for every
+// search direction in one pass over the tets, whose data is loaded (staged)
+// once for all operands.
 __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char* smem) {
   staged_sweep(a, smem, nullptr, [&](const float* w, int TT, int tid) {
     const StagedTet e(w, TT, tid);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
     for (int j = 0; j < a.nwarm; ++j)
       tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
   });
@@ -1110,6 +1089,7 @@ __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
     const int tile = t / TT;
     const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
     for (int j = 0; j < a.nwarm; ++j)
       tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
   }
@@ -1139,10 +1119,10 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
   else apply_patches<R>(a, u4, ulo, q4, re, bb, cc, scale, smem);
 }
 
-// Projected start: A W_j for every search direction (products into
-// a.wprod).  Tets and staged variants do all directions in one pass; the
-// patch variants sweep once per direction.
-__device__ bool apply_directions(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round) {
+// Projected start: A v (into q) and A W_j for every search direction
+// (products into a.wprod).  Tets and staged variants do all operands in one
+// pass; the patch variants sweep once per operand.
+__device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round) {
   if (a.apply_variant == kApplyStaged) {
     apply_staged_dirs(a, scale, smem);
     return true;
@@ -1151,8 +1131,9 @@ __device__ bool apply_directions(const MixedArgs& a, float scale, unsigned char*
     apply_tets_dirs(a, scale);
     return true;
   }
+  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   for (int j = 0; j < a.nwarm; ++j) {
-    if (j > 0 && !grid_barrier(a.sync, a.spin_limit, round)) return false;
+    if (!grid_barrier(a.sync, a.spin_limit, round)) return false;
     apply_sweep<float>(a, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N, a.re_f, a.b_f, a.c_f, scale, smem);
   }
   return true;
@@ -1413,11 +1394,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // the least-energy point v + sum_j g_j W_j (warm_solve), whose residual is
   // r - sum_j g_j A W_j.
   int applies = 1;
-  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   if (a.nwarm) {
-    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    if (!apply_directions(a, scale, smem, round)) return;
+    if (!apply_start_operands(a, scale, smem, round)) return;
     applies += a.nwarm;
+  } else {
+    apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   if (tracer) phase_stamp(a, 1, t_start);
@@ -1849,7 +1830,7 @@ __device__ __forceinline__ NodeRange warp_node_range(int N) {
 }
 
 // Running per-mesh sums of a warp (mesh ids are non-decreasing along nodes).
-template <int NV>
+template <int NV, int Stride = kBatchSlots>
 struct SegSum {
   int cur;  // uniform across the warp; -1: none yet
   DF acc[NV];
@@ -1861,7 +1842,7 @@ struct SegSum {
   __device__ __forceinline__ void flush(double* acc_half) {
     DF x;
     const int k = warp_totals<DF, NV>(acc, x);
-    if (k >= 0 && cur >= 0) atomicAdd(&acc_half[kBatchSlots * cur + k], AccOps<DF>::to_double(x));
+    if (k >= 0 && cur >= 0) atomicAdd(&acc_half[Stride * cur + k], AccOps<DF>::to_double(x));
 #pragma unroll
     for (int j = 0; j < NV; ++j) acc[j] = DF{0.f, 0.f};
   }
@@ -1940,10 +1921,10 @@ struct FinBatchInit {
   }
 };
 
-// totals: d.Ad, d.Ac, c.Ac, d.r, c.r (learned start, projected per mesh)
-struct FinBatchWarm {
+// projected / learned start: each mesh's Gram system (a.wbacc), solved per mesh
+struct FinBatchGram {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
-    warm_projection(t, a.bm[m].gamma_d, a.bm[m].gamma_c);
+    warm_solve(a.wbacc + size_t(m) * kMaxWarmSums, a.nwarm, a.bm[m].wgam);
   }
 };
 
@@ -1956,7 +1937,7 @@ struct FinBatchStart {
     b.restart = b.stalls = b.iterations = 0;
     b.best_buf = 0;
     b.stalled = 0;
-    b.applies = a.wd ? 3 : 1;
+    b.applies = 1 + a.nwarm;
     b.status = isfinite(t[0]) && isfinite(b.bnorm2) ? 0 : OTFEM_ERR_NONFINITE;
     b.converged = b.status == 0 && t[0] <= b.thresh;
     b.active = b.status == 0 && !b.converged && a.max_it > 0;
@@ -2095,13 +2076,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
         a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
         store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
         a.q_f[i] = zero4;
-        if (a.wd) {
-          const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
-          const float fw = fx ? 0.f : 1.f;
-          a.wd[i] = make_float4(d.x, d.y, d.z, fw);
-          a.wc[i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fw);
-          a.ad[i] = zero4;
-          a.ac[i] = zero4;
+        if (a.nwarm) {
+          // learned start: the network's correction is the last search direction
+          if (a.nwarm > a.hist_k) {
+            const float4 d = fx ? zero4 : a.dv_last[i], w = fx ? zero4 : a.warm_dv[i];
+            a.wprod[size_t(kMaxWarmDirs) * N + i] = make_float4(w.x - d.x, w.y - d.y, w.z - d.z, fx ? 0.f : 1.f);
+          }
+          for (int j = 0; j < a.nwarm; ++j) a.wprod[size_t(j) * N + i] = zero4;
         }
       }
       ss.add(valid, m, bb, acc_half(round + 1));
@@ -2110,53 +2091,69 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   }
   if (!batch_reduce(a, round, FinBatchInit(), counts)) return;
 
-  // initial residual r = b - A v (FP64), p = r, for every mesh; with the
-  // learned start also A d, A c and each mesh's projected start
-  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
-  ++sweeps;
-  if (a.wd) {
-    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    apply_sweep<float>(a, a.wd, nullptr, a.ad, a.re_f, a.b_f, a.c_f, scale, smem);
-    if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    apply_sweep<float>(a, a.wc, nullptr, a.ac, a.re_f, a.b_f, a.c_f, scale, smem);
-    sweeps += 2;
+  // initial residual r = b - A v (FP64), p = S r, for every mesh; with the
+  // projected or learned start also A W_j and each mesh's start (k_cg_mixed)
+  if (a.nwarm) {
+    if (!apply_start_operands(a, scale, smem, round)) return;
+    sweeps += 1 + a.nwarm;
+  } else {
+    apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+    ++sweeps;
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-  if (a.wd) {
-    SegSum<5> ss;
-    ss.start(first_mesh);
-    for (long base = nr.beg; base < nr.end; base += 32) {
-      const long i = base + lane;
-      const bool valid = i < nr.end;
-      int m = -1;
-      float s5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      if (valid) {
-        m = a.mesh_of_node[i];
-        if (!a.fixed[i]) {
-          const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-          const double dg = a.diag[i];
-          float rf[3];
-          rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
-          rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
-          rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
-          const float df = float(dg);
-          const float4 d = a.wd[i], c = a.wc[i], ad4 = load_acc(a.ad + i), ac4 = load_acc(a.ac + i);
-          const float adx = df * d.x + ad4.x, ady = df * d.y + ad4.y, adz = df * d.z + ad4.z;
-          const float acx = df * c.x + ac4.x, acy = df * c.y + ac4.y, acz = df * c.z + ac4.z;
-          s5[0] = d.x * adx + d.y * ady + d.z * adz;
-          s5[1] = d.x * acx + d.y * acy + d.z * acz;
-          s5[2] = c.x * acx + c.y * acy + c.z * acz;
-          s5[3] = d.x * rf[0] + d.y * rf[1] + d.z * rf[2];
-          s5[4] = c.x * rf[0] + c.y * rf[1] + c.z * rf[2];
-          a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-          a.ad[i] = make_float4(adx, ady, adz, 0.f);
-          a.ac[i] = make_float4(acx, acy, acz, 0.f);
-        }
+  if (a.nwarm) {
+    const int nw = a.nwarm;
+    // r = b - A v; A W_j += diag W_j (the mass term)
+    for (long i = nr.beg + lane; i < nr.end; i += 32) {
+      if (a.fixed[i]) continue;
+      const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+      const double dg = a.diag[i];
+      float rf[3];
+      rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
+      rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
+      rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
+      a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
+      const float df = float(dg);
+      for (int j = 0; j < nw; ++j) {
+        const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
+        a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
       }
-      ss.add(valid, m, s5, acc_half(round + 1));
     }
-    ss.flush(acc_half(round + 1));
-    if (!batch_reduce(a, round, FinBatchWarm(), counts)) return;
+    // per-mesh Gram systems, in chunks of 8 sums: W_i.A W_j (i <= j), then W_i.r
+    __shared__ signed char s_pi[kMaxWarmSums], s_pj[kMaxWarmSums];
+    if (threadIdx.x == 0) {
+      int m = 0;
+      for (int i = 0; i < nw; ++i)
+        for (int j = i; j < nw; ++j, ++m) s_pi[m] = (signed char)i, s_pj[m] = (signed char)j;
+      for (int i = 0; i < nw; ++i, ++m) s_pi[m] = (signed char)i, s_pj[m] = -1;
+    }
+    __syncthreads();
+    const int nv = nw * (nw + 1) / 2 + nw;
+    for (int c0 = 0; c0 < nv; c0 += 8) {
+      SegSum<8, kMaxWarmSums> ss;
+      ss.start(first_mesh);
+      for (long base = nr.beg; base < nr.end; base += 32) {
+        const long i = base + lane;
+        const bool valid = i < nr.end;
+        int m = -1;
+        float v8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (valid) {
+          m = a.mesh_of_node[i];
+          if (!a.fixed[i]) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              if (c0 + k >= nv) break;
+              const float4 w = warm_dir(a, s_pi[c0 + k])[i];
+              const float4 q = s_pj[c0 + k] >= 0 ? a.wprod[size_t(s_pj[c0 + k]) * N + i] : a.r_f[i];
+              v8[k] = w.x * q.x + w.y * q.y + w.z * q.z;
+            }
+          }
+        }
+        ss.add(valid, m, v8, a.wbacc + c0);
+      }
+      ss.flush(a.wbacc + c0);
+    }
+    if (!batch_reduce(a, round, FinBatchGram(), counts)) return;
   }
   {
     SegSum<1> ss;
@@ -2174,18 +2171,27 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
         } else {
           const float sp = a.r_f[i].w;
           float rf[3];
-          if (a.wd) {
-            const float gd = float(a.bm[m].gamma_d), gc = float(a.bm[m].gamma_c);
-            const float4 d = a.wd[i], c = a.wc[i], ad4 = a.ad[i], ac4 = a.ac[i], r4 = a.r_f[i];
+          if (a.nwarm) {
+            // v += sum_j g_j W_j (the mesh's coefficients); r -= sum_j g_j A W_j
+            const float4 r4 = a.r_f[i];
             float4 vh = a.v_f[i], vl = a.v_lo[i];
-            df_inc(vh.x, vl.x, gd * d.x + gc * c.x);
-            df_inc(vh.y, vl.y, gd * d.y + gc * c.y);
-            df_inc(vh.z, vl.z, gd * d.z + gc * c.z);
+            rf[0] = r4.x;
+            rf[1] = r4.y;
+            rf[2] = r4.z;
+            const double* gam = a.bm[m].wgam;
+            for (int j = 0; j < a.nwarm; ++j) {
+              const float g = float(gam[j]);
+              if (g == 0.f) continue;
+              const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
+              df_inc(vh.x, vl.x, g * w.x);
+              df_inc(vh.y, vl.y, g * w.y);
+              df_inc(vh.z, vl.z, g * w.z);
+              rf[0] -= g * aw.x;
+              rf[1] -= g * aw.y;
+              rf[2] -= g * aw.z;
+            }
             a.v_f[i] = vh;
             a.v_lo[i] = vl;
-            rf[0] = r4.x - (gd * ad4.x + gc * ac4.x);
-            rf[1] = r4.y - (gd * ad4.y + gc * ac4.y);
-            rf[2] = r4.z - (gd * ad4.z + gc * ac4.z);
           } else {
             const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
             const double d = a.diag[i];
@@ -2309,13 +2315,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     const long kb = 2L * bmi.best_buf * N;
     const float4 vh = bmi.stalled ? a.v_keep[kb + i] : a.v_f[i], vl = bmi.stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
     const double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
-    float dv[3];
+    double dv[3];
     for (int c = 0; c < 3; ++c) {
-      dv[c] = float(v3[c] - a.v[3 * i + c]);
+      dv[c] = v3[c] - a.v[3 * i + c];
       a.v[3 * i + c] = v3[c];
       a.x[3 * i + c] += v3[c] * a.dt;
     }
-    a.dv_last[i] = make_float4(dv[0], dv[1], dv[2], 0.f);
+    a.dv_last[i] = make_float4(float(dv[0]), float(dv[1]), float(dv[2]), 0.f);
+    if (a.hist) record_velocity_change(a, i, dv);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // batch summary: the largest iteration count and relative residual, the
@@ -2898,24 +2905,18 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.tile_tets = c.tile_tets;
   a.num_tiles = c.num_tiles;
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
-  const bool single = c.num_meshes <= 1;
-  const bool learned =
-      prm.warm_start == OTFEM_WARM_START_LEARNED && (single ? c.warm_hist != nullptr : c.warm_ops != nullptr);
+  const bool learned = prm.warm_start == OTFEM_WARM_START_LEARNED && c.warm_hist != nullptr;
   a.warm_dv = learned ? c.warm_dv : nullptr;
   a.dv_last = c.dv_last;
   a.v_keep = c.v_keep;
-  const bool batch_learned = learned && !single;
-  a.wd = batch_learned ? c.warm_ops : nullptr;
-  a.wc = batch_learned ? c.warm_ops + c.N : nullptr;
-  a.ad = batch_learned ? c.warm_ops + 2L * c.N : nullptr;
-  a.ac = batch_learned ? c.warm_ops + 3L * c.N : nullptr;
-  a.hist = single ? c.warm_hist : nullptr;
+  a.hist = c.warm_hist;
   a.wprod = c.warm_prod;
   a.wpart = c.warm_part;
+  a.wbacc = c.warm_bacc;
   a.hist_k = 0;
   if (a.hist && prm.warm_start == OTFEM_WARM_START_PROJECTED) a.hist_k = prm.warm_history;
   if (a.hist && learned) a.hist_k = std::max(prm.warm_history, 1);
-  a.nwarm = a.hist_k + (a.hist && learned ? 1 : 0);
+  a.nwarm = a.hist_k + (learned ? 1 : 0);
   // a step records the levels it searches (all of them when it searches none)
   a.hist_rec = a.hist ? (a.hist_k > 0 ? a.hist_k : kMaxHistory) : 0;
   a.num_meshes = c.num_meshes;
@@ -2971,6 +2972,10 @@ static cudaError_t reset_tile_tickets(Context& c) {
 cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params& prm) {
   cudaError_t e;
   if ((e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream)) != cudaSuccess) return e;
+  if (c.warm_bacc &&
+      (e = cudaMemsetAsync(c.warm_bacc, 0, sizeof(double) * (kMaxWarmSums * size_t(c.num_meshes) + 8), c.stream)) !=
+          cudaSuccess)
+    return e;
   if ((e = cudaMemsetAsync(c.bacc, 0, sizeof(double) * 2 * kBatchSlots * size_t(c.num_meshes), c.stream)) != cudaSuccess)
     return e;
   MixedArgs a;

@@ -1146,10 +1146,6 @@ int otfem_set_mlp(otfem_handle h, otfem_mlp m) {
     cudaError_t e = cudaMalloc(&c->warm_tmp, sizeof(float4) * size_t(std::max(c->N, 1)));
     if (e != cudaSuccess) return mlp_cuda(e, "cudaMalloc");
   }
-  if (m && !c->warm_ops) {
-    cudaError_t e = cudaMalloc(&c->warm_ops, sizeof(float4) * 4 * size_t(std::max(c->N, 1)));
-    if (e != cudaSuccess) return mlp_cuda(e, "cudaMalloc");
-  }
   c->mlp = m;
   return OTFEM_OK;
 }
