@@ -155,12 +155,20 @@ __device__ __forceinline__ void load_a_bf16(const __nv_bfloat16* x, int ld, int 
   }
 }
 
-// GELU, tanh form: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).
+// GELU, tanh form: 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3).
+// With 0.5 (1 + tanh(u)) = 1 / (1 + exp(-2u)) (the logistic function of 2u)
+// it is z s with s = 1 / (1 + exp(-2u)), one exponential and one division;
+// the derivative is s + z s (1 - s) 2 u'.  Large |u| saturate cleanly
+// (exp -> inf gives s = 0, exp -> 0 gives s = 1).
 constexpr float kGeluC = 0.7978845608028654f, kGeluA = 0.044715f;
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + tanhf(kGeluC * (z + kGeluA * z * z * z))); }
+__device__ __forceinline__ float gelu_logistic(float z) {
+  const float u = kGeluC * (z + kGeluA * z * z * z);
+  return __fdividef(1.f, 1.f + __expf(-2.f * u));
+}
+__device__ __forceinline__ float gelu(float z) { return z * gelu_logistic(z); }
 __device__ __forceinline__ float gelu_grad(float z) {
-  const float th = tanhf(kGeluC * (z + kGeluA * z * z * z));
-  return 0.5f * (1.f + th) + 0.5f * z * (1.f - th * th) * kGeluC * (1.f + 3.f * kGeluA * z * z);
+  const float s = gelu_logistic(z);
+  return s + z * s * (1.f - s) * (2.f * kGeluC) * (1.f + 3.f * kGeluA * z * z);
 }
 
 // Bias of columns 8nt+2t..+1 into both rows of the accumulator tile.
@@ -239,7 +247,7 @@ struct FeatureArgs {
 // Network inputs of every node and, with a.warm_dv, the learned initial
 // guess.  8 warps per CTA, 32 nodes per warp (one per lane for the inputs,
 // two 16-row tiles for the network).
-__global__ void __launch_bounds__(32 * kFeatWarps) k_node_features(FeatureArgs a) {
+__global__ void __launch_bounds__(32 * kFeatWarps, 3) k_node_features(FeatureArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16* Wf = reinterpret_cast<__nv_bfloat16*>(smem);
   float* xs_all = reinterpret_cast<float*>(smem + kFwdElems * sizeof(__nv_bfloat16));
@@ -777,7 +785,7 @@ cudaError_t launch_node_features(Context& c, bool predict) {
   a.re_f = c.re_f;
   a.tile_f = c.tile_f;
   a.tile_tets = c.tile_tets;
-  a.quat_g = c.quat_in_g_f ? c.g_f : nullptr;
+  a.quat_g = nullptr;  // the tile words: measured faster than the force entries' w lanes
   a.features = c.collect ? c.features : nullptr;
   a.warm_dv = predict ? c.warm_dv : nullptr;
   a.packed = predict ? c.mlp->packed : nullptr;
