@@ -147,6 +147,7 @@ struct Context {
   // c0..c2), copied to shared memory whole by the bulk-copy engine
   float* tile_f = nullptr;
   int num_tiles = 0, tile_tets = 0;
+  unsigned long long tile_magic = 0;  // tile_magic_of(tile_tets)
   // learned warm start: the velocity change of the last matrix-free step,
   // the network's initial guess for the next, the per-node network inputs
   // of the last step (kept when collecting training samples) and the
@@ -252,10 +253,27 @@ __device__ __forceinline__ void quaternion_to_rotation(float4 q, float* R) {
   R[6] = 2.f * (xz - yw), R[7] = 2.f * (yz + xw), R[8] = 1.f - 2.f * (xx + yy);
 }
 
+// t / tile_tets for 0 <= t < 2^32 and 2 <= tile_tets: the high half of
+// t * magic with magic = floor((2^64 - 1) / tile_tets) + 1 (= ceil(2^64 /
+// tile_tets)), exact because t * (magic - 2^64 / tile_tets) / 2^64 < 2^-32 is
+// below the distance 1 / tile_tets from t / tile_tets to the next integer
+// (division by invariant integers by multiplication, Granlund and
+// Montgomery 1994).
+__device__ __forceinline__ int tile_of(int t, unsigned long long magic) {
+  return int(__umul64hi(static_cast<unsigned long long>(t), magic));
+}
+inline unsigned long long tile_magic_of(int tile_tets) { return ~0ull / static_cast<unsigned>(tile_tets) + 1ull; }
+
 // Word w of tet t in the staged-apply tiles (Context::tile_f).
 __device__ __forceinline__ long tile_word(int tile_tets, int t, int w) {
   const int tile = t / tile_tets;
   return (long(tile) * kTileWords + w) * tile_tets + (t - tile * tile_tets);
+}
+
+// The rotation quaternion (tile words 4..7) of tet t in tile `tile`.
+__device__ __forceinline__ float4 tile_quaternion(const float* tile_f, int tile_tets, int tile, int t) {
+  const float* w = tile_f + (long(tile) * kTileWords + 4) * tile_tets + (t - tile * tile_tets);
+  return make_float4(w[0], w[tile_tets], w[2 * tile_tets], w[3 * tile_tets]);
 }
 
 // Writes m_Re (FP64) from the FP32 orientations of the last mixed step.

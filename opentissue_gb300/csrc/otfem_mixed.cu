@@ -117,6 +117,7 @@ struct MixedArgs {
   int apply_variant;                    // kApplyAtomics / kApplyGather / kApplyTets / kApplyStaged
   const float* tile_f;                  // staged apply tiles (see Context::tile_f)
   int tile_tets, num_tiles;
+  unsigned long long tile_magic;        // tile_of(t, tile_magic) = t / tile_tets
   int ordered_sums;                     // grid sums of the CTA totals in CTA order
   const float4* warm_dv;                // learned guess v + warm_dv (null: plain start from v)
   float4* dv_last;                      // in: dv_prev; out: v_new - v_old per free node
@@ -1061,7 +1062,7 @@ __device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const flo
   const int T = a.T, TT = a.tile_tets;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
     if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
-    const int tile = t / TT;
+    const int tile = tile_of(t, a.tile_magic);
     const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
   }
@@ -1087,7 +1088,7 @@ __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char
 __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
   const int T = a.T, TT = a.tile_tets;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
-    const int tile = t / TT;
+    const int tile = tile_of(t, a.tile_magic);
     const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
     for (int j = 0; j < a.nwarm; ++j)
@@ -2741,6 +2742,7 @@ void staged_tiles(Context& c) {
   long tt = (T + G * rounds - 1) / (G * rounds);
   tt = std::min<long>(kTileMaxTets, std::max(16L, (tt + 15) / 16 * 16));
   c.tile_tets = int(tt);
+  c.tile_magic = tile_magic_of(c.tile_tets);
   c.num_tiles = int((T + tt - 1) / tt);
 }
 
@@ -2904,6 +2906,7 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.tile_f = c.tile_f;
   a.tile_tets = c.tile_tets;
   a.num_tiles = c.num_tiles;
+  a.tile_magic = c.tile_magic;
   a.ordered_sums = prm.sequential_dots ? 1 : 0;
   const bool learned = prm.warm_start == OTFEM_WARM_START_LEARNED && c.warm_hist != nullptr;
   a.warm_dv = learned ? c.warm_dv : nullptr;

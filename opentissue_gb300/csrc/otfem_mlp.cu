@@ -236,6 +236,7 @@ struct FeatureArgs {
   const float* re_f;       // 9 x T (SoA); used when tile_f is null
   const float* tile_f;     // the tets' rotations as quaternions (tile words 4..7), or null
   int tile_tets;
+  unsigned long long tile_magic;
   const float4* quat_g;    // or the quaternions in the w of the mixed force entries (g_f), or null
   float* features;         // N x kFeatureStride or null
   float4* warm_dv;         // null: features only
@@ -276,8 +277,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps, 3) k_node_features(FeatureArg
         const float4 qt =
             a.quat_g ? make_float4(a.quat_g[4L * t].w, a.quat_g[4L * t + 1].w, a.quat_g[4L * t + 2].w,
                                    a.quat_g[4L * t + 3].w)
-                     : make_float4(a.tile_f[tile_word(a.tile_tets, t, 4)], a.tile_f[tile_word(a.tile_tets, t, 5)],
-                                   a.tile_f[tile_word(a.tile_tets, t, 6)], a.tile_f[tile_word(a.tile_tets, t, 7)]);
+                     : tile_quaternion(a.tile_f, a.tile_tets, tile_of(t, a.tile_magic), t);
         float R[9];
         quaternion_to_rotation(qt, R);
 #pragma unroll
@@ -785,6 +785,7 @@ cudaError_t launch_node_features(Context& c, bool predict) {
   a.re_f = c.re_f;
   a.tile_f = c.tile_f;
   a.tile_tets = c.tile_tets;
+  a.tile_magic = c.tile_magic;
   a.quat_g = nullptr;  // the tile words: measured faster than the force entries' w lanes
   a.features = c.collect ? c.features : nullptr;
   a.warm_dv = predict ? c.warm_dv : nullptr;
