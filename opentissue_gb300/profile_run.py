@@ -31,6 +31,9 @@ def main():
     ap.add_argument("--sweeps", type=int, default=4)
     ap.add_argument("--variant", type=int, default=-1, help="force an element-apply variant (0..3)")
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--warm-start", default="previous", choices=["previous", "projected"])
+    ap.add_argument("--trace", action="store_true",
+                    help="print the last step's phases and per-iteration breakdown (SM clock stamps)")
     args = ap.parse_args()
     build.build()
     lib = capi.lib()
@@ -56,16 +59,50 @@ def main():
     f[fixed == 0, 1] = -9.81 * mass[fixed == 0]
     capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
     solver = capi.SOLVER_MIXED if args.solver == "mixed" else capi.SOLVER_FP64
-    p = capi.default_params(solver=solver, max_iterations=5000, rtol=1e-6, graph=0)
+    warm = capi.WARM_START_PROJECTED if args.warm_start == "projected" else capi.WARM_START_PREVIOUS
+    p = capi.default_params(solver=solver, max_iterations=5000, rtol=1e-6, graph=0, warm_start=warm)
     st = capi.StepStats()
     for _ in range(args.steps):
         capi.check(lib.otfem_simulate_ex(h, 0.01, 1, ctypes.byref(p), ctypes.byref(st)))
         print(f"step: iterations {st.iterations}, applies {st.applies}, rel. residual {st.rel_residual:.3e}")
+    if args.trace:
+        trace_report(lib, h, dp)
     if args.sweeps:
         capi.check(lib.otfem_apply_sweeps(h, solver, 0.01, args.sweeps))
     capi.check(lib.otfem_synchronize(h))
     print(f"tets {T}, nodes {N}, apply variant {variant.value}, sweep ms per variant {ms.tolist()}")
     capi.check(lib.otfem_destroy(h))
+
+
+def trace_report(lib, h, dp):
+    """Phases of the last solve and the median of each part of a CG
+    iteration, from the SM clock stamps of the first CTA (microseconds at
+    the SM clock the GPU reports as its maximum)."""
+    import subprocess
+    try:
+        mhz = float(subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i", "0"],
+                                   capture_output=True, text=True, timeout=20).stdout.split()[0])
+    except (OSError, ValueError, IndexError, subprocess.SubprocessError):
+        mhz = 2070.0
+    ph = np.zeros(5)
+    capi.check(lib.otfem_solver_phases(h, ph.ctypes.data_as(dp)))
+    names = ["b and |b|", "initial residual and direction sweeps", "start (projection solved)", "CG loop",
+             "position update"]
+    for n, v in zip(names, np.diff(np.concatenate([[0.0], ph]))):
+        print(f"phase {n}: {v / mhz:.1f} us")
+    tr = np.zeros((256, 10))
+    rows = ctypes.c_int32()
+    capi.check(lib.otfem_solver_trace(h, tr.ctypes.data_as(dp), 256, ctypes.byref(rows)))
+    tr = tr[:rows.value]
+    if rows.value > 2:
+        prev = tr[:-1, 9]
+        cur = tr[1:]
+        parts = np.stack([cur[:, 4] - prev, cur[:, 5] - cur[:, 4], cur[:, 6] - cur[:, 5], cur[:, 7] - cur[:, 6],
+                          cur[:, 8] - cur[:, 7], cur[:, 9] - cur[:, 8]], 1) / mhz
+        med = np.median(parts, 0)
+        labels = ["apply sweep", "barrier", "dot products", "grid sum", "vector update", "barrier"]
+        print("iteration (median us): " + ", ".join(f"{l} {v:.2f}" for l, v in zip(labels, med)) +
+              f"; total {med.sum():.1f}")
 
 
 if __name__ == "__main__":
