@@ -87,6 +87,50 @@ def test_history_restarts_at_init(gpu):
     assert abs(int(its_a[0]) - int(its_b[0])) <= 1, (its_a, its_b)
 
 
+def test_projected_start_is_the_least_energy_point(gpu):
+    """The kernel's start (its reported initial residual) is the FP64
+    least-energy point of v + span{the last 4 velocity changes}, rebuilt on
+    the host from the step's velocities, b and the library's own operator."""
+    from helpers import gravity_force, tip_load
+    tets, coord, fixed = beam(*DIMS, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    mass = m.get(capi.MASS)
+    free = np.repeat(fixed == 0, 3)
+    p = params(warm_start=capi.WARM_START_PROJECTED, warm_history=4)
+    _dp = ctypes.POINTER(ctypes.c_double)
+
+    def apply(x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        capi.check(m.lib.otfem_apply_operator(m.h, capi.SOLVER_MIXED, 0.01, 2.0, x.ctypes.data_as(_dp),
+                                              y.ctypes.data_as(_dp)))
+        return y.reshape(-1)[free]
+
+    vs = [m.get(capi.VELOCITY)]
+    checked = 0
+    for s in range(12):
+        f = gravity_force(mass, fixed) + tip_load(coord, *DIMS, LOAD[0], LOAD[1], LOAD[2], s * 0.01)
+        m.set(capi.F_EXTERNAL, f)
+        _, st = m.step(0.01, True, p)
+        vs.append(m.get(capi.VELOCITY))
+        if s < 6:
+            continue
+        v = vs[-2]
+        W = [vs[-2 - j] - vs[-3 - j] for j in range(4)]  # the changes of the four steps before
+        b = m.get(capi.B).reshape(-1)[free]
+        r_v = b - apply(v)
+        AW = np.stack([apply(w) for w in W], 1)
+        Wf = np.stack([w.reshape(-1)[free] for w in W], 1)
+        g = np.linalg.lstsq(Wf.T @ AW, Wf.T @ r_v, rcond=None)[0]
+        rel = np.linalg.norm(r_v - AW @ g) / np.linalg.norm(b)
+        assert np.linalg.norm(r_v) / np.linalg.norm(b) > 3 * rel  # the projection matters here
+        assert abs(st.initial_rel_residual - rel) <= 0.02 * rel, (s, st.initial_rel_residual, rel)
+        checked += 1
+    assert checked == 6
+    m.close()
+
+
 def test_projected_start_parameter_checks(gpu):
     tets, coord, fixed = beam(3, 2, 2)
     m = GpuMesh(tets, coord, fixed)
