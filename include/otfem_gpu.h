@@ -329,7 +329,8 @@ OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, 
 /* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 5 stamps in SM
  * clock cycles since the kernel started (first CTA): b and |b| done, the
  * initial residual's element sweeps (and the search directions') done, the
- * start ready (projection solved), CG loop done, position update done. */
+ * start ready (projection solved), CG loop done, position update done.
+ * A batch records the same five stamps for its persistent launch. */
 OTFEM_API int otfem_solver_phases(otfem_handle h, double* out);
 /* The element-apply variant the autotuner chose for this mesh at otfem_init
  * (0: patches with shared-memory atomics, 1: patches with a deterministic

@@ -59,6 +59,7 @@ constexpr int kApplyGather = 1;   // patches, per-node gather over patch-local i
 constexpr int kApplyTets = 2;     // grid-stride over tets, global vector reductions
 constexpr int kApplyStaged = 3;   // tiles of tets staged in shared memory by bulk copies, global reductions
 constexpr int kApplyVariants = kNumApplyVariants;
+static_assert(kTileMaxTets <= 512, "a tile's tets fit one CTA (one tet per thread)");
 // Staged apply: two tile buffers and their two mbarriers.
 constexpr size_t kStageBytes = size_t(kTileMaxTets) * kTileWords * sizeof(float);
 constexpr size_t kStagedSmem = 2 * kStageBytes + 2 * sizeof(unsigned long long);
@@ -944,6 +945,26 @@ __device__ __forceinline__ int claim_tile(const MixedArgs& a) {
 // bandwidth take more tiles.  On a copy that does not complete within
 // spin_limit cycles the CTA sets OTFEM_ERR_TIMEOUT, stops, and waits (again
 // bounded) for the copies it still has in flight before returning.
+// Batched solve: whether any mesh with tets in `tile` is in the sweep
+// (meshes own contiguous tet ranges, so the tile's first and last tets bound
+// them).
+__device__ __forceinline__ bool tile_in_sweep(const MixedArgs& a, int tile, const unsigned char* mask) {
+  const int first = tile * a.tile_tets;
+  const int last = min(a.T, first + a.tile_tets) - 1;
+  for (int m = a.mesh_of_tet[first]; m <= a.mesh_of_tet[last]; ++m)
+    if (mask[m]) return true;
+  return false;
+}
+
+// The next tile of this sweep whose meshes take part (every tile is drawn
+// exactly once; -1: none left).
+__device__ __forceinline__ int claim_sweep_tile(const MixedArgs& a, const unsigned char* mask) {
+  for (;;) {
+    const int tile = claim_tile(a);
+    if (tile < 0 || !mask || tile_in_sweep(a, tile, mask)) return tile;
+  }
+}
+
 template <typename Body>
 __device__ void staged_sweep(const MixedArgs& a, unsigned char* smem, const unsigned char* mask, Body body) {
   const int TT = a.tile_tets;
@@ -960,7 +981,7 @@ __device__ void staged_sweep(const MixedArgs& a, unsigned char* smem, const unsi
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     int more = 1;
     for (int sb = 0; sb < 2; ++sb) {
-      const int tile = more ? claim_tile(a) : -1;
+      const int tile = more ? claim_sweep_tile(a, mask) : -1;
       if (tile < 0) more = 0;
       s_tile[sb] = tile;
       if (tile >= 0) {
@@ -986,7 +1007,7 @@ __device__ void staged_sweep(const MixedArgs& a, unsigned char* smem, const unsi
       break;
     }
     if (tid == 0) {
-      const int next = s_more ? claim_tile(a) : -1;
+      const int next = s_more ? claim_sweep_tile(a, mask) : -1;
       if (next < 0) s_more = 0;
       s_tile[sb] = next;
       if (next >= 0) {
@@ -2037,6 +2058,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   int counts[4];
   int sweeps = 0;
   auto acc_half = [&](unsigned next_round) { return a.bacc + size_t(next_round & 1u) * M * kBatchSlots; };
+  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const long long t_start = tracer ? cycles_now() : 0ll;
 
   // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess), q = 0
   {
@@ -2091,6 +2114,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     ss.flush(acc_half(round + 1));
   }
   if (!batch_reduce(a, round, FinBatchInit(), counts)) return;
+  if (tracer) phase_stamp(a, 0, t_start);
 
   // initial residual r = b - A v (FP64), p = S r, for every mesh; with the
   // projected or learned start also A W_j and each mesh's start (k_cg_mixed)
@@ -2102,6 +2126,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     ++sweeps;
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+  if (tracer) phase_stamp(a, 1, t_start);
   if (a.nwarm) {
     const int nw = a.nwarm;
     // r = b - A v; A W_j += diag W_j (the mass term)
@@ -2213,6 +2238,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     ss.flush(acc_half(round + 1));
   }
   if (!batch_reduce(a, round, FinBatchStart(), counts)) return;
+  if (tracer) phase_stamp(a, 2, t_start);
   int n_active = counts[0];
 
   for (int it = 0; n_active > 0 && it < a.max_it; ++it) {
@@ -2308,6 +2334,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     }
   }
 
+  if (tracer) phase_stamp(a, 3, t_start);
   // v back to FP64 (a mesh stopped at the floor takes its kept best
   // iterate); position update; velocity change (all meshes)
   for (long i = nr.beg + lane; i < nr.end; i += 32) {
@@ -2326,6 +2353,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     if (a.hist) record_velocity_change(a, i, dv);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    phase_stamp(a, 4, t_start);
     // batch summary: the largest iteration count and relative residual, the
     // worst status
     int its = 0, st = ld_status(&a.sync->status), warn = 0;
