@@ -55,6 +55,61 @@ def generate_blocks(I, J, K, block_width, block_height, block_depth):
     return tets, coord
 
 
+def tetgen_read(basename):
+    """t4mesh::tetgen_read (t4mesh_tetgen_read.h:30-136): a TetGen mesh from
+    `basename`.node and `basename`.ele.
+
+    .node: first line `<#points> <dimension 3> <#attributes> <boundary markers 0/1>`,
+    then `<point id> <x> <y> <z> [attributes] [marker]`.  .ele: first line
+    `<#tets> <points per tet 4> <#attributes (at most 1, the region)>`, then
+    `<tet id> <p0> <p1> <p2> <p3> [attribute]`, the points given by their ids
+    in the .node file (any base).  '#' starts a comment, as in TetGen's
+    files.  Returns (tets int32 [T, 4], coord float64 [N, 3]), nodes in file
+    order; raises ValueError where the reference returns false.
+    """
+    def numbers(path):
+        try:
+            with open(path) as f:
+                return [tok for line in f for tok in line.split('#', 1)[0].split()]
+        except OSError as e:
+            raise ValueError(f"unable to open file '{path}'") from e
+
+    tok = numbers(basename + ".node")
+    n, dim, nattr, has_marker = int(tok[0]), int(tok[1]), int(tok[2]), int(tok[3])
+    if dim != 3:
+        raise ValueError("TetGen .node files of dimension 3 only")
+    width = 4 + nattr + (1 if has_marker else 0)
+    rows = np.array(tok[4:4 + n * width], dtype=np.float64).reshape(n, width)
+    ids = rows[:, 0].astype(np.int64)
+    coord = np.ascontiguousarray(rows[:, 1:4])
+    index = {int(k): i for i, k in enumerate(ids)}
+    tok = numbers(basename + ".ele")
+    t, per, nattr = int(tok[0]), int(tok[1]), int(tok[2])
+    if per != 4:
+        raise ValueError("We only support tetrahedra with 4 points")
+    if nattr > 1:
+        raise ValueError("We only support tetrahedra with 1 region")
+    rows = np.array(tok[3:3 + t * (5 + nattr)], dtype=np.float64).reshape(t, 5 + nattr)
+    try:
+        tets = np.array([[index[int(k)] for k in r[1:5]] for r in rows], dtype=np.int32).reshape(-1, 4)
+    except KeyError as e:
+        raise ValueError(f"tetrahedron refers to an unknown point {e}") from e
+    return tets, coord
+
+
+def tetgen_write(basename, tets, coord):
+    """Writes a mesh as TetGen .node/.ele files (1-based ids), the format
+    tetgen_read reads."""
+    with open(basename + ".node", "w") as f:
+        f.write(f"{len(coord)} 3 0 0\n")
+        for i, (x, y, z) in enumerate(coord):
+            f.write(f"{i + 1} {float(x)!r} {float(y)!r} {float(z)!r}\n")
+    with open(basename + ".ele", "w") as f:
+        f.write(f"{len(tets)} 4 0\n")
+        for i, t in enumerate(tets):
+            f.write(f"{i + 1} {t[0] + 1} {t[1] + 1} {t[2] + 1} {t[3] + 1}\n")
+
+
 class Mesh:
     """fem::Mesh: host node fields plus the device-resident mesh handle."""
 

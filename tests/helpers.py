@@ -196,3 +196,36 @@ def run_loaded(m, dims, steps, params, amp, freq, direction, net=None, dt=0.01):
         if net is not None:
             net.add_samples(m.h)
     return np.array(its), xs
+
+
+def irregular_mesh(shape=(8, 4, 4), h=0.1, jitter=0.35, seed=0):
+    """An unstructured tetrahedral mesh: the Delaunay tetrahedralization of a
+    jittered lattice of (shape + 1) points (spacing h, jitter in units of h),
+    flat tets (volume below 5% of the median) dropped, every tet oriented to
+    a positive volume and unused points removed; the x = min face fixed.
+    Node order and tet order come from the triangulation, so the
+    connectivity has none of the block mesh's regularity."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    I, J, K = shape
+    g = np.stack(np.meshgrid(np.arange(I + 1), np.arange(J + 1), np.arange(K + 1), indexing="ij"), -1).reshape(-1, 3)
+    pts = g.astype(np.float64) * h
+    interior = np.all((g > 0) & (g < np.array([I, J, K])), axis=1)
+    pts[interior] += rng.uniform(-jitter * h, jitter * h, (int(interior.sum()), 3))
+    perm = rng.permutation(len(pts))  # scramble the node numbering
+    pts = pts[perm]
+    tri = Delaunay(pts)
+    tets = tri.simplices.astype(np.int64)
+    e = pts[tets[:, 1:]] - pts[tets[:, :1]]
+    vol = np.einsum("ij,ij->i", e[:, 0], np.cross(e[:, 1], e[:, 2])) / 6.0
+    keep = np.abs(vol) > 0.05 * np.median(np.abs(vol))
+    tets, vol = tets[keep], vol[keep]
+    neg = vol < 0
+    tets[neg, 0], tets[neg, 1] = tets[neg, 1].copy(), tets[neg, 0].copy()
+    used = np.unique(tets)
+    remap = np.full(len(pts), -1, np.int64)
+    remap[used] = np.arange(len(used))
+    tets = remap[tets].astype(np.int32)
+    coord = np.ascontiguousarray(pts[used])
+    fixed = (coord[:, 0] < 1e-9).astype(np.uint8)
+    return tets, coord, fixed
