@@ -348,6 +348,32 @@ OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);
 /* Launch shape of the persistent CG kernel (grid CTAs, threads per CTA). */
 OTFEM_API int otfem_solver_shape(otfem_handle h, int32_t* grid, int32_t* block);
 
+/* ---- mesh coupling (t4mesh::mesh_coupling, t4mesh_mesh_coupling.h) ------
+ * A point set (the vertices of a render surface, say) bound to the tets of a
+ * mesh and moved with them.  The surface refers to its mesh's handle, which
+ * must outlive it; calls run on the mesh's stream. */
+typedef struct otfem_surface_s* otfem_surface;
+/* bind_surface (t4mesh_mesh_coupling.h:129-236): binds each of `count`
+ * points (host, 3 doubles each) to a tet that embeds it in the mesh's current
+ * coordinates, all four barycentric weights in (-1e-4, 1 + 1e-4)
+ * (collision_policy::report, :84-111; weights as geometry_barycentric.h:
+ * 343-385); where several tets embed a point, the lowest tet index.  Points
+ * no tet embeds stay unbound, as in the reference (they keep their given
+ * position in updates).  bound (may be NULL): number of bound points. */
+OTFEM_API int otfem_surface_bind(otfem_handle h, const double* points, int64_t count, otfem_surface* out,
+                                 int64_t* bound);
+/* update_surface (:238-275): every bound point at w0 x_i + w1 x_j + w2 x_k +
+ * w3 x_m of its tet's current node coordinates; host_out: 3 doubles per
+ * point (synchronises); the _device form writes a device array on the mesh's
+ * stream without synchronising. */
+OTFEM_API int otfem_surface_update(otfem_surface s, double* host_out, int64_t count);
+OTFEM_API int otfem_surface_update_device(otfem_surface s, double* device_out, int64_t count);
+/* The binding as bind_surface stores it: tet index per point (-1: unbound)
+ * and its `barycentric` (w1, w2, w3), the weights of the tet's nodes j, k, m
+ * (node i takes 1 - w1 - w2 - w3).  Either output may be NULL. */
+OTFEM_API int otfem_surface_binding(otfem_surface s, int32_t* tet, double* barycentric, int64_t count);
+OTFEM_API int otfem_surface_destroy(otfem_surface s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -202,6 +202,8 @@ struct Context {
 
 // ---- pattern / incidence (otfem_pattern.cu) ------------------------------
 cudaError_t build_incidence(Context& c);
+// Exclusive prefix sum of n counts into out[0..n], out[n] = total.
+cudaError_t prefix_sum_counts(Context& c, long n, const int* in, int* out);
 cudaError_t build_pattern(Context& c);
 
 // ---- reference-order FP64 kernels (otfem_exact.cu) ------------------------

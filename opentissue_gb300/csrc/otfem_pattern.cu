@@ -259,4 +259,8 @@ cudaError_t build_pattern(Context& c) {
   return cudaSuccess;
 }
 
+// Exclusive prefix sum of n counts into out[0..n], out[n] = total (device,
+// on the context's stream).
+cudaError_t prefix_sum_counts(Context& c, long n, const int* in, int* out) { return scan_exclusive(c, n, in, out); }
+
 }  // namespace otfem

@@ -265,3 +265,55 @@ def export_K(mesh):
                     cs.append(3 * j + c)
                     vs.append(vals[q, r, c])
     return np.array(rows, np.int32), np.array(cs, np.int32), np.array(vs)
+
+
+class SurfaceBinding:
+    """t4mesh::mesh_coupling (t4mesh_mesh_coupling.h): points bound to the
+    tets of a mesh that embed them, moved with the deformed tets.  The
+    binding keeps a reference to the mesh, whose handle must outlive it."""
+
+    def __init__(self, mesh, points):
+        self.lib = capi.lib()
+        self.mesh = mesh
+        pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+        self.count = pts.shape[0]
+        self.s = ctypes.c_void_p()
+        bound = ctypes.c_int64()
+        capi.check(self.lib.otfem_surface_bind(mesh.handle, _p(pts, _dp), self.count, ctypes.byref(self.s),
+                                               ctypes.byref(bound)))
+        self.bound = bound.value
+
+    def update(self):
+        """update_surface: the points at their tets' current coordinates."""
+        out = np.zeros((self.count, 3))
+        capi.check(self.lib.otfem_surface_update(self.s, _p(out, _dp), self.count))
+        return out
+
+    def binding(self):
+        """(tet per point, -1 if unbound; barycentric (w1, w2, w3) per point)."""
+        tet = np.zeros(self.count, np.int32)
+        bary = np.zeros((self.count, 3))
+        capi.check(self.lib.otfem_surface_binding(self.s, _p(tet, _i32p), _p(bary, _dp), self.count))
+        return tet, bary
+
+    def close(self):
+        if self.s:
+            self.lib.otfem_surface_destroy(self.s)
+            self.s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def bind_surface(mesh, points):
+    """t4mesh::mesh_coupling::bind_surface (t4mesh_mesh_coupling.h:129-236)
+    against the mesh's current coordinates."""
+    return SurfaceBinding(mesh, points)
+
+
+def update_surface(binding):
+    """t4mesh::mesh_coupling::update_surface (t4mesh_mesh_coupling.h:238-275)."""
+    return binding.update()
