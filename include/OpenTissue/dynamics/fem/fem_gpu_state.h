@@ -32,12 +32,22 @@ inline SolverParams reference_solver() {
   return p;
 }
 
-// Matrix-free solver: FP32 element apply, FP64 CG, stop at ||r|| <= rtol ||b||.
+// Matrix-free solver: FP32 element apply, FP64 CG (Jacobi-preconditioned),
+// stop at ||r|| <= rtol ||b||.
 inline SolverParams mixed_solver(double rtol = 1e-6, int max_iterations = 10000) {
   SolverParams p = reference_solver();
   p.solver = OTFEM_SOLVER_MIXED;
   p.rtol = rtol;
   p.max_iterations = max_iterations;
+  return p;
+}
+
+// The matrix-free solver starting from the least-energy point on the span of
+// the last `history` velocity changes (the same stopping rule).
+inline SolverParams projected_solver(double rtol = 1e-6, int history = 4, int max_iterations = 10000) {
+  SolverParams p = mixed_solver(rtol, max_iterations);
+  p.warm_start = OTFEM_WARM_START_PROJECTED;
+  p.warm_history = history;
   return p;
 }
 

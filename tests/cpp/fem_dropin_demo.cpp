@@ -5,7 +5,7 @@
 // with libotfem_gpu.so; used by tests/test_dropin_cpp.py.
 //
 // usage: fem_dropin_demo I J K steps solver out.bin [export.bin]
-//   solver: reference | sequential | mixed
+//   solver: reference | sequential | mixed | projected
 //   out.bin: per step the N x 3 positions then the N x 3 velocities (doubles)
 //   export.bin: fem::export_K triplets after step 1 (int row, int col, double)
 #include <OpenTissue/configuration.h>
@@ -53,6 +53,7 @@ int main(int argc, char** argv) {
     OpenTissue::fem::SolverParams params = OpenTissue::fem::reference_solver();
     if (std::strcmp(solver, "sequential") == 0) params.sequential_dots = 1;
     if (std::strcmp(solver, "mixed") == 0) params = OpenTissue::fem::mixed_solver(1e-6);
+    if (std::strcmp(solver, "projected") == 0) params = OpenTissue::fem::projected_solver(1e-6, 4);
     FILE* out = std::fopen(argv[6], "wb");
     if (!out) return 3;
     std::vector<double> buf(3 * mesh.size_nodes());

@@ -92,11 +92,12 @@ def test_dropin_cpp_default_and_mixed_solvers(gpu, oracle, tmp_path):
     data = _run_demo(exe, str(tmp_path), (10, 4, 4), 20, "reference")
     disp = np.abs(g["x_10"] - g["coord"]).max()
     assert np.abs(data[9, 0] - g["x_10"]).max() <= 2e-5 * disp
-    data = _run_demo(exe, str(tmp_path), (10, 4, 4), 10, "mixed")
     from helpers import run_oracle
     _, ref = run_oracle(oracle, g["tets"], g["coord"], g["fixed"], 10, converged=True)
     x_ref = ref[-1][0]
-    assert np.abs(data[-1, 0] - x_ref).max() <= 1e-5 * np.abs(x_ref - g["coord"]).max()
+    for solver in ("mixed", "projected"):
+        data = _run_demo(exe, str(tmp_path), (10, 4, 4), 10, solver)
+        assert np.abs(data[-1, 0] - x_ref).max() <= 1e-5 * np.abs(x_ref - g["coord"]).max(), solver
 
 
 @pytest.mark.gpu
