@@ -131,6 +131,34 @@ def test_projected_start_is_the_least_energy_point(gpu):
     m.close()
 
 
+def test_projected_start_with_plasticity_no_warping_and_dt_changes(gpu, oracle):
+    """The projected start stops where the converged FP64 oracle does with
+    plasticity active, with stiffness warping off, and when dt changes
+    between steps (the history then spans changes of other step sizes)."""
+    from helpers import gravity_force
+    tets, coord, fixed = beam(10, 4, 4, jitter_seed=4)
+    mat = (5e5, 0.33, 1000.0, 1e-4, 50.0, 1e-2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init(mat)
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*mat)
+    mass = o.get(oracle.MASS)
+    p = params(warm_start=capi.WARM_START_PROJECTED)
+    schedule = [(0.01, True)] * 6 + [(0.005, True)] * 3 + [(0.01, False)] * 4 + [(0.02, True)] * 3
+    for dt, warp in schedule:
+        f = gravity_force(mass, fixed) * 3.0
+        m.set(capi.F_EXTERNAL, f)
+        o.set(oracle.F_EXTERNAL, f)
+        _, st = m.step(dt, warp, p)
+        o.simulate_converged(dt, warp, 2.0, 1e-11, 100000)
+        assert st.status == capi.OK and st.rel_residual <= 1e-6
+        x, xo = m.get(capi.COORD), o.get(oracle.COORD)
+        assert np.abs(x - xo).max() <= 1e-5 * np.abs(xo - coord).max(), (dt, warp)
+    assert np.abs(m.plastic()).max() > 0
+    o.close()
+    m.close()
+
+
 def test_projected_start_parameter_checks(gpu):
     tets, coord, fixed = beam(3, 2, 2)
     m = GpuMesh(tets, coord, fixed)
