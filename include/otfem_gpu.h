@@ -326,11 +326,13 @@ OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t 
  * the first CTA): apply sweep done, its barrier passed, reduction phase done,
  * reduction complete, update phase done, update synchronised. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
-/* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 5 stamps in SM
+/* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 8 stamps in SM
  * clock cycles since the kernel started (first CTA): b and |b| done, the
  * initial residual's element sweeps (and the search directions') done, the
- * start ready (projection solved), CG loop done, position update done.
- * A batch records the same five stamps for its persistent launch. */
+ * start ready (projection solved), CG loop done, position update done; then,
+ * for the projected and learned starts (else 0), the Gram sums begun, the
+ * Gram totals in, the coefficients solved.  A batch records the first five
+ * stamps for its persistent launch.  out holds 8 doubles. */
 OTFEM_API int otfem_solver_phases(otfem_handle h, double* out);
 /* The element-apply variant the autotuner chose for this mesh at otfem_init
  * (0: patches with shared-memory atomics, 1: patches with a deterministic

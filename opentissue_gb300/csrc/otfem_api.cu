@@ -310,6 +310,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.v_d4, N);
   OT_ALLOC(c.sync, 1);
   OT_ALLOC(c.trace, size_t(otfem::kTraceCols) * (otfem::kTraceRows + 1));  // + the phase stamps
+  cudaMemsetAsync(c.trace, 0, sizeof(double) * otfem::kTraceCols * (otfem::kTraceRows + 1), c.stream);
   OT_ALLOC(c.stats, 1);
   if ((e = cudaMallocHost(reinterpret_cast<void**>(&c.stats_host), sizeof(otfem::DeviceStats))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
@@ -821,7 +822,7 @@ int otfem_solver_phases(otfem_handle h, double* out) {
   if (!h || !out) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   Context& c = h->c;
   OT_CUDA(cudaStreamSynchronize(c.stream));
-  OT_CUDA(cudaMemcpy(out, c.trace + size_t(otfem::kTraceCols) * otfem::kTraceRows, sizeof(double) * 5,
+  OT_CUDA(cudaMemcpy(out, c.trace + size_t(otfem::kTraceCols) * otfem::kTraceRows, sizeof(double) * 8,
                      cudaMemcpyDeviceToHost));
   return OTFEM_OK;
 }

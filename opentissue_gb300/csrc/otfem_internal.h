@@ -46,7 +46,8 @@ struct DeviceSync {
                                  // sets of 8 values, each value on its own 128-byte line
   unsigned tile_ticket;      // staged apply: monotonic tile tickets
   unsigned pad5[31];
-  double wacc[kMaxWarmSums];  // projected start: Gram system totals (FP64 reductions)
+  double wacc[kMaxWarmSums][kAccStride];  // projected start: Gram system totals (FP64
+                                          // reductions), each on its own 128-byte line
 };
 
 // Per-mesh state of a batched solve (device memory, one per mesh).

@@ -84,12 +84,15 @@ def trace_report(lib, h, dp):
                                    capture_output=True, text=True, timeout=20).stdout.split()[0])
     except (OSError, ValueError, IndexError, subprocess.SubprocessError):
         mhz = 2070.0
-    ph = np.zeros(5)
+    ph = np.zeros(8)
     capi.check(lib.otfem_solver_phases(h, ph.ctypes.data_as(dp)))
     names = ["b and |b|", "initial residual and direction sweeps", "start (projection solved)", "CG loop",
              "position update"]
-    for n, v in zip(names, np.diff(np.concatenate([[0.0], ph]))):
+    for n, v in zip(names, np.diff(np.concatenate([[0.0], ph[:5]]))):
         print(f"phase {n}: {v / mhz:.1f} us")
+    if ph[5] > 0:
+        print(f"start detail: node pass {(ph[5] - ph[1]) / mhz:.1f} us, Gram sums {(ph[6] - ph[5]) / mhz:.1f} us, "
+              f"coefficients {(ph[7] - ph[6]) / mhz:.1f} us, moving the start {(ph[2] - ph[7]) / mhz:.1f} us")
     tr = np.zeros((256, 10))
     rows = ctypes.c_int32()
     capi.check(lib.otfem_solver_trace(h, tr.ctypes.data_as(dp), 256, ctypes.byref(rows)))
