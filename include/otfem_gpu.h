@@ -323,11 +323,12 @@ OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t 
  * CG iteration (at most 256 rows): the squared residual norm (its estimate)
  * before the iteration, p.Ap (0 where the solver does not form it), alpha,
  * beta, then six stamps in SM clock cycles since the kernel started (taken by
- * the first CTA): apply sweep done, its barrier passed, reduction phase done,
- * reduction complete, update phase done, update synchronised. */
+ * the middle CTA of the grid): apply sweep done, its barrier passed,
+ * reduction phase done, reduction complete, update phase done, update
+ * synchronised. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 8 stamps in SM
- * clock cycles since the kernel started (first CTA): b and |b| done, the
+ * clock cycles since the kernel started (middle CTA): b and |b| done, the
  * initial residual's element sweeps (and the search directions') done, the
  * start ready (projection solved), CG loop done, position update done; then,
  * for the projected and learned starts (else 0), the Gram sums begun, the

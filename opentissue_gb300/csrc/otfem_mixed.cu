@@ -83,6 +83,7 @@ struct MixedArgs {
   double* r;
   double* p;
   double* diag;
+  float* diag_f;         // the same in FP32 (the mixed loop's vector passes)
   const double* node_k;  // tr(sum_e Ke_ii) / 3 per node (Jacobi preconditioner)
   int precond;           // 1: CG preconditioned by the node scalars 1 / (diag + dt^2 node_k)
   // FP32 apply
@@ -157,8 +158,13 @@ __device__ __forceinline__ int ld_status(const int* p) {
 }
 
 // Stamps of the trace: SM clock cycles (the GPU timer's resolution is far
-// coarser than one CG phase).  All stamps come from the first CTA's SM.
+// coarser than one CG phase).  All stamps come from one CTA's SM (is_tracer).
 __device__ __forceinline__ long long cycles_now() { return clock64(); }
+// The stamping thread: thread 0 of the middle CTA, whose node ranges hold
+// free nodes (a mesh whose fixed nodes come first, the usual numbering of a
+// clamped end, leaves the first CTAs little node work), so the node phases
+// it stamps show a full CTA's work.
+__device__ __forceinline__ bool is_tracer() { return blockIdx.x == gridDim.x / 2 && threadIdx.x == 0; }
 
 __device__ __forceinline__ void red_add(float4* q, float a, float b, float c) {
   asm volatile("red.relaxed.gpu.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(q), "f"(a), "f"(b),
@@ -356,6 +362,23 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
   float h = s + e;
   return DF{h, e - (h - s)};
 }
+// (hi, lo) x b, renormalised (the product's rounding error by an FMA).
+__device__ __forceinline__ DF df_mul(DF a, float b) {
+  const float p = a.hi * b;
+  float e = fmaf(a.hi, b, -p);
+  e = fmaf(a.lo, b, e);
+  const float h = p + e;
+  return DF{h, e - (h - p)};
+}
+// a / b rounded to FP32 (one correction step on the FP32 quotient of the
+// high parts: q + (a - q b) / b, with q b formed exactly by an FMA).
+__device__ __forceinline__ float df_div(DF a, DF b) {
+  const float q = a.hi / b.hi;
+  const float p = q * b.hi;
+  const float e = fmaf(q, b.hi, -p);
+  const float r = (((a.hi - p) - e) + a.lo) - q * b.lo;
+  return q + r / b.hi;
+}
 // (hi, lo) += inc
 __device__ __forceinline__ void df_inc(float& hi, float& lo, float inc) {
   float s, e;
@@ -546,6 +569,113 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
   __syncthreads();
   return good;
 }
+
+// Grid sums of NV per-thread (hi, lo) values for the mixed solver, in a fixed
+// order and without FP64 instructions.  On GB300 every FP64 instruction
+// (arithmetic, conversion or compare) holds the issuing SM sub-partition for
+// ~64 cycles, so the scalar work between two phases stays in FP32 pairs: warp
+// shuffles, the warp totals, one (hi, lo) partial per CTA and value, a grid
+// synchronisation, then every CTA adds up all partials in CTA order by the
+// same tree and every thread evaluates fin(totals, outputs).  The sums are
+// bit-identical in every CTA and from run to run.  Partials alternate between
+// two halves by round parity: a CTA writes the partials of round r + 2 only
+// after every CTA has arrived at round r + 1, i.e. has read those of round r.
+template <int NV, int NO, typename Fin>
+__device__ bool grid_reduce_df(const MixedArgs& a, const DF (&val)[NV], float (&out)[NO], unsigned& round,
+                               Fin fin) {
+  static_assert(NV <= kMaxPartials / 2 && NV <= 8 && NO <= 8, "partials too small");
+  constexpr int kWarps = kBlock / 32;
+  __shared__ DF s_warp[kWarps][NV];
+  __shared__ DF s_tot[NV];
+  __shared__ int s_flag;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  ++round;
+  const int half = int(round & 1u);
+  float2* part = reinterpret_cast<float2*>(a.partials) + size_t(half) * (kMaxPartials / 2) * gridDim.x;
+  {
+    DF x;
+    const int k = warp_totals<DF, NV>(val, x);
+    if (k >= 0) s_warp[warp][k] = x;
+  }
+  __syncthreads();
+  if (warp < NV) {
+    DF x = lane < kWarps ? s_warp[lane][warp] : DF{0.f, 0.f};
+#pragma unroll
+    for (int o = kWarps / 2; o > 0; o >>= 1) x = df_add(x, AccOps<DF>::shfl_down(x, o));
+    if (lane == 0) part[size_t(warp) * gridDim.x + blockIdx.x] = make_float2(x.hi, x.lo);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_flag = sync_round(a.sync, round, a.spin_limit) ? 1 : 0;
+  __syncthreads();
+  if (s_flag == 0) return false;
+  DF pv[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) pv[k] = DF{0.f, 0.f};
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const float2 p = __ldcg(part + size_t(k) * gridDim.x + b);
+      pv[k] = df_add(pv[k], DF{p.x, p.y});
+    }
+  }
+  {
+    DF x;
+    const int k = warp_totals<DF, NV>(pv, x);
+    if (k >= 0) s_warp[warp][k] = x;
+  }
+  __syncthreads();
+  if (warp < NV) {
+    DF x = lane < kWarps ? s_warp[lane][warp] : DF{0.f, 0.f};
+#pragma unroll
+    for (int o = kWarps / 2; o > 0; o >>= 1) x = df_add(x, AccOps<DF>::shfl_down(x, o));
+    if (lane == 0) s_tot[warp] = x;
+  }
+  __syncthreads();
+  DF t[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) t[k] = s_tot[k];
+  fin(t, out);
+  return true;
+}
+
+// The mixed solver's scalar step from its seven (hi, lo) totals, in FP32
+// pairs (pcg_scalars restated without FP64 instructions): alpha = r.z / p.q;
+// the updated r.z and r.r from the one-reduction identities
+//   r'.z' = r.z - 2 alpha z.q + alpha^2 q.Sq,  r'.r' = r.r - 2 alpha r.q + alpha^2 q.q
+// for the alpha actually applied; beta = r'.z' / r.z, or 0 on a restart or when
+// the recurrence has drifted from the previous estimate by more than 25%;
+// flag 1 for non-finite totals, 2 for a finite breakdown (p.q <= 0).
+// Outputs: alpha, beta, the r'.r' estimate, flag, the r'.z' estimate.
+struct FinPcgF {
+  float prev_est;
+  bool restart;
+  __device__ void operator()(const DF* t, float* o) const {
+    const DF pq = t[0], zq = t[1], qsq = t[2], rz = t[3], rq = t[4], qq = t[5], rr = t[6];
+    const float alpha = df_div(rz, pq);
+    const DF azq = df_mul(zq, alpha), aaqsq = df_mul(df_mul(qsq, alpha), alpha);
+    const DF arq = df_mul(rq, alpha), aaqq = df_mul(df_mul(qq, alpha), alpha);
+    DF est_z = df_add(df_add(rz, DF{-2.f * azq.hi, -2.f * azq.lo}), aaqsq);
+    DF est_r = df_add(df_add(rr, DF{-2.f * arq.hi, -2.f * arq.lo}), aaqq);
+    if (est_z.hi < 0.f) est_z = DF{0.f, 0.f};
+    if (est_r.hi < 0.f) est_r = DF{0.f, 0.f};
+    float beta = df_div(est_z, rz);
+    float flag = 0.f;
+    bool finite = true;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) finite = finite && isfinite(t[k].hi) && isfinite(t[k].lo);
+    if (!finite) flag = 1.f;
+    else if (!(pq.hi > 0.f) || !isfinite(alpha) || !isfinite(beta)) flag = 2.f;
+    if (restart || (prev_est >= 0.f && fabsf(prev_est - rz.hi) > 0.25f * rz.hi)) beta = 0.f;
+    o[0] = alpha;
+    o[1] = beta;
+    o[2] = est_r.hi + est_r.lo;
+    o[3] = flag;
+    o[4] = est_z.hi + est_z.lo;
+  }
+};
+struct FinIdentityF1 {
+  __device__ void operator()(const DF* t, float* o) const { o[0] = t[0].hi + t[0].lo; }
+};
 
 struct FinIdentity1 {
   __device__ void operator()(const double* t, double* o) const { o[0] = t[0]; }
@@ -1185,7 +1315,7 @@ __device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned c
   return true;
 }
 
-// Phase stamps of the last mixed solve (first CTA; SM clock cycles since the
+// Phase stamps of the last mixed solve (the tracer CTA; SM clock cycles since the
 // kernel started), after the trace rows: 0 b, 1 start sweeps, 2 start ready,
 // 3 CG loop, 4 position update; 5-7 (projected and learned starts) Gram sums
 // begun, Gram totals in, coefficients solved, else 0.
@@ -1442,7 +1572,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   unsigned round = 0;  // grid barriers and reductions passed so far
   extern __shared__ __align__(16) unsigned char smem[];  // patch staging of the apply
-  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool tracer = is_tracer();
   const long long t_start = tracer ? cycles_now() : 0ll;
   if (tracer) clear_phase_stamps(a);
   __shared__ double stamp[6];  // trace stamps, written by the tracer thread only
@@ -1473,9 +1603,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       bbsum[0] = df_add(bbsum[0], DF{bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2], 0.f});
       const double dg = m + a.dt * (a.alpha * m);
       a.diag[i] = dg;
+      a.diag_f[i] = float(dg);
       sp = float(jacobi_scale(a, i, dg));
     } else {
       a.diag[i] = 0.0;
+      a.diag_f[i] = 0.f;
     }
     // r.w carries the node's preconditioner scalar through the solve
     a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);
@@ -1494,11 +1626,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       for (int j = 0; j < a.nwarm; ++j) a.wprod[size_t(j) * N + i] = zero4;
     }
   }
-  double tot[1];
-  if (!grid_reduce<DF, 1, 1>(a, bbsum, tot, round, FinIdentity1())) return;
+  // The loop's scalars are FP32 (pairs inside the reductions): no FP64
+  // instruction sits between two phases of an iteration.
+  float tot[1];
+  if (!grid_reduce_df<1, 1>(a, bbsum, tot, round, FinIdentityF1())) return;
   if (tracer) phase_stamp(a, 0, t_start);
-  const double bnorm2 = tot[0];
-  const double thresh = a.rtol * a.rtol * bnorm2;
+  const float bnorm2 = tot[0];
+  const float thresh = float(a.rtol * a.rtol) * bnorm2;
 
   // Initial residual r = b - A v (FP64), p = S r.  Projected and learned
   // starts: also A W_j for the search directions W_j, and the start moves to
@@ -1598,17 +1732,17 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     a.v_keep[N + i] = a.v_lo[i];
     rr[0] = df_add(rr[0], DF{rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2], 0.f});
   }
-  if (!grid_reduce<DF, 1, 1>(a, rr, tot, round, FinIdentity1())) return;
+  if (!grid_reduce_df<1, 1>(a, rr, tot, round, FinIdentityF1())) return;
   if (tracer) phase_stamp(a, 2, t_start);
-  double rho = tot[0];
-  const double rho0 = rho;
+  float rho = tot[0];
+  const float rho0 = rho;
   int it = 0;
   int best_buf = 0;      // kept iterate with the smallest true residual
   bool stalled = false;  // stopped at the precision floor: return the kept iterate
   bool converged = rho <= thresh;
   // recurrence check and restarts (FinPcg); stagnation of the
   // true residual at the refreshes ends the solve unconverged
-  double prev_est = -1.0, best_true = rho0;
+  float prev_est = -1.f, best_true = rho0;
   bool restart = false;
   int stalls = 0;
 
@@ -1624,7 +1758,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
-      float d = float(a.diag[i]);
+      const float d = a.diag_f[i];
       float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
       const float rq = r4.x * qx + r4.y * qy + r4.z * qz, qq = qx * qx + qy * qy + qz * qz;
       const float rr2 = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, sp = r4.w;
@@ -1637,27 +1771,27 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       s7[6] = df_add(s7[6], DF{rr2, 0.f});
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
-    double sc[5];
-    if (!grid_reduce<DF, 7, 5>(a, s7, sc, round, FinPcg{prev_est, restart})) return;
+    float sc[5];
+    if (!grid_reduce_df<7, 5>(a, s7, sc, round, FinPcgF{prev_est, restart})) return;
     prev_est = sc[4];
     restart = false;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
-    if (sc[3] != 0.0) {
+    if (sc[3] != 0.f) {
       // 1: NaN/Inf in the system (e.g. a non-finite force), an error;
       // 2: finite breakdown (p.Ap <= 0 from rounding at the precision
       // floor): stop, the step reports OTFEM_WARN_NOT_CONVERGED
-      if (sc[3] == 1.0 && blockIdx.x == 0 && threadIdx.x == 0)
+      if (sc[3] == 1.f && blockIdx.x == 0 && threadIdx.x == 0)
         atomicCAS(&a.sync->status, 0, OTFEM_ERR_NONFINITE);
       break;
     }
-    const float alpha = float(sc[0]), beta = float(sc[1]);
+    const float alpha = sc[0], beta = sc[1];
     const int row = it;
     ++it;
     for (long i = gtid; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
-      float d = float(a.diag[i]);
+      const float d = a.diag_f[i];
       float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
       df_inc(vh.x, vl.x, alpha * p4.x);
       df_inc(vh.y, vl.y, alpha * p4.y);
@@ -1700,11 +1834,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
         a.v_keep[cand + N + i] = vl;
         tr[0] = df_add(tr[0], DF{rx * rx + ry * ry + rz * rz, 0.f});
       }
-      if (!grid_reduce<DF, 1, 1>(a, tr, tot, round, FinIdentity1())) return;
+      if (!grid_reduce_df<1, 1>(a, tr, tot, round, FinIdentityF1())) return;
       // the true residual well above the recursive one: the recurrence has
       // decoupled from the system, restart the direction
-      restart = tot[0] > 4.0 * sc[2];
-      prev_est = -1.0;
+      restart = tot[0] > 4.f * sc[2];
+      prev_est = -1.f;
       rho = tot[0];
       // stagnation is judged at the periodic refreshes only (16 iterations
       // apart), not at the convergence checks in between
@@ -1756,7 +1890,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
   const V4 zero4 = make_double4(0.0, 0.0, 0.0, 0.0);
   unsigned round = 0;
   extern __shared__ __align__(16) unsigned char smem[];
-  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool tracer = is_tracer();
   const long long t_start = tracer ? cycles_now() : 0ll;
   __shared__ double stamp[6];
 
@@ -2150,7 +2284,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   int counts[4];
   int sweeps = 0;
   auto acc_half = [&](unsigned next_round) { return a.bacc + size_t(next_round & 1u) * M * kBatchSlots; };
-  const bool tracer = blockIdx.x == 0 && threadIdx.x == 0;
+  const bool tracer = is_tracer();
   const long long t_start = tracer ? cycles_now() : 0ll;
   if (tracer) clear_phase_stamps(a);
 
@@ -2186,9 +2320,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           bb[0] = bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2];
           const double dg = mass + a.dt * (a.alpha * mass);
           a.diag[i] = dg;
+          a.diag_f[i] = float(dg);
           sp = float(jacobi_scale(a, i, dg));
         } else {
           a.diag[i] = 0.0;
+          a.diag_f[i] = 0.f;
         }
         a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
         store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
@@ -2352,7 +2488,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           m = a.mesh_of_node[i];
           if (mask_apply[m] && !a.fixed[i]) {
             const float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
-            const float d = float(a.diag[i]);
+            const float d = a.diag_f[i];
             const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
             s7[0] = p4.x * qx + p4.y * qy + p4.z * qz;
             s7[4] = r4.x * qx + r4.y * qy + r4.z * qz;
@@ -2377,7 +2513,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       const float alpha = float(a.bm[m].alpha), beta = float(a.bm[m].beta);
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
-      const float d = float(a.diag[i]);
+      const float d = a.diag_f[i];
       const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
       df_inc(vh.x, vl.x, alpha * p4.x);
       df_inc(vh.y, vl.y, alpha * p4.y);
@@ -2997,6 +3133,7 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.r = c.r;
   a.p = c.p;
   a.diag = c.diag;
+  a.diag_f = c.diag_f;
   a.node_k = c.node_k;
   a.precond = prm.preconditioner == OTFEM_PRECONDITIONER_JACOBI ? 1 : 0;
   a.re_f = c.re_f;

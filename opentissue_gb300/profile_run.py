@@ -76,7 +76,7 @@ def main():
 
 def trace_report(lib, h, dp):
     """Phases of the last solve and the median of each part of a CG
-    iteration, from the SM clock stamps of the first CTA (microseconds at
+    iteration, from the SM clock stamps of the middle CTA (microseconds at
     the SM clock the GPU reports as its maximum)."""
     import subprocess
     try:
