@@ -1033,6 +1033,16 @@ __device__ void apply_patches_gather(const MixedArgs& a, const typename ApplyOps
   }
 }
 
+// First item (tet or node) of this thread in a grid-stride sweep (stride
+// gridDim.x * blockDim.x).  Warps are numbered across the CTAs first (warp k
+// of CTA b is warp k * gridDim.x + b) and each covers 32 consecutive items, so
+// a partial last round spreads over every SM instead of falling on the first
+// CTAs (whose SMs the next barrier would wait for), while each round still
+// covers one contiguous range of items.
+__device__ __forceinline__ long sweep_first() {
+  return ((long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
+}
+
 // Variant kApplyTets: one tet per thread over the whole mesh (grid-stride),
 // operands gathered from global memory, node forces added with global vector
 // reductions (the accumulator must be zero for every written node).
@@ -1044,7 +1054,7 @@ __device__ void apply_tets(const MixedArgs& a, const typename ApplyOps<R>::V4* u
   typedef typename ApplyOps<R>::V4 V4;
   const int T = a.T;
   const bool has_lo = sizeof(R) == 4 && ulo != nullptr;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+  for (int t = int(sweep_first()); t < T; t += gridDim.x * blockDim.x) {
     if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
     const int4 n = a.tets[t];
     V4 w[4] = {u4[n.x], u4[n.y], u4[n.z], u4[n.w]};
@@ -1235,7 +1245,7 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
 __device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
                                  const unsigned char* mask) {
   const int T = a.T, TT = a.tile_tets;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+  for (int t = int(sweep_first()); t < T; t += gridDim.x * blockDim.x) {
     if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
     const int tile = tile_of(t, a.tile_magic);
     const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
@@ -1262,7 +1272,7 @@ __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char
 }
 __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
   const int T = a.T, TT = a.tile_tets;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+  for (int t = int(sweep_first()); t < T; t += gridDim.x * blockDim.x) {
     const int tile = tile_of(t, a.tile_magic);
     const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
@@ -1338,14 +1348,13 @@ __device__ bool grid_sum_wide(const MixedArgs& a, int nv, Val val, double* tot, 
   constexpr int kWarps = kBlock / 32;
   __shared__ DF s_w[kWarps][kMaxWarmSums];
   __shared__ int s_ok;
-  const long gstride = (long)gridDim.x * blockDim.x;
-  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long N = a.N, n0 = sweep_first(), gstride = (long)gridDim.x * blockDim.x;  // as the node passes
   const int warp = threadIdx.x >> 5;
   for (int c0 = 0; c0 < nv; c0 += 8) {
     DF acc[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) acc[k] = DF{0.f, 0.f};
-    for (long i = gtid; i < a.N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
 #pragma unroll
       for (int k = 0; k < 8; ++k)
@@ -1566,8 +1575,9 @@ __device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int app
 // K2, mixed precision (see the file comment).
 __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const int N = a.N;
-  const long gstride = (long)gridDim.x * blockDim.x;
-  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  // this thread's nodes (sweep_first); every node pass uses the same
+  // mapping, so a node's data passes between phases within one thread
+  const long n0 = sweep_first(), gstride = (long)gridDim.x * blockDim.x;
   const float scale = float(a.dt * a.dt);
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   unsigned round = 0;  // grid barriers and reductions passed so far
@@ -1581,7 +1591,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // ascending tet order and summed as (hi, lo) pairs; the diagonal
   // M(1 + dt*alpha) of fem_dynamics_assembly.h:84-85; v split into (hi, lo).
   DF bbsum[1] = {{0.f, 0.f}};
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     DF g[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
       int e = a.inc_ent[q];
@@ -1651,7 +1661,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   if (a.nwarm) {
     const int nw = a.nwarm;
     // r = b - A v; A W_j += diag W_j (the mass term)
-    for (long i = gtid; i < N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
       const double dg = a.diag[i];
@@ -1690,7 +1700,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     __syncthreads();
   }
   DF rr[1] = {{0.f, 0.f}};
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     if (a.fixed[i]) {
       a.p_f[i] = zero4;
       a.r_f[i] = zero4;
@@ -1755,7 +1765,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (tracer) stamp[1] = double(cycles_now() - t_start);
     // q = diag p + q; the totals of FinPcg (r.w = the node's scalar s)
     DF s7[7] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (long i = gtid; i < N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       const float d = a.diag_f[i];
@@ -1787,7 +1797,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     const float alpha = sc[0], beta = sc[1];
     const int row = it;
     ++it;
-    for (long i = gtid; i < N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
@@ -1821,7 +1831,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       DF tr[1] = {{0.f, 0.f}};
       const long cand = 2L * (best_buf ^ 1) * N;  // the kept copy that is not the best
-      for (long i = gtid; i < N; i += gstride) {
+      for (long i = n0; i < N; i += gstride) {
         if (a.fixed[i]) continue;
         float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
         double d = a.diag[i];
@@ -1859,7 +1869,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // v back to FP64 (the kept best iterate when stopped at the floor);
   // position_update (fem_position_update.h:25-39); the velocity change is
   // kept for the warm starts
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     if (a.fixed[i]) continue;
     const long kb = 2L * best_buf * N;
     float4 vh = stalled ? a.v_keep[kb + i] : a.v_f[i], vl = stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
@@ -1881,8 +1891,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
 __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
   typedef double4 V4;
   const int N = a.N;
-  const long gstride = (long)gridDim.x * blockDim.x;
-  const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  // this thread's nodes (sweep_first); every node pass uses the same
+  // mapping, so a node's data passes between phases within one thread
+  const long n0 = sweep_first(), gstride = (long)gridDim.x * blockDim.x;
   V4* pv = a.p_d;
   V4* vv = a.v_d;
   V4* qv = a.q_d;
@@ -1895,7 +1906,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
   __shared__ double stamp[6];
 
   double bbsum[1] = {0.0};
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     double g[3] = {0.0, 0.0, 0.0};
     for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
       int e = a.inc_ent[q];
@@ -1927,7 +1938,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
   apply_sweep<double>(a, vv, nullptr, qv, a.re_d, a.b_d, a.c_d, scale, smem);
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   double rr[2] = {0.0, 0.0};
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     if (a.fixed[i]) {
       pv[i] = zero4;
       for (int c = 0; c < 3; ++c) a.p[3 * i + c] = 0.0, a.r[3 * i + c] = 0.0;
@@ -1960,7 +1971,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
     double s5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (long i = gtid; i < N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
@@ -1991,7 +2002,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     const int row = it;
     ++it;
     double rn[2] = {0.0, 0.0};
-    for (long i = gtid; i < N; i += gstride) {
+    for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       V4 q4 = load_acc(qv + i);
       double d = a.diag[i];
@@ -2024,7 +2035,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
       ++applies;
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       double tr[2] = {0.0, 0.0};
-      for (long i = gtid; i < N; i += gstride) {
+      for (long i = n0; i < N; i += gstride) {
         if (a.fixed[i]) continue;
         V4 q4 = load_acc(qv + i);
         double d = a.diag[i];
@@ -2044,7 +2055,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
     }
     converged = rho <= thresh;
   }
-  for (long i = gtid; i < N; i += gstride) {
+  for (long i = n0; i < N; i += gstride) {
     if (a.fixed[i]) continue;
     for (int c = 0; c < 3; ++c) a.x[3 * i + c] += a.v[3 * i + c] * a.dt;
   }
