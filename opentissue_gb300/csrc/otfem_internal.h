@@ -53,7 +53,7 @@ struct DeviceSync {
 // Per-mesh state of a batched solve (device memory, one per mesh).
 struct BatchMesh {
   double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta;
-  double wgam[kMaxWarmDirs];  // projected / learned start: the mesh's coefficients
+  float wgam[kMaxWarmDirs];   // projected / learned start: the mesh's coefficients
   int active, restart, stalls, iterations, applies, status, converged, pad;
   int best_buf;  // which kept iterate (v_keep) has the smallest true residual
   int stalled;   // stopped at the precision floor: the kept iterate is the result

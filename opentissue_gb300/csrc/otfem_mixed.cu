@@ -1397,75 +1397,79 @@ __device__ bool grid_sum_wide(const MixedArgs& a, int nv, Val val, double* tot, 
   return ok;
 }
 
+// FP32 value of an FP64 number by bit manipulation: the exponent rebiased,
+// the mantissa truncated to 23 bits (at most 1 ulp of FP32 low).  Integer
+// instructions only: a conversion instruction would run on GB300's FP64 pipe.
+// Magnitudes below the FP32 normal range become 0, above it infinity; NaN
+// stays NaN.
+__device__ __forceinline__ float f32_of_f64(double d) {
+  const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(d));
+  const unsigned sign = unsigned(u >> 32) & 0x80000000u;
+  const int e = int((u >> 52) & 0x7ffu);
+  const unsigned mant = unsigned(u >> 29) & 0x7fffffu;
+  if (e == 0x7ff) return (u & 0xfffffffffffffull) != 0ull ? __uint_as_float(0x7fc00000u) : __uint_as_float(sign | 0x7f800000u);
+  const int fe = e - 1023 + 127;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | (unsigned(fe) << 23) | mant);
+}
+
 // The projected start's coefficients: the least-energy point of v + span{W_j}
 // solves G g = h with G_ij = W_i.A W_j and h_i = W_i.(b - A v).  `tot` holds
-// G's upper triangle row by row, then h.  Directions are taken in order
-// (the newest velocity change first); one whose A-norm is not positive and
-// finite, or that lies (nearly) in the span of the ones before it (Cholesky
-// pivot of the unit-diagonal G below 1e-9), gets g_j = 0.
-__device__ void warm_solve(const double* tot, int n, double* g) {
-  double L[kMaxWarmDirs][kMaxWarmDirs], sc[kMaxWarmDirs], y[kMaxWarmDirs];
-  bool act[kMaxWarmDirs];
+// G's upper triangle row by row, then h (FP64 sums).  The system is scaled to
+// a unit diagonal and solved in FP32 by Gauss-Jordan elimination with the
+// diagonal pivots in order (no FP64 instruction; the coefficients only
+// choose where CG starts, and an error e in g costs e^T G e / 2 of the
+// start's energy).  Directions are taken in order (the newest velocity
+// change first); one whose A-norm is not positive and finite, or that lies
+// (nearly) in the span of the ones before it (pivot, a Schur complement of
+// the unit-diagonal G, below kWarmPivot), gets g_j = 0 and leaves the system.
+constexpr float kWarmPivot = 1e-5f;
+
+// One thread per system (the batch: one per mesh).
+__device__ void warm_solve(const double* tot, int n, float* g) {
+  float M[kMaxWarmDirs][kMaxWarmDirs + 1], sc[kMaxWarmDirs], piv[kMaxWarmDirs];
+  bool live[kMaxWarmDirs];
   auto G = [&](int i, int j) {
     if (i > j) {
       const int t = i;
       i = j;
       j = t;
     }
-    return tot[i * n - i * (i - 1) / 2 + (j - i)];
+    return f32_of_f64(tot[i * n - i * (i - 1) / 2 + (j - i)]);
   };
   const double* h = tot + n * (n + 1) / 2;
   for (int i = 0; i < n; ++i) {
-    const double d = G(i, i);
-    act[i] = d > 0.0 && isfinite(d) && isfinite(h[i]);
-    sc[i] = act[i] ? rsqrt(d) : 0.0;
-    g[i] = 0.0;
+    const float d = G(i, i), hv = f32_of_f64(h[i]);
+    live[i] = d > 0.f && isfinite(d) && isfinite(hv);
+    sc[i] = live[i] ? rsqrtf(d) : 0.f;
+  }
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) M[i][j] = G(i, j) * sc[i] * sc[j];
+    M[i][n] = f32_of_f64(h[i]) * sc[i];
   }
   for (int j = 0; j < n; ++j) {
-    if (!act[j]) continue;
-    double piv = 1.0;
-    for (int k = 0; k < j; ++k)
-      if (act[k]) piv -= L[j][k] * L[j][k];
-    if (!(piv > 1e-9)) {
-      act[j] = false;
+    piv[j] = M[j][j];
+    if (!live[j] || !(piv[j] > kWarmPivot)) {
+      live[j] = false;
       continue;
     }
-    L[j][j] = sqrt(piv);
-    const double inv = 1.0 / L[j][j];
-    for (int i = j + 1; i < n; ++i) {
-      if (!act[i]) continue;
-      double t = G(i, j) * sc[i] * sc[j];
-      for (int k = 0; k < j; ++k)
-        if (act[k]) t -= L[i][k] * L[j][k];
-      L[i][j] = t * inv;
+    for (int i = 0; i < n; ++i) {
+      if (i == j) continue;
+      const float f = M[i][j] / piv[j];
+      for (int k = j + 1; k <= n; ++k) M[i][k] = fmaf(-f, M[j][k], M[i][k]);
     }
   }
-  for (int j = 0; j < n; ++j) {
-    if (!act[j]) continue;
-    double t = h[j] * sc[j];
-    for (int k = 0; k < j; ++k)
-      if (act[k]) t -= L[j][k] * y[k];
-    y[j] = t / L[j][j];
+  for (int i = 0; i < n; ++i) {
+    const float x = M[i][n] / piv[i] * sc[i];
+    g[i] = live[i] && isfinite(x) ? x : 0.f;
   }
-  for (int j = n - 1; j >= 0; --j) {
-    if (!act[j]) continue;
-    double t = y[j];
-    for (int i = j + 1; i < n; ++i)
-      if (act[i]) t -= L[i][j] * g[i];
-    g[j] = t / L[j][j];
-  }
-  for (int j = 0; j < n; ++j) g[j] = act[j] && isfinite(g[j]) ? g[j] * sc[j] : 0.0;
 }
 
-// warm_solve by one warp, for a system every CTA solves for itself: lane i
-// holds row i of the unit-diagonal G and h_i, and Gauss-Jordan elimination
-// with the diagonal pivots in order gives g directly.  The pivot of column j
-// is the Schur complement that the Cholesky factor's pivot is, so the same
-// directions are dropped (pivot below 1e-9; a dropped direction's row and
-// column leave the system).  The serial chain is one shuffle, one reciprocal
-// and one FMA per direction instead of the scalar solve's triangular loops.
+// The same by one warp, for a system every CTA solves for itself: lane i
+// holds row i and h_i, and each elimination step broadcasts the pivot row.
 // Called by the 32 lanes of one warp; g[j] is written for j < n.
-__device__ void warm_solve_warp(const double* tot, int n, double* g) {
+__device__ void warm_solve_warp(const double* tot, int n, float* g) {
   constexpr unsigned kAll = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const bool own = lane < n;
@@ -1476,37 +1480,37 @@ __device__ void warm_solve_warp(const double* tot, int n, double* g) {
       i = j;
       j = t;
     }
-    return tot[i * n - i * (i - 1) / 2 + (j - i)];
+    return f32_of_f64(tot[i * n - i * (i - 1) / 2 + (j - i)]);
   };
-  const double d = own ? G(lane, lane) : 0.0, hv = own ? h[lane] : 0.0;
-  const bool act = own && d > 0.0 && isfinite(d) && isfinite(hv);
-  const double sc = act ? rsqrt(d) : 0.0;
-  double row[kMaxWarmDirs];
+  const float d = own ? G(lane, lane) : 0.f, hv = own ? f32_of_f64(h[lane]) : 0.f;
+  const bool act = own && d > 0.f && isfinite(d) && isfinite(hv);
+  const float sc = act ? rsqrtf(d) : 0.f;
+  float row[kMaxWarmDirs];
 #pragma unroll
   for (int k = 0; k < kMaxWarmDirs; ++k) {
-    const double sk = __shfl_sync(kAll, sc, k);
-    row[k] = own && k < n ? G(lane, k) * sc * sk : 0.0;
+    const float sk = __shfl_sync(kAll, sc, k);
+    row[k] = own && k < n ? G(lane, k) * sc * sk : 0.f;
   }
-  double rhs = hv * sc, piv = 1.0;
+  float rhs = hv * sc, piv = 1.f;
   int live = act ? 1 : 0;
 #pragma unroll
   for (int j = 0; j < kMaxWarmDirs; ++j) {
     if (j >= n) break;
-    const double pj = __shfl_sync(kAll, row[j], j);
-    const bool use = __shfl_sync(kAll, live, j) != 0 && pj > 1e-9;
+    const float pj = __shfl_sync(kAll, row[j], j);
+    const bool use = __shfl_sync(kAll, live, j) != 0 && pj > kWarmPivot;
     if (lane == j) {
       live = use ? 1 : 0;
       piv = pj;
     }
     if (!use) continue;
-    const double f = lane == j ? 0.0 : row[j] * __drcp_rn(pj);
+    const float f = lane == j ? 0.f : row[j] / pj;
 #pragma unroll
-    for (int k = j + 1; k < kMaxWarmDirs; ++k) row[k] = fma(-f, __shfl_sync(kAll, row[k], j), row[k]);
-    rhs = fma(-f, __shfl_sync(kAll, rhs, j), rhs);
+    for (int k = j + 1; k < kMaxWarmDirs; ++k) row[k] = fmaf(-f, __shfl_sync(kAll, row[k], j), row[k]);
+    rhs = fmaf(-f, __shfl_sync(kAll, rhs, j), rhs);
   }
   if (own) {
-    const double x = rhs / piv * sc;
-    g[lane] = live && isfinite(x) ? x : 0.0;
+    const float x = rhs / piv * sc;
+    g[lane] = live && isfinite(x) ? x : 0.f;
   }
 }
 
@@ -1657,7 +1661,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   if (tracer) phase_stamp(a, 1, t_start);
-  __shared__ double s_gam[kMaxWarmDirs];
+  __shared__ float s_gam[kMaxWarmDirs];
   if (a.nwarm) {
     const int nw = a.nwarm;
     // r = b - A v; A W_j += diag W_j (the mass term)
@@ -1716,7 +1720,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       rf[1] = r4.y;
       rf[2] = r4.z;
       for (int j = 0; j < a.nwarm; ++j) {
-        const float g = float(s_gam[j]);
+        const float g = s_gam[j];
         if (g == 0.f) continue;
         const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
         df_inc(vh.x, vl.x, g * w.x);
@@ -2444,9 +2448,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             rf[0] = r4.x;
             rf[1] = r4.y;
             rf[2] = r4.z;
-            const double* gam = a.bm[m].wgam;
+            const float* gam = a.bm[m].wgam;
             for (int j = 0; j < a.nwarm; ++j) {
-              const float g = float(gam[j]);
+              const float g = gam[j];
               if (g == 0.f) continue;
               const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
               df_inc(vh.x, vl.x, g * w.x);
