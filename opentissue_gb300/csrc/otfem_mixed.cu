@@ -1467,49 +1467,50 @@ __device__ void warm_solve(const double* tot, int n, float* g) {
 }
 
 // The same by one warp, for a system every CTA solves for itself: lane i
-// holds row i and h_i, and each elimination step broadcasts the pivot row.
-// Called by the 32 lanes of one warp; g[j] is written for j < n.
+// owns row i of the augmented system [G | h] in shared memory, and each
+// elimination step reads the pivot row from there.  The loops are left
+// rolled: this code runs once per step, where every instruction is fetched
+// cold, so its length, not its dependency chain, sets its time.  Called by
+// the 32 lanes of one warp; g[j] is written for j < n.
 __device__ void warm_solve_warp(const double* tot, int n, float* g) {
   constexpr unsigned kAll = 0xffffffffu;
+  __shared__ float s_m[kMaxWarmDirs][kMaxWarmDirs + 1];
+  __shared__ float s_sc[kMaxWarmDirs];
   const int lane = threadIdx.x & 31;
-  const bool own = lane < n;
-  const double* h = tot + n * (n + 1) / 2;
-  auto G = [&](int i, int j) {
-    if (i > j) {
-      const int t = i;
-      i = j;
-      j = t;
-    }
-    return f32_of_f64(tot[i * n - i * (i - 1) / 2 + (j - i)]);
-  };
-  const float d = own ? G(lane, lane) : 0.f, hv = own ? f32_of_f64(h[lane]) : 0.f;
-  const bool act = own && d > 0.f && isfinite(d) && isfinite(hv);
-  const float sc = act ? rsqrtf(d) : 0.f;
-  float row[kMaxWarmDirs];
-#pragma unroll
-  for (int k = 0; k < kMaxWarmDirs; ++k) {
-    const float sk = __shfl_sync(kAll, sc, k);
-    row[k] = own && k < n ? G(lane, k) * sc * sk : 0.f;
+  const int n1 = n + 1, tri = n * (n + 1) / 2;
+  bool live = false;
+  if (lane < n) {
+    const float d = f32_of_f64(tot[lane * n - lane * (lane - 1) / 2]), hv = f32_of_f64(tot[tri + lane]);
+    live = d > 0.f && isfinite(d) && isfinite(hv);
+    s_sc[lane] = live ? rsqrtf(d) : 0.f;
   }
-  float rhs = hv * sc, piv = 1.f;
-  int live = act ? 1 : 0;
-#pragma unroll
-  for (int j = 0; j < kMaxWarmDirs; ++j) {
-    if (j >= n) break;
-    const float pj = __shfl_sync(kAll, row[j], j);
-    const bool use = __shfl_sync(kAll, live, j) != 0 && pj > kWarmPivot;
+  __syncwarp();
+#pragma unroll 1
+  for (int e = lane; e < n * n1; e += 32) {
+    const int i = e / n1, j = e - i * n1;
+    const int lo = min(i, j), hi = max(i, j);
+    s_m[i][j] = j < n ? f32_of_f64(tot[lo * n - lo * (lo - 1) / 2 + (hi - lo)]) * s_sc[i] * s_sc[j]
+                      : f32_of_f64(tot[tri + i]) * s_sc[i];
+  }
+  __syncwarp();
+  float piv = 1.f;
+#pragma unroll 1
+  for (int j = 0; j < n; ++j) {
+    const float pj = s_m[j][j];
+    const bool use = __shfl_sync(kAll, live ? 1 : 0, j) != 0 && pj > kWarmPivot;
     if (lane == j) {
-      live = use ? 1 : 0;
+      live = use;
       piv = pj;
     }
-    if (!use) continue;
-    const float f = lane == j ? 0.f : row[j] / pj;
-#pragma unroll
-    for (int k = j + 1; k < kMaxWarmDirs; ++k) row[k] = fmaf(-f, __shfl_sync(kAll, row[k], j), row[k]);
-    rhs = fmaf(-f, __shfl_sync(kAll, rhs, j), rhs);
+    if (use && lane < n && lane != j) {
+      const float f = s_m[lane][j] / pj;
+#pragma unroll 1
+      for (int k = j + 1; k <= n; ++k) s_m[lane][k] = fmaf(-f, s_m[j][k], s_m[lane][k]);
+    }
+    __syncwarp();
   }
-  if (own) {
-    const float x = rhs / piv * sc;
+  if (lane < n) {
+    const float x = s_m[lane][n] / piv * s_sc[lane];
     g[lane] = live && isfinite(x) ? x : 0.f;
   }
 }
