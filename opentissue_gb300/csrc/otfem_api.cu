@@ -59,7 +59,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.diag_f, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.v_keep, c.features, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.diag, c.diag_f, c.diag_lo, c.b_hi, c.b_lo, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.v_keep, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -292,6 +292,9 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.c_d, 3 * T);
   OT_ALLOC(c.diag, N);
   OT_ALLOC(c.diag_f, N);
+  OT_ALLOC(c.diag_lo, N);
+  OT_ALLOC(c.b_hi, N);
+  OT_ALLOC(c.b_lo, N);
   OT_ALLOC(c.node_k, N);
   OT_ALLOC(c.r, 3 * N);
   OT_ALLOC(c.p, 3 * N);

@@ -123,7 +123,10 @@ struct Context {
   float *re_f = nullptr, *b_f = nullptr, *c_f = nullptr;  // 9T, 9T, 3T
   double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
   double* diag = nullptr;                                 // N: m(1+dt*alpha)
-  float* diag_f = nullptr;                                // N: the same in FP32
+  float* diag_f = nullptr;                                // N: the same as (hi, lo) FP32 pairs
+  float* diag_lo = nullptr;                               // N
+  float4* b_hi = nullptr;                                 // N: b as (hi, lo) FP32 pairs
+  float4* b_lo = nullptr;                                 // N
   double* node_k = nullptr;  // N: tr(sum_e Ke_ii) / 3 over the node's tets (Jacobi preconditioner), from init
   double *r = nullptr, *p = nullptr, *bvec = nullptr;    // 3N
   float4 *p_f = nullptr, *v_f = nullptr, *q_f = nullptr;  // N (p_f/v_f: high part, w = free flag)

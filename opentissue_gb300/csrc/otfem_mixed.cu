@@ -45,6 +45,7 @@
 #include <vector>
 
 #include "otfem_internal.h"
+#include "otfem_df.h"
 #include "otfem_refmath.cuh"
 
 namespace otfem {
@@ -83,7 +84,10 @@ struct MixedArgs {
   double* r;
   double* p;
   double* diag;
-  float* diag_f;         // the same in FP32 (the mixed loop's vector passes)
+  float* diag_f;         // the same as (hi, lo) pairs: hi (the mixed loop's vector passes)
+  float* diag_lo;        //   and lo
+  float4* b_hi;          // b as (hi, lo) pairs (the mixed solver's residual refreshes)
+  float4* b_lo;
   const double* node_k;  // tr(sum_e Ke_ii) / 3 per node (Jacobi preconditioner)
   int precond;           // 1: CG preconditioned by the node scalars 1 / (diag + dt^2 node_k)
   // FP32 apply
@@ -369,6 +373,30 @@ __device__ __forceinline__ DF df_mul(DF a, float b) {
   e = fmaf(a.lo, b, e);
   const float h = p + e;
   return DF{h, e - (h - p)};
+}
+// a x b for two pairs, renormalised.
+__device__ __forceinline__ DF df_mul2(DF a, DF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float h = p + e;
+  return DF{h, e - (h - p)};
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+// FP64 <-> pair by integer instructions (otfem_df.h)
+__device__ __forceinline__ DF df_of(double x) {
+  DF r;
+  dfbits::split(x, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ double f64_of(DF a) { return dfbits::join(a.hi, a.lo); }
+// One component of b - (d v + q) in pair arithmetic, rounded to FP32: b and d
+// as pairs, v the (hi, lo) iterate, q the FP32 element sum.
+__device__ __forceinline__ float residual_df(DF b, DF d, DF v, float q) {
+  const DF t = df_add(df_mul2(d, v), DF{q, 0.f});
+  const DF r = df_add(b, df_neg(t));
+  return r.hi + r.lo;
 }
 // a / b rounded to FP32 (one correction step on the FP32 quotient of the
 // high parts: q + (a - q b) / b, with q b formed exactly by an FMA).
@@ -1544,12 +1572,12 @@ __device__ __forceinline__ void trace_row(const MixedArgs& a, int row, double rh
 // same space as the last kMaxHistory changes, but for a smooth trajectory its
 // vectors are far from parallel, so their Gram system stays well conditioned
 // in FP32; the pairs keep the differences exact to ~1e-14 of each level.
-__device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long i, const double (&dv)[3]) {
+__device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long i, const DF (&dv)[3]) {
   const long N = a.N;
   float hi[3], lo[3];
   for (int c = 0; c < 3; ++c) {
-    hi[c] = float(dv[c]);
-    lo[c] = float(dv[c] - double(hi[c]));
+    hi[c] = dv[c].hi;
+    lo[c] = dv[c].lo;
   }
   for (int j = 0; j < a.hist_rec; ++j) {
     const float4 oh = a.hist[size_t(j) * N + i], ol = a.hist[size_t(kMaxHistory + j) * N + i];
@@ -1577,6 +1605,18 @@ __device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int app
   a.stats->bb = bnorm2;
 }
 
+// r = b - (d v + q) of node i, rounded to FP32: the FP64 subtraction of the
+// dynamics assembly (fem_dynamics_assembly.h:88-91) in (hi, lo) pairs, from
+// the pairs of b and d the first phase stores.
+__device__ __forceinline__ void node_residual(const MixedArgs& a, long i, float4 vh, float4 vl, float4 q4,
+                                              float (&r)[3]) {
+  const float4 bh = a.b_hi[i], bl = a.b_lo[i];
+  const DF d{a.diag_f[i], a.diag_lo[i]};
+  r[0] = residual_df(DF{bh.x, bl.x}, d, DF{vh.x, vl.x}, q4.x);
+  r[1] = residual_df(DF{bh.y, bl.y}, d, DF{vh.y, vl.y}, q4.y);
+  r[2] = residual_df(DF{bh.z, bl.z}, d, DF{vh.z, vl.z}, q4.z);
+}
+
 // K2, mixed precision (see the file comment).
 __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   const int N = a.N;
@@ -1584,6 +1624,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // mapping, so a node's data passes between phases within one thread
   const long n0 = sweep_first(), gstride = (long)gridDim.x * blockDim.x;
   const float scale = float(a.dt * a.dt);
+  // dt and 1 + dt alpha as (hi, lo) pairs
+  const DF dt2[2] = {df_of(a.dt), df_add(DF{1.f, 0.f}, df_mul2(df_of(a.dt), df_of(a.alpha)))};
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   unsigned round = 0;  // grid barriers and reductions passed so far
   extern __shared__ __align__(16) unsigned char smem[];  // patch staging of the apply
@@ -1605,31 +1647,38 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       df_inc(g[1].hi, g[1].lo, f.y);
       df_inc(g[2].hi, g[2].lo, f.z);
     }
-    bool fx = a.fixed[i] != 0;
-    double m = a.mass[i];
-    double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+    // in (hi, lo) pairs: no FP64 instruction
+    const bool fx = a.fixed[i] != 0;
+    const DF m = df_of(a.mass[i]);
+    const DF vi[3] = {df_of(a.v[3 * i]), df_of(a.v[3 * i + 1]), df_of(a.v[3 * i + 2])};
     float sp = 0.f;
     if (!fx) {
-      double b3[3];
-      for (int c = 0; c < 3; ++c)
-        b3[c] = m * vi[c] + a.dt * (a.fext[3 * i + c] - (double(g[c].hi) + double(g[c].lo)));
-      for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
-      float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
+      DF b3[3];
+      for (int c = 0; c < 3; ++c) {
+        b3[c] = df_add(df_mul2(m, vi[c]), df_mul2(dt2[0], df_add(df_of(a.fext[3 * i + c]), df_neg(g[c]))));
+        a.bvec[3 * i + c] = f64_of(b3[c]);
+      }
+      a.b_hi[i] = make_float4(b3[0].hi, b3[1].hi, b3[2].hi, 0.f);
+      a.b_lo[i] = make_float4(b3[0].lo, b3[1].lo, b3[2].lo, 0.f);
+      float bf[3] = {b3[0].hi + b3[0].lo, b3[1].hi + b3[1].lo, b3[2].hi + b3[2].lo};
       bbsum[0] = df_add(bbsum[0], DF{bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2], 0.f});
-      const double dg = m + a.dt * (a.alpha * m);
-      a.diag[i] = dg;
-      a.diag_f[i] = float(dg);
-      sp = float(jacobi_scale(a, i, dg));
+      const DF dg = df_mul2(m, dt2[1]);  // m (1 + dt alpha)
+      a.diag[i] = f64_of(dg);
+      a.diag_f[i] = dg.hi;
+      a.diag_lo[i] = dg.lo;
+      sp = a.precond ? 1.f / (dg.hi + scale * dfbits::trunc_f32(a.node_k[i])) : 1.f;
     } else {
       a.diag[i] = 0.0;
       a.diag_f[i] = 0.f;
+      a.diag_lo[i] = 0.f;
     }
     // r.w carries the node's preconditioner scalar through the solve
     a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
     // never accumulated (w = 0).
-    store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+    a.v_f[i] = make_float4(vi[0].hi, vi[1].hi, vi[2].hi, fx ? 0.f : 1.f);
+    a.v_lo[i] = make_float4(vi[0].lo, vi[1].lo, vi[2].lo, 0.f);
     a.q_f[i] = zero4;
     if (a.nwarm) {
       // learned start: the network's correction c = its dv - dv_prev is the
@@ -1669,13 +1718,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-      const double dg = a.diag[i];
       float rf[3];
-      rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
-      rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
-      rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
+      node_residual(a, i, vh, vl, q4, rf);
       a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-      const float df = float(dg);
+      const float df = a.diag_f[i];
       for (int j = 0; j < nw; ++j) {
         const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
         a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
@@ -1735,10 +1781,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       a.v_lo[i] = vl;
     } else {
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-      const double d = a.diag[i];
-      rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-      rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-      rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+      node_residual(a, i, vh, vl, q4, rf);
     }
     a.r_f[i] = make_float4(rf[0], rf[1], rf[2], sp);
     a.p_f[i] = make_float4(sp * rf[0], sp * rf[1], sp * rf[2], 1.f);  // p = z = S r
@@ -1838,11 +1881,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       const long cand = 2L * (best_buf ^ 1) * N;  // the kept copy that is not the best
       for (long i = n0; i < N; i += gstride) {
         if (a.fixed[i]) continue;
-        float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-        double d = a.diag[i];
-        float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-        float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-        float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+        const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
+        float rr3[3];
+        node_residual(a, i, vh, vl, q4, rr3);
+        const float rx = rr3[0], ry = rr3[1], rz = rr3[2];
         a.r_f[i] = make_float4(rx, ry, rz, a.r_f[i].w);
         a.q_f[i] = zero4;
         a.v_keep[cand + i] = vh;
@@ -1878,14 +1920,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (a.fixed[i]) continue;
     const long kb = 2L * best_buf * N;
     float4 vh = stalled ? a.v_keep[kb + i] : a.v_f[i], vl = stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
-    double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
-    double dv[3];
+    // in pairs, with one FP64 addition per coordinate (x keeps its 53 bits)
+    const DF v3[3] = {{vh.x, vl.x}, {vh.y, vl.y}, {vh.z, vl.z}};
+    DF dv[3];
     for (int c = 0; c < 3; ++c) {
-      dv[c] = v3[c] - a.v[3 * i + c];
-      a.v[3 * i + c] = v3[c];
-      a.x[3 * i + c] += v3[c] * a.dt;
+      dv[c] = df_add(v3[c], df_neg(df_of(a.v[3 * i + c])));
+      a.v[3 * i + c] = f64_of(v3[c]);
+      a.x[3 * i + c] += f64_of(df_mul2(v3[c], dt2[0]));
     }
-    a.dv_last[i] = make_float4(float(dv[0]), float(dv[1]), float(dv[2]), 0.f);
+    a.dv_last[i] = make_float4(dv[0].hi, dv[1].hi, dv[2].hi, 0.f);
     if (a.hist) record_velocity_change(a, i, dv);
   }
   if (tracer) phase_stamp(a, 4, t_start);
@@ -2288,6 +2331,7 @@ struct FinBatchRefresh {
 __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   const int N = a.N, M = a.num_meshes;
   const float scale = float(a.dt * a.dt);
+  const DF dt_pair = df_of(a.dt);
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   unsigned round = 0;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2587,14 +2631,15 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     const BatchMesh& bmi = a.bm[a.mesh_of_node[i]];
     const long kb = 2L * bmi.best_buf * N;
     const float4 vh = bmi.stalled ? a.v_keep[kb + i] : a.v_f[i], vl = bmi.stalled ? a.v_keep[kb + N + i] : a.v_lo[i];
-    const double v3[3] = {double(vh.x) + double(vl.x), double(vh.y) + double(vl.y), double(vh.z) + double(vl.z)};
-    double dv[3];
+    // in pairs, with one FP64 addition per coordinate (x keeps its 53 bits)
+    const DF v3[3] = {{vh.x, vl.x}, {vh.y, vl.y}, {vh.z, vl.z}};
+    DF dv[3];
     for (int c = 0; c < 3; ++c) {
-      dv[c] = v3[c] - a.v[3 * i + c];
-      a.v[3 * i + c] = v3[c];
-      a.x[3 * i + c] += v3[c] * a.dt;
+      dv[c] = df_add(v3[c], df_neg(df_of(a.v[3 * i + c])));
+      a.v[3 * i + c] = f64_of(v3[c]);
+      a.x[3 * i + c] += f64_of(df_mul2(v3[c], dt_pair));
     }
-    a.dv_last[i] = make_float4(float(dv[0]), float(dv[1]), float(dv[2]), 0.f);
+    a.dv_last[i] = make_float4(dv[0].hi, dv[1].hi, dv[2].hi, 0.f);
     if (a.hist) record_velocity_change(a, i, dv);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -3150,6 +3195,9 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.p = c.p;
   a.diag = c.diag;
   a.diag_f = c.diag_f;
+  a.diag_lo = c.diag_lo;
+  a.b_hi = c.b_hi;
+  a.b_lo = c.b_lo;
   a.node_k = c.node_k;
   a.precond = prm.preconditioner == OTFEM_PRECONDITIONER_JACOBI ? 1 : 0;
   a.re_f = c.re_f;
