@@ -52,7 +52,9 @@ struct DeviceSync {
 
 // Per-mesh state of a batched solve (device memory, one per mesh).
 struct BatchMesh {
-  double bnorm2, thresh, rho, rho0, est, prev_est, best_true, alpha, beta;
+  double bnorm2, rho, rho0, best_true;
+  // the iteration's scalars, FP32 (FP64 instructions are slow on GB300)
+  float thresh, est, prev_est, alpha, beta;
   float wgam[kMaxWarmDirs];   // projected / learned start: the mesh's coefficients
   int active, restart, stalls, iterations, applies, status, converged, pad;
   int best_buf;  // which kept iterate (v_keep) has the smallest true residual

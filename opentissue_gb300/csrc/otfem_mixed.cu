@@ -2224,7 +2224,7 @@ struct FinBatchInit {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
     BatchMesh& b = a.bm[m];
     b.bnorm2 = t[0];
-    b.thresh = a.rtol * a.rtol * t[0];
+    b.thresh = float(a.rtol * a.rtol * t[0]);
   }
 };
 
@@ -2239,8 +2239,9 @@ struct FinBatchGram {
 struct FinBatchStart {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
     BatchMesh& b = a.bm[m];
-    b.rho = b.rho0 = b.best_true = b.est = t[0];
-    b.prev_est = -1.0;
+    b.rho = b.rho0 = b.best_true = t[0];
+    b.est = float(t[0]);
+    b.prev_est = -1.f;
     b.restart = b.stalls = b.iterations = 0;
     b.best_buf = 0;
     b.stalled = 0;
@@ -2265,18 +2266,23 @@ struct FinBatchIter {
     mk[kMaskUpdate * M + m] = 0;
     mk[kMaskRefresh * M + m] = 0;
     if (!mk[kMaskApply * M + m]) return;
-    double o[5];
-    pcg_scalars(t, b.prev_est, b.restart != 0, o);
-    if (o[3] != 0.0) {
+    // the scalar step of k_cg_mixed (FinPcgF), on the totals as (hi, lo) pairs
+    DF td[7];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) td[k] = df_of(t[k]);
+    float o[5];
+    FinPcgF{b.prev_est, b.restart != 0}(td, o);
+    if (o[3] != 0.f) {
       // 1: NaN/Inf in this mesh's system (an error); 2: finite breakdown
-      if (o[3] == 1.0) b.status = OTFEM_ERR_NONFINITE;
+      if (o[3] == 1.f) b.status = OTFEM_ERR_NONFINITE;
       b.active = 0;
       mk[kMaskApply * M + m] = 0;
       return;
     }
     b.alpha = o[0];
     b.beta = o[1];
-    b.est = b.rho = o[2];
+    b.est = o[2];
+    b.rho = dfbits::widen(o[2]);
     b.prev_est = o[4];
     b.restart = 0;
     ++b.iterations;
@@ -2305,7 +2311,7 @@ struct FinBatchRefresh {
     const int M = a.num_meshes;
     if (mk[kMaskRefresh * M + m]) {
       b.restart = t[0] > 4.0 * b.est;
-      b.prev_est = -1.0;
+      b.prev_est = -1.f;
       b.rho = t[0];
       const bool periodic = a.refresh <= 0 || b.iterations % a.refresh == 0;
       if (t[0] < b.best_true) {
@@ -2332,6 +2338,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   const int N = a.N, M = a.num_meshes;
   const float scale = float(a.dt * a.dt);
   const DF dt_pair = df_of(a.dt);
+  const DF damp_pair = df_add(DF{1.f, 0.f}, df_mul2(dt_pair, df_of(a.alpha)));  // 1 + dt alpha
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   unsigned round = 0;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2367,27 +2374,34 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           df_inc(g[1].hi, g[1].lo, f.y);
           df_inc(g[2].hi, g[2].lo, f.z);
         }
+        // in (hi, lo) pairs: no FP64 instruction
         const bool fx = a.fixed[i] != 0;
-        const double mass = a.mass[i];
-        double vi[3] = {a.v[3 * i], a.v[3 * i + 1], a.v[3 * i + 2]};
+        const DF mass = df_of(a.mass[i]);
+        const DF vi[3] = {df_of(a.v[3 * i]), df_of(a.v[3 * i + 1]), df_of(a.v[3 * i + 2])};
         float sp = 0.f;
         if (!fx) {
-          double b3[3];
-          for (int c = 0; c < 3; ++c)
-            b3[c] = mass * vi[c] + a.dt * (a.fext[3 * i + c] - (double(g[c].hi) + double(g[c].lo)));
-          for (int c = 0; c < 3; ++c) a.bvec[3 * i + c] = b3[c];
-          const float bf[3] = {float(b3[0]), float(b3[1]), float(b3[2])};
+          DF b3[3];
+          for (int c = 0; c < 3; ++c) {
+            b3[c] = df_add(df_mul2(mass, vi[c]), df_mul2(dt_pair, df_add(df_of(a.fext[3 * i + c]), df_neg(g[c]))));
+            a.bvec[3 * i + c] = f64_of(b3[c]);
+          }
+          a.b_hi[i] = make_float4(b3[0].hi, b3[1].hi, b3[2].hi, 0.f);
+          a.b_lo[i] = make_float4(b3[0].lo, b3[1].lo, b3[2].lo, 0.f);
+          const float bf[3] = {b3[0].hi + b3[0].lo, b3[1].hi + b3[1].lo, b3[2].hi + b3[2].lo};
           bb[0] = bf[0] * bf[0] + bf[1] * bf[1] + bf[2] * bf[2];
-          const double dg = mass + a.dt * (a.alpha * mass);
-          a.diag[i] = dg;
-          a.diag_f[i] = float(dg);
-          sp = float(jacobi_scale(a, i, dg));
+          const DF dg = df_mul2(mass, damp_pair);  // m (1 + dt alpha)
+          a.diag[i] = f64_of(dg);
+          a.diag_f[i] = dg.hi;
+          a.diag_lo[i] = dg.lo;
+          sp = a.precond ? 1.f / (dg.hi + scale * dfbits::trunc_f32(a.node_k[i])) : 1.f;
         } else {
           a.diag[i] = 0.0;
           a.diag_f[i] = 0.f;
+          a.diag_lo[i] = 0.f;
         }
         a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
-        store_operand(a.v_f, a.v_lo, i, vi[0], vi[1], vi[2], fx ? 0.0 : 1.0);
+        a.v_f[i] = make_float4(vi[0].hi, vi[1].hi, vi[2].hi, fx ? 0.f : 1.f);
+        a.v_lo[i] = make_float4(vi[0].lo, vi[1].lo, vi[2].lo, 0.f);
         a.q_f[i] = zero4;
         if (a.nwarm) {
           // learned start: the network's correction is the last search direction
@@ -2422,13 +2436,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     for (long i = nr.beg + lane; i < nr.end; i += 32) {
       if (a.fixed[i]) continue;
       const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-      const double dg = a.diag[i];
       float rf[3];
-      rf[0] = float(a.bvec[3 * i] - (dg * (double(vh.x) + double(vl.x)) + double(q4.x)));
-      rf[1] = float(a.bvec[3 * i + 1] - (dg * (double(vh.y) + double(vl.y)) + double(q4.y)));
-      rf[2] = float(a.bvec[3 * i + 2] - (dg * (double(vh.z) + double(vl.z)) + double(q4.z)));
+      node_residual(a, i, vh, vl, q4, rf);
       a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-      const float df = float(dg);
+      const float df = a.diag_f[i];
       for (int j = 0; j < nw; ++j) {
         const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
         a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
@@ -2509,10 +2520,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             a.v_lo[i] = vl;
           } else {
             const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-            const double d = a.diag[i];
-            rf[0] = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-            rf[1] = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-            rf[2] = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+            node_residual(a, i, vh, vl, q4, rf);
           }
           a.r_f[i] = make_float4(rf[0], rf[1], rf[2], sp);
           a.p_f[i] = make_float4(sp * rf[0], sp * rf[1], sp * rf[2], 1.f);  // p = z = S r
@@ -2570,7 +2578,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     for (long i = nr.beg + lane; i < nr.end; i += 32) {
       const int m = a.mesh_of_node[i];
       if (!mask_update[m] || a.fixed[i]) continue;
-      const float alpha = float(a.bm[m].alpha), beta = float(a.bm[m].beta);
+      const float alpha = a.bm[m].alpha, beta = a.bm[m].beta;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
       const float d = a.diag_f[i];
@@ -2603,10 +2611,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           m = a.mesh_of_node[i];
           if (mask_refresh[m] && !a.fixed[i]) {
             const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
-            const double d = a.diag[i];
-            const float rx = float(a.bvec[3 * i] - (d * (double(vh.x) + double(vl.x)) + double(q4.x)));
-            const float ry = float(a.bvec[3 * i + 1] - (d * (double(vh.y) + double(vl.y)) + double(q4.y)));
-            const float rz = float(a.bvec[3 * i + 2] - (d * (double(vh.z) + double(vl.z)) + double(q4.z)));
+            float rr3[3];
+            node_residual(a, i, vh, vl, q4, rr3);
+            const float rx = rr3[0], ry = rr3[1], rz = rr3[2];
             a.r_f[i] = make_float4(rx, ry, rz, a.r_f[i].w);
             a.q_f[i] = zero4;
             const long cand = 2L * (a.bm[m].best_buf ^ 1) * N;  // the kept copy that is not the best
