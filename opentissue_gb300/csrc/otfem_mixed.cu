@@ -1566,6 +1566,85 @@ __device__ __forceinline__ void trace_row(const MixedArgs& a, int row, double rh
   tr[9] = double(cycles_now() - t_start);
 }
 
+// The elastic forces g of node i: its incident tets' corner forces in
+// ascending tet order, summed as (hi, lo) pairs.  The incidence entries and
+// then the forces are loaded eight at a time ahead of the sums, so that a
+// node's ~24 dependent gathers overlap instead of queuing one L2 round trip
+// after the other.
+__device__ __forceinline__ void gather_forces(const MixedArgs& a, long i, DF (&g)[3]) {
+  const int q0 = a.inc_ptr[i], q1 = a.inc_ptr[i + 1];
+  for (int c = 0; c < 3; ++c) g[c] = DF{0.f, 0.f};
+  for (int q = q0; q < q1; q += 8) {
+    int e[8];
+    float4 f[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) e[k] = q + k < q1 ? a.inc_ent[q + k] : -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) f[k] = e[k] >= 0 ? a.g_f[4L * (e[k] >> 2) + (e[k] & 3)] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (e[k] < 0) break;
+      df_inc(g[0].hi, g[0].lo, f[k].x);
+      df_inc(g[1].hi, g[1].lo, f[k].y);
+      df_inc(g[2].hi, g[2].lo, f[k].z);
+    }
+  }
+}
+
+// A W_j += diag W_j (the mass term) for the search directions of node i, four
+// directions at a time: their loads are issued ahead of the stores (which the
+// compiler may not move across, not knowing that they touch other
+// directions), so they overlap.
+__device__ __forceinline__ void add_mass_term(const MixedArgs& a, long i, float df) {
+  const long N = a.N;
+  for (int j0 = 0; j0 < a.nwarm; j0 += 4) {
+    float4 w[4], aw[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k < a.nwarm) {
+        w[k] = warm_dir(a, j0 + k)[i];
+        aw[k] = load_acc(a.wprod + size_t(j0 + k) * N + i);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k < a.nwarm)
+        a.wprod[size_t(j0 + k) * N + i] =
+            make_float4(df * w[k].x + aw[k].x, df * w[k].y + aw[k].y, df * w[k].z + aw[k].z, 0.f);
+    }
+  }
+}
+
+// The start v + sum_j g_j W_j (two-sums into the (hi, lo) iterate) and its
+// residual r - sum_j g_j A W_j at node i, directions in order, four loaded at
+// a time.
+__device__ __forceinline__ void move_to_start(const MixedArgs& a, long i, const float* gam, float4& vh, float4& vl,
+                                              float (&rf)[3]) {
+  const long N = a.N;
+  for (int j0 = 0; j0 < a.nwarm; j0 += 4) {
+    float4 w[4], aw[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k < a.nwarm && gam[j0 + k] != 0.f) {
+        w[k] = warm_dir(a, j0 + k)[i];
+        aw[k] = a.wprod[size_t(j0 + k) * N + i];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k >= a.nwarm) break;
+      const float g = gam[j0 + k];
+      if (g == 0.f) continue;
+      df_inc(vh.x, vl.x, g * w[k].x);
+      df_inc(vh.y, vl.y, g * w[k].y);
+      df_inc(vh.z, vl.z, g * w[k].z);
+      rf[0] -= g * aw[k].x;
+      rf[1] -= g * aw[k].y;
+      rf[2] -= g * aw[k].z;
+    }
+  }
+}
+
 // The velocity-change history as a difference basis: D_0 = the newest change,
 // D_j = the j-th backward difference of the last changes (new D_j = new
 // D_{j-1} - old D_{j-1}), kept as (hi, lo) float pairs.  The basis spans the
@@ -1579,16 +1658,29 @@ __device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long 
     hi[c] = dv[c].hi;
     lo[c] = dv[c].lo;
   }
-  for (int j = 0; j < a.hist_rec; ++j) {
-    const float4 oh = a.hist[size_t(j) * N + i], ol = a.hist[size_t(kMaxHistory + j) * N + i];
-    a.hist[size_t(j) * N + i] = make_float4(hi[0], hi[1], hi[2], 1.f);
-    a.hist[size_t(kMaxHistory + j) * N + i] = make_float4(lo[0], lo[1], lo[2], 0.f);
-    // next level: this level's new value minus its old one
-    const float ohc[3] = {oh.x, oh.y, oh.z}, olc[3] = {ol.x, ol.y, ol.z};
-    for (int c = 0; c < 3; ++c) {
-      const DF d = df_add(DF{hi[c], lo[c]}, DF{-ohc[c], -olc[c]});
-      hi[c] = d.hi;
-      lo[c] = d.lo;
+  // four levels at a time: their old values are loaded before any is
+  // overwritten, so the loads overlap
+  for (int j0 = 0; j0 < a.hist_rec; j0 += 4) {
+    float4 oh[4], ol[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k < a.hist_rec) {
+        oh[k] = a.hist[size_t(j0 + k) * N + i];
+        ol[k] = a.hist[size_t(kMaxHistory + j0 + k) * N + i];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k >= a.hist_rec) break;
+      a.hist[size_t(j0 + k) * N + i] = make_float4(hi[0], hi[1], hi[2], 1.f);
+      a.hist[size_t(kMaxHistory + j0 + k) * N + i] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      // next level: this level's new value minus its old one
+      const float ohc[3] = {oh[k].x, oh[k].y, oh[k].z}, olc[3] = {ol[k].x, ol[k].y, ol[k].z};
+      for (int c = 0; c < 3; ++c) {
+        const DF d = df_add(DF{hi[c], lo[c]}, DF{-ohc[c], -olc[c]});
+        hi[c] = d.hi;
+        lo[c] = d.lo;
+      }
     }
   }
 }
@@ -1639,14 +1731,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // M(1 + dt*alpha) of fem_dynamics_assembly.h:84-85; v split into (hi, lo).
   DF bbsum[1] = {{0.f, 0.f}};
   for (long i = n0; i < N; i += gstride) {
-    DF g[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
-      int e = a.inc_ent[q];
-      float4 f = a.g_f[4L * (e >> 2) + (e & 3)];
-      df_inc(g[0].hi, g[0].lo, f.x);
-      df_inc(g[1].hi, g[1].lo, f.y);
-      df_inc(g[2].hi, g[2].lo, f.z);
-    }
+    DF g[3];
+    gather_forces(a, i, g);
     // in (hi, lo) pairs: no FP64 instruction
     const bool fx = a.fixed[i] != 0;
     const DF m = df_of(a.mass[i]);
@@ -1721,11 +1807,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       float rf[3];
       node_residual(a, i, vh, vl, q4, rf);
       a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-      const float df = a.diag_f[i];
-      for (int j = 0; j < nw; ++j) {
-        const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
-        a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
-      }
+      add_mass_term(a, i, a.diag_f[i]);
     }
     // Gram system: W_i.A W_j (i <= j) row by row, then W_i.r
     __shared__ signed char s_pi[kMaxWarmSums], s_pj[kMaxWarmSums];
@@ -1766,17 +1848,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
       rf[0] = r4.x;
       rf[1] = r4.y;
       rf[2] = r4.z;
-      for (int j = 0; j < a.nwarm; ++j) {
-        const float g = s_gam[j];
-        if (g == 0.f) continue;
-        const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
-        df_inc(vh.x, vl.x, g * w.x);
-        df_inc(vh.y, vl.y, g * w.y);
-        df_inc(vh.z, vl.z, g * w.z);
-        rf[0] -= g * aw.x;
-        rf[1] -= g * aw.y;
-        rf[2] -= g * aw.z;
-      }
+      move_to_start(a, i, s_gam, vh, vl, rf);
       a.v_f[i] = vh;
       a.v_lo[i] = vl;
     } else {
@@ -2366,14 +2438,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       float bb[1] = {0.f};
       if (valid) {
         m = a.mesh_of_node[i];
-        DF g[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        for (int q = a.inc_ptr[i]; q < a.inc_ptr[i + 1]; ++q) {
-          int e = a.inc_ent[q];
-          float4 f = a.g_f[4L * (e >> 2) + (e & 3)];
-          df_inc(g[0].hi, g[0].lo, f.x);
-          df_inc(g[1].hi, g[1].lo, f.y);
-          df_inc(g[2].hi, g[2].lo, f.z);
-        }
+        DF g[3];
+        gather_forces(a, i, g);
         // in (hi, lo) pairs: no FP64 instruction
         const bool fx = a.fixed[i] != 0;
         const DF mass = df_of(a.mass[i]);
@@ -2439,11 +2505,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       float rf[3];
       node_residual(a, i, vh, vl, q4, rf);
       a.r_f[i] = make_float4(rf[0], rf[1], rf[2], a.r_f[i].w);
-      const float df = a.diag_f[i];
-      for (int j = 0; j < nw; ++j) {
-        const float4 w = warm_dir(a, j)[i], aw = load_acc(a.wprod + size_t(j) * N + i);
-        a.wprod[size_t(j) * N + i] = make_float4(df * w.x + aw.x, df * w.y + aw.y, df * w.z + aw.z, 0.f);
-      }
+      add_mass_term(a, i, a.diag_f[i]);
     }
     // per-mesh Gram systems, in chunks of 8 sums: W_i.A W_j (i <= j), then W_i.r
     __shared__ signed char s_pi[kMaxWarmSums], s_pj[kMaxWarmSums];
@@ -2504,18 +2566,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
             rf[0] = r4.x;
             rf[1] = r4.y;
             rf[2] = r4.z;
-            const float* gam = a.bm[m].wgam;
-            for (int j = 0; j < a.nwarm; ++j) {
-              const float g = gam[j];
-              if (g == 0.f) continue;
-              const float4 w = warm_dir(a, j)[i], aw = a.wprod[size_t(j) * N + i];
-              df_inc(vh.x, vl.x, g * w.x);
-              df_inc(vh.y, vl.y, g * w.y);
-              df_inc(vh.z, vl.z, g * w.z);
-              rf[0] -= g * aw.x;
-              rf[1] -= g * aw.y;
-              rf[2] -= g * aw.z;
-            }
+            move_to_start(a, i, a.bm[m].wgam, vh, vl, rf);
             a.v_f[i] = vh;
             a.v_lo[i] = vl;
           } else {
