@@ -59,7 +59,7 @@ void free_all(Context& c) {
                   c.residual, c.node_dots, c.scal, c.Ke, c.Re, c.V, c.E, c.Bv, c.D, c.plastic,
                   c.young, c.poisson, c.density, c.yield, c.creep, c.cmax, c.tet_force, c.elastic_force, c.inc_ptr,
                   c.inc_ent, c.row_ptr, c.cols, c.bc_ptr, c.bc_ent, c.K, c.A, c.re_f, c.b_f, c.c_f, c.tile_f,
-                  c.re_d, c.b_d, c.c_d, c.diag, c.diag_f, c.diag_lo, c.b_hi, c.b_lo, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.v_keep, c.features, c.q_d,
+                  c.re_d, c.b_d, c.c_d, c.e0_f, c.diag, c.diag_f, c.diag_lo, c.b_hi, c.b_lo, c.node_k, c.r, c.p, c.bvec, c.p_f, c.v_f, c.q_f, c.p_lo, c.v_lo, c.r_f, c.g_f, c.dv_last, c.warm_dv, c.warm_tmp, c.v_keep, c.features, c.q_d,
                   c.p_d4, c.v_d4, c.partials, c.sync, c.trace, c.stats, c.patch_node_ptr, c.patch_nodes, c.lconn,
                   c.patch_inc_ptr, c.patch_inc};
   for (void* p : ptrs)
@@ -287,6 +287,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.re_f, 9 * T);
   OT_ALLOC(c.b_f, 9 * T);
   OT_ALLOC(c.c_f, 3 * T);
+  OT_ALLOC(c.e0_f, 9 * T);
   OT_ALLOC(c.re_d, 9 * T);
   OT_ALLOC(c.b_d, 9 * T);
   OT_ALLOC(c.c_d, 3 * T);
@@ -560,6 +561,8 @@ static int transfer(otfem_handle h, int field, double* ptr, int64_t count, bool 
   size_t bytes = sizeof(double) * size_t(count);
   if (to_device) {
     OT_CUDA(cudaMemcpyAsync(d, ptr, bytes, kind, c.stream));
+    // the mixed solver's rest edges follow the model coordinates
+    if (field == OTFEM_MODEL_COORD) OT_CUDA(otfem::mixed_rest_edges(c));
   } else {
     OT_CUDA(cudaMemcpyAsync(ptr, d, bytes, kind, c.stream));
     if (kind == cudaMemcpyDeviceToHost) OT_CUDA(cudaStreamSynchronize(c.stream));
@@ -697,6 +700,7 @@ int otfem_update_original_coord(otfem_handle h) {
   if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
   Context& c = h->c;
   if (c.N) OT_CUDA(cudaMemcpyAsync(c.x0, c.x, sizeof(double) * 3 * size_t(c.N), cudaMemcpyDeviceToDevice, c.stream));
+  OT_CUDA(otfem::mixed_rest_edges(c));
   return OTFEM_OK;
 }
 

@@ -123,6 +123,7 @@ struct Context {
 
   // matrix-free data
   float *re_f = nullptr, *b_f = nullptr, *c_f = nullptr;  // 9T, 9T, 3T
+  float* e0_f = nullptr;                                  // 9T: rest edges x0_k - x0_0 (k_rest_edges)
   double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
   double* diag = nullptr;                                 // N: m(1+dt*alpha)
   float* diag_f = nullptr;                                // N: the same as (hi, lo) FP32 pairs
@@ -228,6 +229,7 @@ cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
 
 // ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
 cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
+cudaError_t mixed_rest_edges(Context& c);  // the FP32 rest edges from the model coordinates
 // Tile size of the staged apply for the persistent grid (sets tile_tets and
 // num_tiles): tiles of at most kTileMaxTets tets, as even a share of the
 // tets per CTA as a multiple of 16 allows.

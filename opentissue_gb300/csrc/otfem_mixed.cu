@@ -2731,23 +2731,28 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
 // Gram-Schmidt orthonormalises exactly as the reference's F (a positive
 // multiple of it) would be.
 __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets, const double* __restrict__ x,
-                                 const double* __restrict__ x0, const float* __restrict__ b_f,
+                                 const float* __restrict__ e0_f, const float* __restrict__ b_f,
                                  const float* __restrict__ c_f, float* re_f, float4* g_f, float* tile_f,
                                  int tile_tets) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   int4 n = tets[t];
   const int nn[4] = {n.x, n.y, n.z, n.w};
+  // current edges x_k - x_0 from the positions as (hi, lo) pairs (integer
+  // instructions; the high parts of nearby nodes subtract exactly), rest
+  // edges precomputed (k_rest_edges)
   float ep[3][3], e0[3][3];
   {
-    double p0[3] = {x[3 * nn[0]], x[3 * nn[0] + 1], x[3 * nn[0] + 2]};
-    double m0[3] = {x0[3 * nn[0]], x0[3 * nn[0] + 1], x0[3 * nn[0] + 2]};
+    DF p0[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p0[c] = df_of(x[3 * nn[0] + c]);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        ep[k][c] = float(x[3 * nn[k + 1] + c] - p0[c]);
-        e0[k][c] = float(x0[3 * nn[k + 1] + c] - m0[c]);
+        const DF pk = df_of(x[3 * nn[k + 1] + c]);
+        ep[k][c] = (pk.hi - p0[c].hi) + (pk.lo - p0[c].lo);
+        e0[k][c] = e0_f[long(3 * k + c) * T + t];
       }
   }
   float b[9];
@@ -2931,6 +2936,18 @@ __global__ void k_prepare(int T, const int4* __restrict__ tets, const double* __
   tile_f[tile_word(tile_tets, t, 5)] = 0.f;
   tile_f[tile_word(tile_tets, t, 6)] = 0.f;
   tile_f[tile_word(tile_tets, t, 7)] = 1.f;
+}
+
+// Rest-frame edges x0_k - x0_0 of every tet (k = 1..3), FP32 (SoA 9 x T):
+// the orientation kernel's rest term, recomputed whenever the model
+// coordinates change.
+__global__ void k_rest_edges(int T, const int4* __restrict__ tets, const double* __restrict__ x0, float* e0_f) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int4 n = tets[t];
+  const int nn[4] = {n.x, n.y, n.z, n.w};
+  for (int k = 0; k < 3; ++k)
+    for (int c = 0; c < 3; ++c) e0_f[long(3 * k + c) * T + t] = float(x0[3 * nn[k + 1] + c] - x0[3 * nn[0] + c]);
 }
 
 // Node stiffness scale of the Jacobi preconditioner: k_i = sum over the
@@ -3146,8 +3163,15 @@ cudaError_t mixed_prepare(Context& c) {
   k_prepare<<<nb, 256, 0, c.stream>>>(c.T, c.tets, c.Bv, c.D, c.V, c.b_f, c.c_f, c.b_d, c.c_d, c.tile_f,
                                       c.tile_tets);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = mixed_rest_edges(c)) != cudaSuccess) return e;
   const int nn = c.N > 0 ? (c.N + 255) / 256 : 1;
   k_node_stiffness<<<nn, 256, 0, c.stream>>>(c.N, c.T, c.inc_ptr, c.inc_ent, c.Bv, c.c_d, c.node_k);
+  return cudaGetLastError();
+}
+
+cudaError_t mixed_rest_edges(Context& c) {
+  if (c.T == 0) return cudaSuccess;
+  k_rest_edges<<<(c.T + 255) / 256, 256, 0, c.stream>>>(c.T, c.tets, c.x0, c.e0_f);
   return cudaGetLastError();
 }
 
@@ -3161,7 +3185,7 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
     c.re_f32_pending = false;
     c.quat_in_g_f = false;
   } else {
-    k_orient_rhs_f32<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.x0, c.b_f, c.c_f, c.re_f,
+    k_orient_rhs_f32<<<nb, 256, 0, c.stream>>>(c.T, warp ? 1 : 0, c.tets, c.x, c.e0_f, c.b_f, c.c_f, c.re_f,
                                                c.g_f, c.tile_f, c.tile_tets);
     c.re_f32_pending = true;
     c.quat_in_g_f = true;
