@@ -35,11 +35,11 @@ constexpr int kTraceCols = 10;
 // contend with the CTAs polling `gen`.
 struct DeviceSync {
   unsigned int count;        // monotonic arrival counter
-  unsigned int pad0[31];
+  int status;                // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code; next to the
+                             // counter, so that one 8-byte load polls both
+  unsigned int pad0[30];
   unsigned int gen;          // number of completed barriers (written by the last arrival)
   unsigned int pad1[31];
-  int status;                // 0 = OK, else an OTFEM_ERR_* / OTFEM_WARN_* code
-  int pad2[31];
   double result[2][8];       // grid-sum results, double-buffered by barrier parity
   double pad3[16];
   double acc[3][8][kAccStride];  // grid-sum accumulators (FP64 reductions): three rotating

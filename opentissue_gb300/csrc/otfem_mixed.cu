@@ -319,19 +319,22 @@ __device__ __forceinline__ void release_round(DeviceSync* s, unsigned round) {
 // counter with release semantics and polls the counter itself (acquire) until
 // all gridDim.x arrivals of the round are in: one L2 round trip fewer than a
 // last-arriver release (measured on GB300 with 304 CTAs: 2,900 against 3,700
-// SM cycles per barrier).  The status word is read before arriving; a CTA
-// that finds an error leaves without arriving, and the others notice the
-// error while they wait or at their next synchronisation.  The first CTA
-// clears the stale accumulator set once the round is complete; its next
-// arrival (a release) publishes the clear before any CTA can pass round + 1.
+// SM cycles per barrier).  The status word sits next to the counter and every
+// poll reads both, so an error recorded anywhere ends the wait (a CTA that
+// stopped arriving leaves the others waiting only until they see its error),
+// and no separate status read precedes the arrival.  The first CTA clears
+// the stale accumulator set once the round is complete; its next arrival (a
+// release) publishes the clear before any CTA can pass round + 1.
 __device__ __forceinline__ bool sync_round(DeviceSync* s, unsigned round, long long spin_limit) {
-  if (ld_status(&s->status) != 0) return false;
   red_add_release(&s->count, 1u);
   const unsigned target = round * gridDim.x;
-  long long start = clock64();
-  unsigned polls = 0;
-  while (int(ld_acquire(&s->count) - target) < 0) {
-    if ((++polls & 63u) == 0u && ld_status(&s->status) != 0) return false;
+  const long long start = clock64();
+  for (;;) {
+    // the counter and the status word in one acquire load
+    unsigned long long w;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(&s->count) : "memory");
+    if (unsigned(w >> 32) != 0u) return false;
+    if (int(unsigned(w) - target) >= 0) break;
     if (clock64() - start > spin_limit) {
       atomicCAS(&s->status, 0, OTFEM_ERR_TIMEOUT);
       return false;
@@ -549,9 +552,9 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
     return good;
   }
   if (threadIdx.x == 0) {
-    // 2: last CTA, 1: wait for the release, 0: an error is recorded
-    if (ld_status(&a.sync->status) != 0) s_flag = 0;
-    else s_flag = arrive(a.sync, round) ? 2 : 1;
+    // 2: last CTA, 1: wait for the release (0 once the wait failed); an
+    // error recorded earlier ends the wait or the next synchronisation
+    s_flag = arrive(a.sync, round) ? 2 : 1;
   }
   __syncthreads();
   if (s_flag == 2) {
@@ -2255,9 +2258,9 @@ __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (
   const int half = int(round & 1u);
   __syncthreads();
   if (threadIdx.x == 0) {
-    // 2: last CTA, 1: wait for the release, 0: an error is recorded
-    if (ld_status(&a.sync->status) != 0) s_flag = 0;
-    else s_flag = arrive(a.sync, round) ? 2 : 1;
+    // 2: last CTA, 1: wait for the release (0 once the wait failed); an
+    // error recorded earlier ends the wait or the next synchronisation
+    s_flag = arrive(a.sync, round) ? 2 : 1;
   }
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0;
   __syncthreads();
