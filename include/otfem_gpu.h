@@ -319,6 +319,12 @@ OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt
  * handle's stream: the stiffness apply alone, for timing.  Leaves the solver
  * state unspecified until the next step. */
 OTFEM_API int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t sweeps);
+/* Runs the grid barrier's bounded wait once with nothing to release it (one
+ * CTA waits for a second arrival that never comes) and a limit of `cycles` SM
+ * clock cycles, and reports the status the wait recorded: OTFEM_ERR_TIMEOUT.
+ * A diagnostic of the timeout path every device-side wait takes; the handle
+ * stays usable.  Not during a captured step. */
+OTFEM_API int otfem_check_wait_timeout(otfem_handle h, int64_t cycles, int32_t* status);
 /* Convergence history of the last matrix-free step, one row of 10 doubles per
  * CG iteration (at most 256 rows): the squared residual norm (its estimate)
  * before the iteration, p.Ap (0 where the solver does not form it), alpha,

@@ -123,6 +123,7 @@ SIGNATURES = {
     "otfem_apply_sweeps": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_int32]),
     "otfem_solver_trace": (ctypes.c_int, [_h, _dp, ctypes.c_int32, _i32p]),
     "otfem_solver_phases": (ctypes.c_int, [_h, _dp]),
+    "otfem_check_wait_timeout": (ctypes.c_int, [_h, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]),
     "otfem_surface_bind": (ctypes.c_int, [_h, _dp, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), _i64p]),
     "otfem_surface_update": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int64]),
     "otfem_surface_update_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),

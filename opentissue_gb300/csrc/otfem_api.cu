@@ -813,6 +813,15 @@ int otfem_apply_sweeps(otfem_handle h, int solver, double dt, int32_t sweeps) {
   return OTFEM_OK;
 }
 
+int otfem_check_wait_timeout(otfem_handle h, int64_t cycles, int32_t* status) {
+  if (!h || !status || cycles <= 0) return fail(OTFEM_ERR_INVALID_ARGUMENT, "bad argument");
+  int st = 0;
+  cudaError_t e = otfem::check_wait_timeout(h->c, static_cast<long long>(cycles), &st);
+  if (e != cudaSuccess) return cuda_fail(e, "wait timeout check");
+  *status = st;
+  return OTFEM_OK;
+}
+
 int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows) {
   if (!h || !rows || (!out && max_rows > 0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   Context& c = h->c;

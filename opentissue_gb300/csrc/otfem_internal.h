@@ -230,6 +230,7 @@ cudaError_t launch_export_k_counts(Context& c, int* row_cnt);
 // ---- matrix-free solver (otfem_mixed.cu) ----------------------------------
 cudaError_t mixed_prepare(Context& c);  // FP32/FP64 per-tet operands from init data
 cudaError_t mixed_rest_edges(Context& c);  // the FP32 rest edges from the model coordinates
+cudaError_t check_wait_timeout(Context& c, long long cycles, int* status);  // the barrier's timeout path
 // Tile size of the staged apply for the persistent grid (sets tile_tets and
 // num_tiles): tiles of at most kTileMaxTets tets, as even a share of the
 // tets per CTA as a multiple of 16 allows.

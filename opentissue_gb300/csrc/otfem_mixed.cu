@@ -2941,6 +2941,15 @@ __global__ void k_prepare(int T, const int4* __restrict__ tets, const double* __
   tile_f[tile_word(tile_tets, t, 7)] = 1.f;
 }
 
+// The timeout path of the grid barrier: one CTA arrives at a round that two
+// arrivals complete, so the wait runs until its limit, records
+// OTFEM_ERR_TIMEOUT and returns; the kernel then reports the status.
+__global__ void k_wait_timeout(DeviceSync* sync, long long limit, int* status_out) {
+  if (threadIdx.x != 0) return;
+  const bool ok = sync_round(sync, 2u, limit);  // gridDim.x == 1: two arrivals never come
+  *status_out = ok ? 0 : ld_status(&sync->status);
+}
+
 // Rest-frame edges x0_k - x0_0 of every tet (k = 1..3), FP32 (SoA 9 x T):
 // the orientation kernel's rest term, recomputed whenever the model
 // coordinates change.
@@ -3170,6 +3179,21 @@ cudaError_t mixed_prepare(Context& c) {
   const int nn = c.N > 0 ? (c.N + 255) / 256 : 1;
   k_node_stiffness<<<nn, 256, 0, c.stream>>>(c.N, c.T, c.inc_ptr, c.inc_ent, c.Bv, c.c_d, c.node_k);
   return cudaGetLastError();
+}
+
+cudaError_t check_wait_timeout(Context& c, long long cycles, int* status) {
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream);
+  if (e == cudaSuccess) {
+    k_wait_timeout<<<1, 32, 0, c.stream>>>(c.sync, cycles, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status, d, sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c.sync, 0, sizeof(DeviceSync), c.stream);
+  if (d) cudaFree(d);
+  return e;
 }
 
 cudaError_t mixed_rest_edges(Context& c) {

@@ -3,6 +3,8 @@ reference's relative-residual runs.  Tolerance from the target: position
 error below 1e-5 relative to the FP64 oracle, measured here against the
 largest displacement of the step (stricter than relative to the positions),
 true relative residual <= rtol = 1e-6."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -159,6 +161,22 @@ def test_nonfinite_force_reports_error_and_context_recovers(gpu):
     m.set(capi.F_EXTERNAL, f)
     rc, st = m.step(0.01, True, mixed())
     assert rc == capi.OK and st.rel_residual <= 1e-6
+
+
+def test_device_wait_times_out_and_context_recovers(gpu):
+    """The grid barrier's bounded wait, with nothing to release it (one CTA
+    waits for a second arrival), gives up after its limit and records
+    OTFEM_ERR_TIMEOUT; the kernel returns and the handle keeps working."""
+    tets, coord, fixed = beam(4, 2, 2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    st = ctypes.c_int32(0)
+    capi.check(m.lib.otfem_check_wait_timeout(m.h, 4_000_000, ctypes.byref(st)))  # ~2 ms of SM cycles
+    assert st.value == capi.ERR_TIMEOUT
+    assert m.lib.otfem_check_wait_timeout(m.h, 0, ctypes.byref(st)) == capi.ERR_INVALID_ARGUMENT
+    m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
+    rc, stats = m.step(0.01, True, mixed())
+    assert rc == capi.OK and stats.rel_residual <= 1e-6
 
 
 def test_iteration_cap_is_a_warning(gpu):
