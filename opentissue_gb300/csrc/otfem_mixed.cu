@@ -754,13 +754,7 @@ __device__ __forceinline__ void pcg_scalars(const double* t, double prev_est, bo
   o[3] = flag;
   o[4] = est_z;
 }
-struct FinPcg {
-  double prev_est;
-  bool restart;
-  __device__ void operator()(const double* t, double* o) const { pcg_scalars(t, prev_est, restart, o); }
-};
-
-// The same for the FP64 solver, whose exact r.z (t_rz) and r.r come from the
+// The FP64 solver's scalar step, whose exact r.z (t_rz) and r.r come from the
 // grid sum after the vector update: totals p.q, z.q, q.Sq, r.q, q.q; outputs
 // alpha, beta, the r'.r' estimate, flag.
 struct FinPcgFp64 {
@@ -1873,7 +1867,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   int best_buf = 0;      // kept iterate with the smallest true residual
   bool stalled = false;  // stopped at the precision floor: return the kept iterate
   bool converged = rho <= thresh;
-  // recurrence check and restarts (FinPcg); stagnation of the
+  // recurrence check and restarts (FinPcgF); stagnation of the
   // true residual at the refreshes ends the solve unconverged
   float prev_est = -1.f, best_true = rho0;
   bool restart = false;
@@ -1886,7 +1880,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
-    // q = diag p + q; the totals of FinPcg (r.w = the node's scalar s)
+    // q = diag p + q; the totals of FinPcgF (r.w = the node's scalar s)
     DF s7[7] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     for (long i = n0; i < N; i += gstride) {
       if (a.fixed[i]) continue;
@@ -2332,7 +2326,7 @@ struct FinBatchStart {
   }
 };
 
-// totals: those of FinPcg for the meshes in the sweep
+// totals: those of FinPcgF for the meshes in the sweep
 struct FinBatchIter {
   __device__ void operator()(const MixedArgs& a, int m, const double* t, int* cnt) const {
     BatchMesh& b = a.bm[m];
@@ -2597,7 +2591,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_apply);
     ++sweeps;
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
-    // q = diag p + q; the totals of FinPcg per mesh
+    // q = diag p + q; the totals of FinPcgF per mesh
     {
       SegSum<7> ss;
       ss.start(first_mesh);
