@@ -179,6 +179,35 @@ def test_device_wait_times_out_and_context_recovers(gpu):
     assert rc == capi.OK and stats.rel_residual <= 1e-6
 
 
+def test_model_coordinate_changes_follow_the_oracle(gpu, oracle):
+    """The mixed solver's rest edges (a per-tet FP32 table) follow the model
+    coordinates: update_original_coord after step 3 and model coordinates set
+    to a stretched shape after step 6, against the converged FP64 oracle."""
+    tets, coord, fixed = beam(8, 3, 3, jitter_seed=5)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    o = oracle.OracleMesh(tets, coord, coord, fixed)
+    o.init(*MATERIAL)
+    mass = o.get(oracle.MASS)
+    stretched = coord * np.array([1.01, 1.0, 0.995])
+    for s in range(10):
+        f = gravity_force(mass, fixed)
+        m.set(capi.F_EXTERNAL, f)
+        o.set(oracle.F_EXTERNAL, f)
+        m.step(0.01, True, mixed())
+        o.simulate_converged(0.01, True, 2.0, 1e-11, 100000)
+        if s == 2:
+            capi.check(m.lib.otfem_update_original_coord(m.h))
+            o.update_original_coord()
+        if s == 5:
+            m.set(capi.MODEL_COORD, stretched)
+            o.set(oracle.MODEL_COORD, stretched)
+        x, xo = m.get(capi.COORD), o.get(oracle.COORD)
+        assert np.abs(x - xo).max() <= 1e-5 * np.abs(xo - coord).max(), s
+    o.close()
+    m.close()
+
+
 def test_iteration_cap_is_a_warning(gpu):
     tets, coord, fixed = beam(8, 3, 3, jitter_seed=1)
     m = GpuMesh(tets, coord, fixed)
