@@ -1227,6 +1227,17 @@ struct StagedTet {
   __device__ __forceinline__ StagedTet(const float* w, int TT, int tid) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) nn[k] = __float_as_int(w[k * TT + tid]);
+    load_rest(w, TT, tid);
+  }
+  // with the node ids already loaded (the tets variant loads them one tet ahead)
+  __device__ __forceinline__ StagedTet(const float* w, int TT, int tid, const int4& ids) {
+    nn[0] = ids.x;
+    nn[1] = ids.y;
+    nn[2] = ids.z;
+    nn[3] = ids.w;
+    load_rest(w, TT, tid);
+  }
+  __device__ __forceinline__ void load_rest(const float* w, int TT, int tid) {
     quaternion_to_rotation(make_float4(w[4 * TT + tid], w[5 * TT + tid], w[6 * TT + tid], w[7 * TT + tid]), Re);
 #pragma unroll
     for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT + tid];
@@ -1235,6 +1246,14 @@ struct StagedTet {
     c2 = w[19 * TT + tid];
   }
 };
+
+// Node ids of tet t from its tile (words 0..3), or zeros past the end.
+__device__ __forceinline__ int4 tile_node_ids(const MixedArgs& a, int t) {
+  if (t >= a.T) return make_int4(0, 0, 0, 0);
+  const int TT = a.tile_tets, tile = tile_of(t, a.tile_magic);
+  const float* w = a.tile_f + size_t(tile) * kTileWords * TT + (t - tile * TT);
+  return make_int4(__float_as_int(w[0]), __float_as_int(w[TT]), __float_as_int(w[2 * TT]), __float_as_int(w[3 * TT]));
+}
 
 // q += dt^2 K_e u for one tet (FP32; u with an optional lo part).
 __device__ __forceinline__ void tet_apply(const float* Re, const float* b, float c0, float c1, float c2, float scale,
@@ -1267,13 +1286,27 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
 
 // Tets variant in FP32: one tet per thread, grid-stride, its words read
 // straight from the tiles (node ids, quaternion, B-vectors, constants: 80 B).
+// The node ids of the thread's next tet are loaded one tet ahead, so that
+// their L2 round trip overlaps this tet's gathers and arithmetic instead of
+// preceding the next tet's gathers.  In a batch (mask) a tet of a mesh not in
+// the sweep is skipped before anything but its mesh id is loaded.
+__device__ __forceinline__ bool tet_in_sweep(const MixedArgs& a, const unsigned char* mask, int t) {
+  return t < a.T && (!mask || mask[a.mesh_of_tet[t]]);
+}
 __device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
                                  const unsigned char* mask) {
-  const int T = a.T, TT = a.tile_tets;
-  for (int t = int(sweep_first()); t < T; t += gridDim.x * blockDim.x) {
-    if (mask && !mask[a.mesh_of_tet[t]]) continue;  // batched solve: mesh not in this sweep
+  const int T = a.T, TT = a.tile_tets, stride = gridDim.x * blockDim.x;
+  int t = int(sweep_first());
+  bool act = tet_in_sweep(a, mask, t);
+  int4 ids = act ? tile_node_ids(a, t) : make_int4(0, 0, 0, 0);
+  for (; t < T; t += stride) {
+    const int4 cur = ids;
+    const bool cur_act = act;
+    act = tet_in_sweep(a, mask, t + stride);
+    ids = act ? tile_node_ids(a, t + stride) : make_int4(0, 0, 0, 0);
+    if (!cur_act) continue;
     const int tile = tile_of(t, a.tile_magic);
-    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT, cur);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
   }
 }
@@ -1296,10 +1329,14 @@ __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char
   });
 }
 __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
-  const int T = a.T, TT = a.tile_tets;
-  for (int t = int(sweep_first()); t < T; t += gridDim.x * blockDim.x) {
+  const int T = a.T, TT = a.tile_tets, stride = gridDim.x * blockDim.x;
+  int t = int(sweep_first());
+  int4 ids = tile_node_ids(a, t);
+  for (; t < T; t += stride) {
+    const int4 cur = ids;
+    ids = tile_node_ids(a, t + stride);
     const int tile = tile_of(t, a.tile_magic);
-    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT, cur);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
     for (int j = 0; j < a.nwarm; ++j)
       tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
