@@ -269,20 +269,36 @@ __global__ void __launch_bounds__(32 * kFeatWarps, 3) k_node_features(FeatureArg
     }
     f[3] = d.x, f[4] = d.y, f[5] = d.z;
     const int q0 = a.inc_ptr[i], q1 = a.inc_ptr[i + 1];
-    for (int q = q0; q < q1; ++q) {
-      const int t = a.inc_ent[q] >> 2;
-      if (a.quat_g || a.tile_f) {
-        // the tet's rotation from its quaternion (the FP32 rotation of the
-        // matrix-free solvers is rebuilt the same way)
-        const float4 qt =
-            a.quat_g ? make_float4(a.quat_g[4L * t].w, a.quat_g[4L * t + 1].w, a.quat_g[4L * t + 2].w,
-                                   a.quat_g[4L * t + 3].w)
-                     : tile_quaternion(a.tile_f, a.tile_tets, tile_of(t, a.tile_magic), t);
-        float R[9];
-        quaternion_to_rotation(qt, R);
+    if (a.quat_g || a.tile_f) {
+      // the tets' rotations from their quaternions (the FP32 rotation of the
+      // matrix-free solvers is rebuilt the same way), four tets at a time:
+      // their incidence entries, then their quaternions, are loaded ahead of
+      // the sums so that the dependent gathers overlap
+      for (int q = q0; q < q1; q += 4) {
+        int tq[4];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) f[9 + k] += R[k];
-      } else {
+        for (int k = 0; k < 4; ++k) tq[k] = q + k < q1 ? a.inc_ent[q + k] >> 2 : -1;
+        float4 qt[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int t = tq[k];
+          qt[k] = t < 0 ? make_float4(0.f, 0.f, 0.f, 1.f)
+                  : a.quat_g ? make_float4(a.quat_g[4L * t].w, a.quat_g[4L * t + 1].w, a.quat_g[4L * t + 2].w,
+                                           a.quat_g[4L * t + 3].w)
+                             : tile_quaternion(a.tile_f, a.tile_tets, tile_of(t, a.tile_magic), t);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (tq[k] < 0) break;
+          float R[9];
+          quaternion_to_rotation(qt[k], R);
+#pragma unroll
+          for (int c = 0; c < 9; ++c) f[9 + c] += R[c];
+        }
+      }
+    } else {
+      for (int q = q0; q < q1; ++q) {
+        const int t = a.inc_ent[q] >> 2;
 #pragma unroll
         for (int k = 0; k < 9; ++k) f[9 + k] += a.re_f[long(k) * a.T + t];
       }
