@@ -108,8 +108,10 @@ typedef struct otfem_solver_params {
   int refresh_period;       /* matrix-free: recompute r = b - A v every N iterations (16) */
   int sequential_dots;      /* reference solver: 1 = sum dot products in node order on one
                                thread (bit-identical to the reference), 0 = parallel tree.
-                               matrix-free: 1 = grid sums of the CTA totals in CTA order,
-                               0 = FP64 atomic accumulation of them (faster) */
+                               matrix-free: the mixed solver's CG sums always add the CTA
+                               totals in CTA order (deterministic); 1 also orders the
+                               projected start's Gram sums, the FP64 solver's and the
+                               batches' sums, 0 = FP64 atomic accumulation of those */
   int warm_start;           /* OTFEM_WARM_START_* (PROJECTED and LEARNED: OTFEM_SOLVER_MIXED,
                                single meshes and batches; a batch solves each mesh's own
                                search space) */
