@@ -23,7 +23,11 @@
 // implied, so a rigid translation gives exactly zero force.
 //
 // Precision of the mixed solver.  GB300 executes FP64 at ~1/64 of the FP32
-// rate, so FP64 is used only where cancellation needs it.
+// rate, and every FP64 instruction (conversions and compares included) holds
+// the issuing SM sub-partition for ~64 cycles, so the mixed solver runs no
+// FP64 arithmetic: where cancellation needs more than FP32 it uses (hi, lo)
+// float pairs, and FP64 node data is split into pairs and joined back by
+// integer instructions (otfem_df.h).
 //  * Element apply, search direction p, residual r: FP32.
 //  * Velocity v: a (hi, lo) float pair, updated with an exact two-sum, which
 //    is also the apply operand when the residual is recomputed.  The stiffness
@@ -32,11 +36,14 @@
 //    as (hi_k - hi_0) + (lo_k - lo_0), exact for nearby values (Sterbenz), so
 //    they keep full FP32 relative precision.
 //  * Dot products: FP32 node terms accumulated as (hi, lo) float pairs
-//    (~48-bit mantissa, the accuracy of FP64 summation); alpha and beta in
-//    FP64, computed once per iteration by the last CTA of the grid sum.
-//  * b and the residual recompute b - A v: FP64 (once per step / every
-//    refresh_period iterations).
-//  * K1: FP32, except the FP64 edge differences of the FP64 coordinates.
+//    (~48-bit mantissa, the accuracy of FP64 summation) and added up over the
+//    grid in CTA order; alpha, beta and the estimates in FP32-pair arithmetic,
+//    computed by every CTA from the same totals.
+//  * b, the mass diagonal and the residual recompute b - A v: (hi, lo) pairs
+//    (once per step / every refresh_period iterations); the position update
+//    x += dt v keeps one FP64 addition per coordinate.
+//  * K1: FP32, with the edges of the current positions from their (hi, lo)
+//    split and the rest edges from a per-tet FP32 table.
 // The FP64 solver keeps every vector and reduction in FP64 (accuracy
 // reference).
 #include <algorithm>
@@ -2224,7 +2231,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_fp64(MixedArgs a) {
 // to arrive at a reduction updates the scalars of all meshes at once (one
 // thread per mesh).  Node phases walk one contiguous node range per warp, so
 // a warp meets each mesh boundary at most once and adds its per-mesh sums
-// with one FP64 atomic per value and mesh.
+// with one FP64 atomic per value and mesh (the batch's per-mesh sums).
 
 constexpr int kMaskApply = 0, kMaskUpdate = 1, kMaskRefresh = 2;
 constexpr int kBatchSlots = 8;  // accumulators per mesh and round
@@ -2759,8 +2766,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   }
 }
 
-// K1, mixed: FP32 orientation and elastic forces.  Edge differences of the
-// FP64 current and model coordinates are taken in FP64, then rounded.  The
+// K1, mixed: FP32 orientation and elastic forces.  The current edges come
+// from the (hi, lo) split of the FP64 positions (exact differences of the
+// high parts of nearby nodes, plus those of the low parts), the rest edges
+// from k_rest_edges' FP32 table (FP64 differences, rounded).  The
 // rows of E^-1 are -b_k (fem_compute_b.h), so F = -sum_k e'_k (x) b_k, which
 // Gram-Schmidt orthonormalises exactly as the reference's F (a positive
 // multiple of it) would be.
