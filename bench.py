@@ -594,7 +594,7 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * r_learn["dev_s"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 element apply, f64 CG vectors and reductions, bf16/f32 warm-start network",
+        "dtype": "f32 element apply and CG vectors (velocity as f32 hi/lo pairs), f32-pair reductions and scalars, bf16/f32 warm-start network",
         "data": "synthetic",
         "config": {"workload": WORKLOAD["name"],
                    "warm_start": "learned (node MLP on 1-ring mean inputs, trained in this run) in the projected search space",
