@@ -109,7 +109,7 @@ typedef struct otfem_solver_params {
   int sequential_dots;      /* reference solver: 1 = sum dot products in node order on one
                                thread (bit-identical to the reference), 0 = parallel tree.
                                matrix-free: the mixed solver's CG sums always add the CTA
-                               totals in CTA order (deterministic); 1 also orders the
+                               totals in CTA order; 1 also orders the
                                projected start's Gram sums, the FP64 solver's and the
                                batches' sums, 0 = FP64 atomic accumulation of those */
   int warm_start;           /* OTFEM_WARM_START_* (PROJECTED and LEARNED: OTFEM_SOLVER_MIXED,

@@ -615,7 +615,9 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
 // shuffles, the warp totals, one (hi, lo) partial per CTA and value, a grid
 // synchronisation, then every CTA adds up all partials in CTA order by the
 // same tree and every thread evaluates fin(totals, outputs).  The sums are
-// bit-identical in every CTA and from run to run.  Partials alternate between
+// bit-identical in every CTA, and for the same node values from run to run
+// (the element apply's float reductions into q are unordered, so a whole
+// solve is not bit-reproducible).  Partials alternate between
 // two halves by round parity: a CTA writes the partials of round r + 2 only
 // after every CTA has arrived at round r + 1, i.e. has read those of round r.
 template <int NV, int NO, typename Fin>
