@@ -409,6 +409,25 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng):
                      "max_iterations_per_step": float(np.mean(its)),
                      "mesh_iterations_last_step": {"mean": float(mi.mean()), "min": int(mi.min()), "max": int(mi.max())},
                      "setup_s": round(setup_s, 2)}
+        if name == "plain":
+            # the element apply over all 4M tets (325 MB of tiles: beyond the
+            # 129 MB L2, the HBM-bound regime), L2 flushed before each sweep
+            variant = ctypes.c_int32()
+            capi.check(lib.otfem_tuning(h, ctypes.byref(variant), None))
+            n_free = int((fixed_all == 0).sum())
+            nbytes = BYTES_PER_TET_APPLY[int(variant.value)] * T + BYTES_PER_NODE_APPLY * n_free
+            sweep_ms = []
+            for _ in range(10):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                flush_l2()
+                e0.record(stream)
+                capi.check(lib.otfem_apply_sweeps(h, capi.SOLVER_MIXED, 0.005, 1))
+                e1.record(stream)
+                torch.cuda.synchronize()
+                sweep_ms.append(e0.elapsed_time(e1))
+            ms = float(np.median(sweep_ms))
+            res["apply_sweep"] = {"variant": int(variant.value), "ms": ms, "algorithmic_bytes": nbytes,
+                                  "achieved_gbs": nbytes / (ms * 1e-3) / 1e9, "l2": "flushed before each sweep"}
         if warm == capi.WARM_START_LEARNED:
             net.detach(h)
         capi.check(lib.otfem_destroy(h))
@@ -583,6 +602,10 @@ def run_ours(args, world, rank, local):
     if not args.no_extra:
         extra["inference_ab_64x16x16"] = run_inference_ab(lib, capi, torch, stream, net, args, flush_l2, rng)
         extra["batch"] = run_batch_workload(lib, capi, torch, stream, net, args, flush_l2, rng)
+        if "apply_sweep" in extra["batch"]:
+            sw = extra["batch"]["apply_sweep"]
+            sw["frac"] = sw["achieved_gbs"] / peak
+            sw["peak_gbs"] = peak
 
     total_tet_steps = T * args.steps * world
     value = total_tet_steps / r_learn["dev_s"]
