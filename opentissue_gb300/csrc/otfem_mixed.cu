@@ -408,14 +408,15 @@ __device__ __forceinline__ float residual_df(DF b, DF d, DF v, float q) {
   const DF r = df_add(b, df_neg(t));
   return r.hi + r.lo;
 }
-// a / b rounded to FP32 (one correction step on the FP32 quotient of the
-// high parts: q + (a - q b) / b, with q b formed exactly by an FMA).
+// a / b rounded to FP32: a fast approximate quotient of the high parts, then
+// one correction step q + (a - q b) / b with q b formed exactly by an FMA,
+// which also absorbs the approximation's few-ulp error.
 __device__ __forceinline__ float df_div(DF a, DF b) {
-  const float q = a.hi / b.hi;
+  const float q = __fdividef(a.hi, b.hi);
   const float p = q * b.hi;
   const float e = fmaf(q, b.hi, -p);
   const float r = (((a.hi - p) - e) + a.lo) - q * b.lo;
-  return q + r / b.hi;
+  return q + __fdividef(r, b.hi);
 }
 // (hi, lo) += inc
 __device__ __forceinline__ void df_inc(float& hi, float& lo, float inc) {
@@ -614,11 +615,11 @@ __device__ bool grid_reduce(const MixedArgs& a, const Acc (&val)[NV], double (&o
 // ~64 cycles, so the scalar work between two phases stays in FP32 pairs: warp
 // shuffles, the warp totals, one (hi, lo) partial per CTA and value, a grid
 // synchronisation, then every CTA adds up all partials in CTA order by the
-// same tree and every thread evaluates fin(totals, outputs).  The sums are
-// bit-identical in every CTA, and for the same node values from run to run
-// (the element apply's float reductions into q are unordered, so a whole
-// solve is not bit-reproducible).  Partials alternate between
-// two halves by round parity: a CTA writes the partials of round r + 2 only
+// same tree, and one warp evaluates fin(totals, outputs) for the CTA.  The
+// sums are bit-identical in every CTA, and for the same node values from run
+// to run (the element apply's float reductions into q are unordered, so a
+// whole solve is not bit-reproducible).  Partials alternate between two
+// halves by round parity: a CTA writes the partials of round r + 2 only
 // after every CTA has arrived at round r + 1, i.e. has read those of round r.
 template <int NV, int NO, typename Fin>
 __device__ bool grid_reduce_df(const MixedArgs& a, const DF (&val)[NV], float (&out)[NO], unsigned& round,
@@ -671,10 +672,22 @@ __device__ bool grid_reduce_df(const MixedArgs& a, const DF (&val)[NV], float (&
     if (lane == 0) s_tot[warp] = x;
   }
   __syncthreads();
-  DF t[NV];
+  // the scalar step by one warp, its outputs through shared memory
+  __shared__ float s_out[NO];
+  if (warp == 0) {
+    DF t[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) t[k] = s_tot[k];
-  fin(t, out);
+    for (int k = 0; k < NV; ++k) t[k] = s_tot[k];
+    float o[NO];
+    fin(t, o);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < NO; ++k) s_out[k] = o[k];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NO; ++k) out[k] = s_out[k];
   return true;
 }
 
