@@ -591,8 +591,10 @@ def run_ours(args, world, rank, local):
         capi.check(lib.otfem_set_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
         capi.check(lib.otfem_set_nodes(h_learn, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
         capi.check(lib.otfem_simulate_ex(h_learn, w["dt"], 1, ctypes.byref(learned), None))
-        capi.check(lib.otfem_get_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-        capi.check(lib.otfem_get_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        # both downloads queued back to back, one wait
+        capi.check(lib.otfem_get_nodes_async(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+        capi.check(lib.otfem_get_nodes_async(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        capi.check(lib.otfem_synchronize(h_learn))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = dist_max(world, sum(e2e_ms) / 1e3)
     dist_barrier(world)

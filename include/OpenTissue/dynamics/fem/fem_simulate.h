@@ -50,8 +50,9 @@ inline StepStats simulate(fem_mesh& mesh, real_type const& time_step, bool use_s
   gpu::check(otfem_set_nodes(h, OTFEM_F_EXTERNAL, f, n3), "fem::simulate");
   gpu::check(otfem_simulate_ex(h, double(time_step), use_stiffness_warping ? 1 : 0, &params, &g.stats()),
              "fem::simulate");
-  gpu::check(otfem_get_nodes(h, OTFEM_COORD, x, n3), "fem::simulate");
-  gpu::check(otfem_get_nodes(h, OTFEM_VELOCITY, v, n3), "fem::simulate");
+  // queued back to back; the last, blocking download waits for all three
+  gpu::check(otfem_get_nodes_async(h, OTFEM_COORD, x, n3), "fem::simulate");
+  gpu::check(otfem_get_nodes_async(h, OTFEM_VELOCITY, v, n3), "fem::simulate");
   gpu::check(otfem_get_nodes(h, OTFEM_F_EXTERNAL, f, n3), "fem::simulate");
   for (std::size_t i = 0; i < N; ++i) {
     typename fem_mesh::node_type& n = mesh.node_at(i);

@@ -170,6 +170,12 @@ OTFEM_API int otfem_set_nodes(otfem_handle h, int field, const double* host_src,
 OTFEM_API int otfem_get_nodes(otfem_handle h, int field, double* host_dst, int64_t count);
 OTFEM_API int otfem_set_nodes_device(otfem_handle h, int field, const double* device_src, int64_t count);
 OTFEM_API int otfem_get_nodes_device(otfem_handle h, int field, double* device_dst, int64_t count);
+/* As otfem_get_nodes without waiting: the copy is queued on the handle's
+ * stream behind the work already there, and host_dst holds the values once
+ * the stream has reached it (otfem_synchronize, or a later blocking call).
+ * With page-locked host memory several fields download back to back with one
+ * wait; with pageable memory the copy completes before the call returns. */
+OTFEM_API int otfem_get_nodes_async(otfem_handle h, int field, double* host_dst, int64_t count);
 OTFEM_API int otfem_set_fixed(otfem_handle h, const uint8_t* host_fixed, int64_t count);
 
 /* fem::simulate (fem_simulate.h:49-113) with the reference's fixed solver

@@ -100,6 +100,7 @@ SIGNATURES = {
     "otfem_init": (ctypes.c_int, [_h] + [ctypes.c_double] * 6),
     "otfem_set_nodes": (ctypes.c_int, [_h, ctypes.c_int, _dp, ctypes.c_int64]),
     "otfem_get_nodes": (ctypes.c_int, [_h, ctypes.c_int, _dp, ctypes.c_int64]),
+    "otfem_get_nodes_async": (ctypes.c_int, [_h, ctypes.c_int, _dp, ctypes.c_int64]),
     "otfem_set_nodes_device": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64]),
     "otfem_get_nodes_device": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64]),
     "otfem_set_fixed": (ctypes.c_int, [_h, _u8p, ctypes.c_int64]),

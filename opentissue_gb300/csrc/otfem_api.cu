@@ -582,6 +582,11 @@ int otfem_set_nodes_device(otfem_handle h, int field, const double* src, int64_t
 int otfem_get_nodes_device(otfem_handle h, int field, double* dst, int64_t count) {
   return transfer(h, field, dst, count, false, cudaMemcpyDeviceToDevice);
 }
+int otfem_get_nodes_async(otfem_handle h, int field, double* dst, int64_t count) {
+  // cudaMemcpyDefault: the copy direction follows from the pointers; transfer()
+  // waits only for cudaMemcpyDeviceToHost
+  return transfer(h, field, dst, count, false, cudaMemcpyDefault);
+}
 
 int otfem_set_fixed(otfem_handle h, const uint8_t* fixed, int64_t count) {
   if (!h || (!fixed && count)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");

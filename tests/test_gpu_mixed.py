@@ -208,6 +208,30 @@ def test_model_coordinate_changes_follow_the_oracle(gpu, oracle):
     m.close()
 
 
+def test_async_download_matches_blocking_one(gpu):
+    """otfem_get_nodes_async queues the copy behind the step; after
+    otfem_synchronize the values equal a blocking download's."""
+    import torch
+    tets, coord, fixed = beam(6, 3, 3, jitter_seed=2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
+    pinned = torch.empty((2, m.N, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pageable = np.zeros((m.N, 3))
+    for _ in range(3):
+        m.step(0.01, True, mixed(), check=False)
+        dp = ctypes.POINTER(ctypes.c_double)
+        capi.check(m.lib.otfem_get_nodes_async(m.h, capi.COORD, pinned[0].ctypes.data_as(dp), pinned[0].size))
+        capi.check(m.lib.otfem_get_nodes_async(m.h, capi.VELOCITY, pinned[1].ctypes.data_as(dp), pinned[1].size))
+        capi.check(m.lib.otfem_get_nodes_async(m.h, capi.COORD, pageable.ctypes.data_as(dp), pageable.size))
+        capi.check(m.lib.otfem_synchronize(m.h))
+        assert np.array_equal(pinned[0], m.get(capi.COORD))
+        assert np.array_equal(pinned[1], m.get(capi.VELOCITY))
+        assert np.array_equal(pageable, pinned[0])
+    assert m.lib.otfem_get_nodes_async(m.h, capi.COORD, pageable.ctypes.data_as(dp), 5) == capi.ERR_INVALID_ARGUMENT
+    m.close()
+
+
 def test_iteration_cap_is_a_warning(gpu):
     tets, coord, fixed = beam(8, 3, 3, jitter_seed=1)
     m = GpuMesh(tets, coord, fixed)
