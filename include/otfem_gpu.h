@@ -342,7 +342,7 @@ OTFEM_API int otfem_check_wait_timeout(otfem_handle h, int64_t cycles, int32_t* 
  * synchronised. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 8 stamps in SM
- * clock cycles since the kernel started (middle CTA): b and |b| done, the
+ * clock cycles since the kernel started (middle CTA): b done, the
  * initial residual's element sweeps (and the search directions') done, the
  * start ready (projection solved), CG loop done, position update done; then,
  * for the projected and learned starts (else 0), the Gram sums begun, the

@@ -729,6 +729,12 @@ struct FinPcgF {
 struct FinIdentityF1 {
   __device__ void operator()(const DF* t, float* o) const { o[0] = t[0].hi + t[0].lo; }
 };
+struct FinIdentityF2 {
+  __device__ void operator()(const DF* t, float* o) const {
+    o[0] = t[0].hi + t[0].lo;
+    o[1] = t[1].hi + t[1].lo;
+  }
+};
 
 struct FinIdentity1 {
   __device__ void operator()(const double* t, double* o) const { o[0] = t[0]; }
@@ -1833,12 +1839,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     }
   }
   // The loop's scalars are FP32 (pairs inside the reductions): no FP64
-  // instruction sits between two phases of an iteration.
-  float tot[1];
-  if (!grid_reduce_df<1, 1>(a, bbsum, tot, round, FinIdentityF1())) return;
+  // instruction sits between two phases of an iteration.  |b|^2 is first
+  // needed at the convergence test after the start, so its sums ride along
+  // with the start's |r|^2 reduction; here a barrier suffices (the sweep
+  // gathers the operand of other CTAs' nodes).
+  if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   if (tracer) phase_stamp(a, 0, t_start);
-  const float bnorm2 = tot[0];
-  const float thresh = float(a.rtol * a.rtol) * bnorm2;
 
   // Initial residual r = b - A v (FP64), p = S r.  Projected and learned
   // starts: also A W_j for the search directions W_j, and the start moves to
@@ -1918,8 +1924,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     a.v_keep[N + i] = a.v_lo[i];
     rr[0] = df_add(rr[0], DF{rf[0] * rf[0] + rf[1] * rf[1] + rf[2] * rf[2], 0.f});
   }
-  if (!grid_reduce_df<1, 1>(a, rr, tot, round, FinIdentityF1())) return;
+  float tot[2];
+  {
+    const DF sums[2] = {rr[0], bbsum[0]};
+    if (!grid_reduce_df<2, 2>(a, sums, tot, round, FinIdentityF2())) return;
+  }
   if (tracer) phase_stamp(a, 2, t_start);
+  const float bnorm2 = tot[1];
+  const float thresh = float(a.rtol * a.rtol) * bnorm2;
   float rho = tot[0];
   const float rho0 = rho;
   int it = 0;
@@ -2019,12 +2031,13 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
         a.v_keep[cand + N + i] = vl;
         tr[0] = df_add(tr[0], DF{rx * rx + ry * ry + rz * rz, 0.f});
       }
-      if (!grid_reduce_df<1, 1>(a, tr, tot, round, FinIdentityF1())) return;
+      float tt[1];
+      if (!grid_reduce_df<1, 1>(a, tr, tt, round, FinIdentityF1())) return;
       // the true residual well above the recursive one: the recurrence has
       // decoupled from the system, restart the direction
-      restart = tot[0] > 4.f * sc[2];
+      restart = tt[0] > 4.f * sc[2];
       prev_est = -1.f;
-      rho = tot[0];
+      rho = tt[0];
       // stagnation is judged at the periodic refreshes only (16 iterations
       // apart), not at the convergence checks in between
       if (rho < best_true) {

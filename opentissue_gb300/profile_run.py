@@ -86,7 +86,7 @@ def trace_report(lib, h, dp):
         mhz = 2070.0
     ph = np.zeros(8)
     capi.check(lib.otfem_solver_phases(h, ph.ctypes.data_as(dp)))
-    names = ["b and |b|", "initial residual and direction sweeps", "start (projection solved)", "CG loop",
+    names = ["b", "initial residual and direction sweeps", "start (projection solved, |r| and |b|)", "CG loop",
              "position update"]
     for n, v in zip(names, np.diff(np.concatenate([[0.0], ph[:5]]))):
         print(f"phase {n}: {v / mhz:.1f} us")
