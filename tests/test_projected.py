@@ -172,3 +172,23 @@ def test_projected_start_parameter_checks(gpu):
     rc, _ = m.step(0.01, True, params(warm_start=3), check=False)
     assert rc == capi.ERR_INVALID_ARGUMENT
     m.close()
+
+
+def test_solver_phases_record_the_start(gpu):
+    """otfem_solver_phases: five ordered stamps for every mixed solve, and for
+    the projected start three more (Gram sums begun, totals in, coefficients
+    solved) between the start sweeps and the start; zeros otherwise."""
+    tets, coord, fixed = beam(*DIMS, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    dp = ctypes.POINTER(ctypes.c_double)
+    ph = np.zeros(8)
+    for warm in (capi.WARM_START_PREVIOUS, capi.WARM_START_PROJECTED, capi.WARM_START_PREVIOUS):
+        run_loaded(m, DIMS, 3, params(warm_start=warm), *LOAD)
+        capi.check(m.lib.otfem_solver_phases(m.h, ph.ctypes.data_as(dp)))
+        assert np.all(np.diff(ph[:5]) > 0) and ph[0] > 0, ph
+        if warm == capi.WARM_START_PROJECTED:
+            assert ph[1] < ph[5] < ph[6] < ph[7] < ph[2], ph
+        else:
+            assert np.all(ph[5:] == 0), ph
+    m.close()
