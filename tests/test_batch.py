@@ -89,10 +89,12 @@ def params(**kw):
     return capi.default_params(**base)
 
 
-def run_batch(beams, steps, variant=None, **kw):
+def run_batch(beams, steps, variant=None, net=None, **kw):
     b = Batch(beams)
     if variant is not None:
         capi.check(b.lib.otfem_set_apply_variant(b.h, variant))
+    if net is not None:
+        net.attach(b.h)
     mass = b.get(capi.MASS)
     f = np.concatenate([loads(m, bm["fixed"], bm["tip_force"]) for m, bm in zip(b.per_mesh(mass), beams)])
     out = []
@@ -213,6 +215,35 @@ def test_batch_projected_start_per_mesh(gpu):
     assert late1 < 0.75 * late0, (late0, late1)
     b0.close()
     b1.close()
+
+
+def test_batch_learned_start_per_mesh(gpu):
+    """A network attached to a batch: each mesh starts from its least-energy
+    point over the network's correction and its own history.  The network is
+    untrained (random weights), so its correction is arbitrary; the search
+    space still holds the projected start's directions, and every mesh ends
+    at the plain start's answer."""
+    from oracle import mlp_oracle as mo
+    from opentissue_gb300.warmstart import WarmStartNet
+    rng = np.random.default_rng(8)
+    w = {name: rng.uniform(-1, 1, shape) / np.sqrt(shape[1] if len(shape) == 2 else 64) for name, shape in mo.SHAPES}
+    norm = {"mu_x": np.zeros(18), "sd_x": np.ones(18), "mu_y": np.zeros(3), "sd_y": np.full(3, 1e-3)}
+    net = WarmStartNet(capacity=1 << 10, seed=3)
+    net.set_state(mo.pack(w, norm))
+    beams = random_beams(5, seed=36, nx=(10, 16), nyz=(3, 5))
+    steps = 10
+    b0, out0 = run_batch(beams, steps)
+    b1, out1 = run_batch(beams, steps, net=net, warm_start=capi.WARM_START_LEARNED)
+    for s in range(steps):
+        for k, bm in enumerate(beams):
+            disp = np.abs(out0[s][0][k] - bm["coord"]).max()
+            assert np.abs(out1[s][0][k] - out0[s][0][k]).max() <= 1e-4 * disp, (s, k)
+        its, st, rel, _ = out1[s][1]
+        assert np.all(st == capi.OK) and np.all(rel <= 1e-6)
+    WarmStartNet.detach(b1.h)
+    b0.close()
+    b1.close()
+    net.close()
 
 
 def test_batch_rejects_other_solvers_and_variants(gpu):
