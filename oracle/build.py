@@ -13,7 +13,12 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = os.environ.get("OTFEM_REFERENCE_ROOT", "/root/reference")
+# The OpenTissue source tree the reference build reads (in place, never
+# copied): the environment variable OTFEM_REFERENCE_ROOT, else the recipe's
+# default location DEFAULT_REFERENCE_ROOT.  Where neither holds the tree,
+# build_reference() builds nothing and the reference-backed checks skip.
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("OTFEM_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
 
 
 def _newer(out, srcs):
@@ -37,7 +42,8 @@ def build_reference(force=False):
     if not os.path.exists(os.path.join(REFERENCE_ROOT, "OpenTissue", "dynamics", "fem", "fem.h")):
         return None
     out = os.path.join(HERE, "_ref", "libotfem_ref.so")
-    srcs = [os.path.join(HERE, "ref", "ref_capi.cpp"), os.path.join(HERE, "otfem_oracle.h")]
+    srcs = [os.path.join(HERE, "ref", "ref_capi.cpp"), os.path.join(HERE, "ref", "ref_coupling.cpp"),
+            os.path.join(HERE, "ref", "build_ref.sh"), os.path.join(HERE, "otfem_oracle.h")]
     if force or not _newer(out, srcs):
         subprocess.check_call(["bash", os.path.join(HERE, "ref", "build_ref.sh"), REFERENCE_ROOT])
     return out

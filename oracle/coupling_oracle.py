@@ -7,15 +7,19 @@ imports, links or runs it.
   columns of P the edges x1 - x4, x2 - x4, x3 - x4; w4 = 1 - w1 - w2 - w3.
 * bind(): bind_surface (t4mesh_mesh_coupling.h:129-236) with the embedding
   test of collision_policy::report (:84-111), all four weights in
-  (-1e-4, 1 + 1e-4); the reference keeps the first tet its spatial hash
-  reports, the library and this restatement the lowest tet index that embeds
-  the point.  Stored per point: the tet and (m_w1, m_w2, m_w3).
+  (-1e-4, 1 + 1e-4).  The reference's spatial-hash point query
+  (collision/spatial_hashing/spatial_hashing_query.h:141-158) visits the
+  tets in index order and report() keeps a point's first embedding tet, so
+  the binding is the lowest tet index that embeds the point, which is what
+  this restatement computes.  Stored per point: the tet and (m_w1, m_w2,
+  m_w3).
 * update(): update_surface (:238-275), p0 w0 + p1 w1 + p2 w2 + p3 w3 with
   w0 = 1 - w1 - w2 - w3.
 
-Parity unpinned: mesh_coupling sits outside the FEM include closure that the
-oracle builds from the reference sources (it needs the spatial hashing and
-surface mesh libraries), so this is a restatement from the source only.
+Pinned to the reference: tests/golden/coupling.npz holds bind_surface and
+update_surface of the unmodified reference headers (oracle/ref/
+ref_coupling.cpp, tests/golden/make_coupling.py), and tests/test_coupling.py
+checks this restatement against it (identical tets, weights to 1e-12).
 """
 import numpy as np
 

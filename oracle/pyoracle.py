@@ -57,8 +57,43 @@ def load(kind="port"):
     lib.orc_get_plastic.argtypes = [v, _dp]
     lib.orc_get_volume.argtypes = [v, _dp]
     lib.orc_generate_blocks.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + [_ip, _dp]
+    if kind == "reference":
+        lib.orc_coupling_bind.restype = ctypes.c_int
+        lib.orc_coupling_bind.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _dp, ctypes.c_int, _dp, _ip, _dp]
+        lib.orc_coupling_update.restype = ctypes.c_int
+        lib.orc_coupling_update.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _dp, ctypes.c_int, _ip, _dp, _dp]
     _libs[path] = lib
     return lib
+
+
+def coupling_bind(tets, coord, points):
+    """t4mesh::mesh_coupling::bind_surface of the reference build: per point
+    the tet index (-1: unbound) and (w1, w2, w3)."""
+    lib = load("reference")
+    tets = np.ascontiguousarray(tets, np.int32)
+    coord = np.ascontiguousarray(coord, np.float64)
+    pts = np.ascontiguousarray(points, np.float64)
+    tet = np.full(pts.shape[0], -1, np.int32)
+    bary = np.zeros((pts.shape[0], 3))
+    lib.orc_coupling_bind(coord.shape[0], tets.shape[0], _ptr(tets, _ip), _ptr(coord, _dp), pts.shape[0],
+                          _ptr(pts, _dp), _ptr(tet, _ip), _ptr(bary, _dp))
+    return tet, bary
+
+
+def coupling_update(tets, coord, tet, bary):
+    """t4mesh::mesh_coupling::update_surface of the reference build for bound
+    points (every tet index >= 0)."""
+    lib = load("reference")
+    tets = np.ascontiguousarray(tets, np.int32)
+    coord = np.ascontiguousarray(coord, np.float64)
+    tet = np.ascontiguousarray(tet, np.int32)
+    bary = np.ascontiguousarray(bary, np.float64)
+    out = np.zeros((tet.shape[0], 3))
+    rc = lib.orc_coupling_update(coord.shape[0], tets.shape[0], _ptr(tets, _ip), _ptr(coord, _dp), tet.shape[0],
+                                 _ptr(tet, _ip), _ptr(bary, _dp), _ptr(out, _dp))
+    if rc != 0:
+        raise ValueError("update_surface needs a tet for every point")
+    return out
 
 
 def generate_blocks(I, J, K, w, h, d, kind="port"):

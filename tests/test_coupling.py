@@ -1,12 +1,57 @@
 """Mesh coupling (t4mesh::mesh_coupling): surface points bound to the tets
-that embed them and moved with the deformed mesh, against the CPU
-restatement in oracle/coupling_oracle.py."""
+that embed them and moved with the deformed mesh, against the reference
+itself (tests/golden/coupling.npz: bind_surface and update_surface compiled
+from the unmodified reference headers, tests/golden/make_coupling.py) and
+against the CPU restatement in oracle/coupling_oracle.py (itself pinned to
+that fixture)."""
 import numpy as np
 import pytest
 
-from helpers import beam, irregular_mesh
+from helpers import beam, golden, irregular_mesh
 from oracle import coupling_oracle as co
 from opentissue_gb300 import capi, fem
+
+MESHES = ("blocks", "delaunay")
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_restatement_matches_the_reference_fixture(name):
+    """The restatement against the reference build: the same tet for every
+    point (the reference's spatial-hash query visits tets in index order and
+    keeps the first that embeds a point, so on shared faces and at nodes the
+    lowest tet index), weights and moved points to rounding."""
+    g = golden("coupling")
+    tets, coord, pts = g[f"{name}_tets"], g[f"{name}_coord"], g[f"{name}_points"]
+    tet, bary = co.bind(tets, coord, pts)
+    assert np.array_equal(tet, g[f"{name}_tet"])
+    assert np.abs(bary - g[f"{name}_bary"]).max() <= 1e-12
+    moved = co.update(tets, g[f"{name}_coord_deformed"], tet, bary, pts)
+    ref = g[f"{name}_moved"]
+    assert np.abs(moved - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", MESHES)
+def test_library_matches_the_reference_fixture(gpu, name):
+    """otfem_surface_bind / otfem_surface_update against the reference build:
+    bound tets identical (shared faces and nodes included), weights and moved
+    points to rounding, unbound points kept where they were."""
+    g = golden("coupling")
+    tets, coord, pts = g[f"{name}_tets"], g[f"{name}_coord"], g[f"{name}_points"]
+    mesh = fem.Mesh(tets, coord)
+    fem.init(mesh, 5e5, 0.33, 1000.0, 1e30, 0.0, 0.0)
+    b = fem.bind_surface(mesh, pts)
+    tet, bary = b.binding()
+    assert np.array_equal(tet, g[f"{name}_tet"])
+    assert np.abs(bary - g[f"{name}_bary"]).max() <= 1e-12
+    assert b.bound == int((g[f"{name}_tet"] >= 0).sum())
+    mesh.coord = np.ascontiguousarray(g[f"{name}_coord_deformed"])
+    mesh.upload(capi.COORD)
+    moved = fem.update_surface(b)
+    ref = g[f"{name}_moved"]
+    assert np.abs(moved - ref).max() <= 1e-12 * np.abs(ref).max()
+    b.close()
+    mesh.close()
 
 # ---- the restatement (CPU) ------------------------------------------------------
 
