@@ -32,8 +32,9 @@ inline SolverParams reference_solver() {
   return p;
 }
 
-// Matrix-free solver: FP32 element apply, FP64 CG (Jacobi-preconditioned),
-// stop at ||r|| <= rtol ||b||.
+// Matrix-free solver: FP32 element apply, Jacobi-preconditioned CG with the
+// velocity, dot products and scalars in (hi, lo) float pairs (~48-bit), stop
+// at ||r|| <= rtol ||b||.
 inline SolverParams mixed_solver(double rtol = 1e-6, int max_iterations = 10000) {
   SolverParams p = reference_solver();
   p.solver = OTFEM_SOLVER_MIXED;

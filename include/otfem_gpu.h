@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 5
+#define OTFEM_ABI_VERSION 6
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -64,9 +64,11 @@ enum {
    * rows, reference operation order, CG with min/max iterations, the absolute
    * clamps tiny = 1e-10 and the d1 < 0.001 break (fem_conjugate_gradients.h). */
   OTFEM_SOLVER_REFERENCE = 0,
-  /* Matrix-free step: FP64 orientation and right-hand side, FP32 stiffness
-   * apply, FP64 CG vectors, dot products and alpha/beta, residual replaced
-   * by b - A v every refresh_period iterations, stop at ||r|| <= rtol*||b||.
+  /* Matrix-free step: FP32 orientation and stiffness apply (the element
+   * deformations formed in (hi, lo) float pairs), FP64 positions, the
+   * velocity and the right-hand side as (hi, lo) float pairs, dot products
+   * and alpha/beta in float-pair arithmetic (~48-bit), residual replaced by
+   * b - A v every refresh_period iterations, stop at ||r|| <= rtol*||b||.
    * One persistent CG kernel per step, replayed from a CUDA graph. */
   OTFEM_SOLVER_MIXED = 1,
   /* Matrix-free step with the FP64 stiffness apply (accuracy reference for the
@@ -311,15 +313,19 @@ OTFEM_API int otfem_apply_operator(otfem_handle h, int solver, double dt, double
  * for callers that may not allocate device memory at the call: fixed-rate
  * loops, where cudaMalloc/cudaFree stall the device and take unbounded time,
  * and hosts whose device memory is owned by another allocator with a cap or
- * pool of its own.  x_device, y_device: device arrays of 3
- * doubles per node, written on the handle's stream and not synchronized.
+ * pool of its own.  x_device, y_device: device (or managed) arrays of 3
+ * doubles per node on the handle's device, written on the handle's stream
+ * and not synchronized; other pointers return OTFEM_ERR_INVALID_ARGUMENT.
  * The operand and accumulator live in one 16 MiB static device array that
  * every GPU loading the library holds until exit, so meshes are limited to
  * 262,144 nodes (larger ones return OTFEM_ERR_INVALID_ARGUMENT).  All calls
  * share that array: calls that may overlap on the GPU (other handles, other
  * streams) race; order them.  The first call on a device looks up the
  * array's device address (with that device current, which must be the
- * handle's device); make it before any stream capture. */
+ * handle's device) and keeps it; make it before any stream capture.  A call
+ * with x_device = y_device = NULL does only that set-up and returns OTFEM_OK.
+ * The kept address does not survive cudaDeviceReset (which invalidates every
+ * handle of the device as well). */
 OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt, double mass_damping,
                                            const double* x_device, double* y_device);
 /* Enqueues `sweeps` element-apply sweeps q += dt^2 K' p on the resident
@@ -360,6 +366,20 @@ OTFEM_API int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_vari
 /* Forces an element-apply variant (0..OTFEM_NUM_APPLY_VARIANTS-1) for the
  * following steps. */
 OTFEM_API int otfem_set_apply_variant(otfem_handle h, int32_t variant);
+/* The autotuner's search at otfem_init (no counterpart in the reference):
+ * the patch variants 0 and 1 once (single meshes; tile_tets reported as 0),
+ * the tiled variants 2 and 3 at every candidate tile size (the size that
+ * splits the tets evenly over the persistent grid, then 128, 256 and 512
+ * tets per tile), each timed as the best of 3 x 4 sweeps; the fastest
+ * combination is kept.  rows: the number of measured combinations (at most
+ * 16); the first max_rows are written to variant, tile_tets and ms (each may
+ * be NULL); chosen_tile_tets (may be NULL): the tile size in use. */
+OTFEM_API int otfem_tuning_search(otfem_handle h, int32_t max_rows, int32_t* rows, int32_t* variant,
+                                  int32_t* tile_tets, double* ms, int32_t* chosen_tile_tets);
+/* Forces an element-apply variant and a tile size (one of the autotuner's
+ * candidates; 0 keeps the current one) for the following steps; the tiles'
+ * rotations are rebuilt from the last orientations. */
+OTFEM_API int otfem_set_apply_shape(otfem_handle h, int32_t variant, int32_t tile_tets);
 /* Number of kernels this handle has enqueued so far (graph replays included). */
 OTFEM_API int otfem_launch_count(otfem_handle h, int64_t* count);
 /* Launch shape of the persistent CG kernel (grid CTAs, threads per CTA). */

@@ -132,6 +132,8 @@ SIGNATURES = {
     "otfem_surface_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_tuning": (ctypes.c_int, [_h, _i32p, _dp]),
     "otfem_set_apply_variant": (ctypes.c_int, [_h, ctypes.c_int32]),
+    "otfem_tuning_search": (ctypes.c_int, [_h, ctypes.c_int32, _i32p, _i32p, _i32p, _dp, _i32p]),
+    "otfem_set_apply_shape": (ctypes.c_int, [_h, ctypes.c_int32, ctypes.c_int32]),
     "otfem_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "otfem_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),

@@ -287,7 +287,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   OT_ALLOC(c.re_f, 9 * T);
   OT_ALLOC(c.b_f, 9 * T);
   OT_ALLOC(c.c_f, 3 * T);
-  OT_ALLOC(c.e0_f, 9 * T);
+  OT_ALLOC(c.e0_f, 18 * T);
   OT_ALLOC(c.re_d, 9 * T);
   OT_ALLOC(c.b_d, 9 * T);
   OT_ALLOC(c.c_d, 3 * T);
@@ -323,7 +323,11 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   if ((e = otfem::build_patches(c, d->tets)) != cudaSuccess) return bail(e, "build_patches");
   otfem::mixed_grid_shape(c, &c.mf_grid, &c.mf_block);
   otfem::staged_tiles(c);
-  OT_ALLOC(c.tile_f, size_t(c.num_tiles) * otfem::kTileWords * size_t(c.tile_tets));
+  {
+    int cand[4];
+    otfem::tile_candidates(c, cand, &c.tile_capacity);
+  }
+  OT_ALLOC(c.tile_f, c.tile_capacity);
   OT_ALLOC(c.partials, size_t(otfem::kMaxPartials) * c.mf_grid);
 
   // zero-initialised node members (math_vector3.h:63-66) and uploads
@@ -854,6 +858,39 @@ int otfem_tuning(otfem_handle h, int32_t* variant, double* ms_per_variant) {
   *variant = h->c.apply_variant;
   if (ms_per_variant)
     for (int v = 0; v < otfem::kNumApplyVariants; ++v) ms_per_variant[v] = h->c.apply_ms[v];
+  return OTFEM_OK;
+}
+
+int otfem_tuning_search(otfem_handle h, int32_t max_rows, int32_t* rows, int32_t* variant, int32_t* tile_tets,
+                        double* ms, int32_t* chosen_tile_tets) {
+  if (!h || !rows) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  const Context& c = h->c;
+  *rows = c.tune_rows;
+  for (int k = 0; k < c.tune_rows && k < max_rows; ++k) {
+    if (variant) variant[k] = c.tune_variant[k];
+    if (tile_tets) tile_tets[k] = c.tune_tile[k];
+    if (ms) ms[k] = c.tune_ms[k];
+  }
+  if (chosen_tile_tets) *chosen_tile_tets = c.tile_tets;
+  return OTFEM_OK;
+}
+
+int otfem_set_apply_shape(otfem_handle h, int32_t variant, int32_t tile_tets) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  int cand[4];
+  size_t floats = 0;
+  const int nc = otfem::tile_candidates(c, cand, &floats);
+  bool ok = tile_tets == 0;
+  for (int k = 0; k < nc; ++k) ok = ok || cand[k] == tile_tets;
+  if (!ok) return fail(OTFEM_ERR_INVALID_ARGUMENT, "tile size is not one of the autotuner's candidates");
+  int rc = otfem_set_apply_variant(h, variant);
+  if (rc != OTFEM_OK) return rc;
+  if (tile_tets != 0 && tile_tets != c.tile_tets) {
+    cudaError_t e;
+    if ((e = otfem::set_tile_layout(c, tile_tets)) != cudaSuccess) return cuda_fail(e, "tile layout");
+  }
   return OTFEM_OK;
 }
 

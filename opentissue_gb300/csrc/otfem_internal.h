@@ -123,7 +123,7 @@ struct Context {
 
   // matrix-free data
   float *re_f = nullptr, *b_f = nullptr, *c_f = nullptr;  // 9T, 9T, 3T
-  float* e0_f = nullptr;                                  // 9T: rest edges x0_k - x0_0 (k_rest_edges)
+  float* e0_f = nullptr;                                  // 18T: rest edges x0_k - x0_0 as (hi, lo) pairs (k_rest_edges)
   double *re_d = nullptr, *b_d = nullptr, *c_d = nullptr;  // 9T, 9T, 3T (FP64 apply)
   double* diag = nullptr;                                 // N: m(1+dt*alpha)
   float* diag_f = nullptr;                                // N: the same as (hi, lo) FP32 pairs
@@ -193,7 +193,14 @@ struct Context {
   unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
-  double apply_ms[OTFEM_NUM_APPLY_VARIANTS] = {};  // measured time of one sweep per variant
+  double apply_ms[OTFEM_NUM_APPLY_VARIANTS] = {};  // measured time of one sweep per variant (best tile size)
+  // the autotuner's search (autotune_apply): every measured (variant, tile
+  // size; 0 for the patch variants, which do not read tiles) and its time
+  static constexpr int kMaxTuneRows = 16;
+  int tune_rows = 0;
+  int tune_variant[kMaxTuneRows] = {}, tune_tile[kMaxTuneRows] = {};
+  double tune_ms[kMaxTuneRows] = {};
+  size_t tile_capacity = 0;       // floats allocated at tile_f: the largest candidate layout
   DeviceSync* sync = nullptr;
   double* trace = nullptr;                                 // kTraceRows x kTraceCols
   DeviceStats* stats = nullptr;
@@ -235,11 +242,20 @@ cudaError_t check_wait_timeout(Context& c, long long cycles, int* status);  // t
 // num_tiles): tiles of at most kTileMaxTets tets, as even a share of the
 // tets per CTA as a multiple of 16 allows.
 void staged_tiles(Context& c);
+// Candidate tile sizes of the autotuner's search: the balanced size of
+// staged_tiles first, then 128, 256 and 512 tets (each at most once).
+// Returns how many (at most 4) and, in *floats, the tile_f size the largest
+// layout needs.
+int tile_candidates(const Context& c, int* out, size_t* floats);
+// Lays the tiles out with tile_tets tets each (tile words from the init data,
+// identity rotations until the next orientation phase).
+cudaError_t set_tile_layout(Context& c, int tile_tets);
 // Builds the apply patches from the host connectivity (once per mesh).
 cudaError_t build_patches(Context& c, const int32_t* tets_host);
 cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver);
-// Times one element-apply sweep of every variant on this mesh and keeps the
-// fastest in c.apply_variant (synchronises the stream).
+// Times one element-apply sweep of every variant on this mesh, the tiled
+// variants at every candidate tile size, and keeps the fastest combination
+// in c.apply_variant and the tile layout (synchronises the stream).
 cudaError_t autotune_apply(Context& c);
 constexpr int kNumApplyVariants = OTFEM_NUM_APPLY_VARIANTS;
 static_assert(sizeof(Context::apply_ms) == sizeof(double) * kNumApplyVariants, "one time per apply variant");

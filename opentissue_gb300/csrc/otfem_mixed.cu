@@ -2794,13 +2794,25 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   }
 }
 
-// K1, mixed: FP32 orientation and elastic forces.  The current edges come
-// from the (hi, lo) split of the FP64 positions (exact differences of the
-// high parts of nearby nodes, plus those of the low parts), the rest edges
-// from k_rest_edges' FP32 table (FP64 differences, rounded).  The
-// rows of E^-1 are -b_k (fem_compute_b.h), so F = -sum_k e'_k (x) b_k, which
-// Gram-Schmidt orthonormalises exactly as the reference's F (a positive
-// multiple of it) would be.
+// K1, mixed: FP32 orientation and elastic forces.  The rows of E^-1 are
+// -b_k (fem_compute_b.h), so F = -sum_k e'_k (x) b_k, which Gram-Schmidt
+// orthonormalises exactly as the reference's F (a positive multiple of it)
+// would be.
+//
+// The deformation d_k = Re^T (x_k - x_0) - (x0_k - x0_0) is the small
+// difference of two edge-sized vectors, so it is formed in (hi, lo) pair
+// arithmetic and only then rounded to FP32: the current edges as exact pairs
+// from the split FP64 positions (two-sums of the high parts, plus the
+// differences of the low parts), the rest edges as pairs from k_rest_edges'
+// table, and Re as a pair orthonormal to ~1e-14: the FP32 rotation R plus
+// the correction -R (R^T R - I) / 2 of one Newton-Schulz step, with R^T R
+// from exact products.  In FP32 both edges carry rounding errors of ~6e-8 of
+// an edge, and a rotation orthonormal only to FP32 adds a symmetric part of
+// that size to Re^T e; either one is a spurious strain of ~1e-7, which on a
+// stiff body that deforms little (strains of 1e-5) is a force error of 1e-2
+// per element.  With the pair arithmetic the strain keeps FP32 relative
+// precision, and the rest of the element force (stress, rotation back,
+// node forces) is FP32 with ~1e-7 relative error.
 __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets, const double* __restrict__ x,
                                  const float* __restrict__ e0_f, const float* __restrict__ b_f,
                                  const float* __restrict__ c_f, float* re_f, float4* g_f, float* tile_f,
@@ -2809,10 +2821,11 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
   if (t >= T) return;
   int4 n = tets[t];
   const int nn[4] = {n.x, n.y, n.z, n.w};
-  // current edges x_k - x_0 from the positions as (hi, lo) pairs (integer
-  // instructions; the high parts of nearby nodes subtract exactly), rest
-  // edges precomputed (k_rest_edges)
-  float ep[3][3], e0[3][3];
+  // current edges x_k - x_0 as pairs from the positions' (hi, lo) split
+  // (integer instructions), rounded (ep) for the orientation; rest edges as
+  // pairs from the table (hi: 9 x T words, then lo: 9 x T words)
+  float ep[3][3];
+  DF epp[3][3], e0p[3][3];
   {
     DF p0[3];
 #pragma unroll
@@ -2822,8 +2835,13 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const DF pk = df_of(x[3 * nn[k + 1] + c]);
-        ep[k][c] = (pk.hi - p0[c].hi) + (pk.lo - p0[c].lo);
-        e0[k][c] = e0_f[long(3 * k + c) * T + t];
+        float s, e;
+        two_sum(pk.hi, -p0[c].hi, s, e);
+        e += pk.lo - p0[c].lo;
+        const float h = s + e;
+        epp[k][c] = DF{h, e - (h - s)};
+        ep[k][c] = h;
+        e0p[k][c] = DF{e0_f[long(3 * k + c) * T + t], e0_f[long(9 + 3 * k + c) * T + t]};
       }
   }
   float b[9];
@@ -2863,12 +2881,41 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
   tile_f[tile_word(tile_tets, t, 7)] = quat.w;
 #pragma unroll
   for (int q = 0; q < 9; ++q) re_f[(long)q * T + t] = R[q];
-  // rest-frame displacements d_k = Re^T (x_k - x_0) - (x0_k - x0_0)
+  // Re as a pair: R + R_lo, R_lo = -R (R^T R - I) / 2 (one Newton-Schulz
+  // step; the entries of R^T R - I from exact products and two-sums)
+  float Rl[9];
+  {
+    float E[3][3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+#pragma unroll
+      for (int c = b; c < 3; ++c) {
+        DF acc = {0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float p = R[3 * a + b] * R[3 * a + c];
+          acc = df_add(acc, DF{p, fmaf(R[3 * a + b], R[3 * a + c], -p)});
+        }
+        if (b == c) acc = df_add(acc, DF{-1.f, 0.f});
+        E[b][c] = E[c][b] = acc.hi + acc.lo;
+      }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        Rl[3 * a + c] = -0.5f * (R[3 * a] * E[0][c] + R[3 * a + 1] * E[1][c] + R[3 * a + 2] * E[2][c]);
+  }
+  // rest-frame displacements d_k = Re^T (x_k - x_0) - (x0_k - x0_0) in pairs
   float dk[3][3];
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
-    for (int a = 0; a < 3; ++a) dk[k][a] = (R[a] * ep[k][0] + R[3 + a] * ep[k][1] + R[6 + a] * ep[k][2]) - e0[k][a];
+    for (int a = 0; a < 3; ++a) {
+      DF acc = df_neg(e0p[k][a]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc = df_add(acc, df_mul2(DF{R[3 * c + a], Rl[3 * c + a]}, epp[k][c]));
+      dk[k][a] = acc.hi + acc.lo;
+    }
   float H[3][3];
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -2900,6 +2947,20 @@ __global__ void k_orient_rhs_f32(int T, int warp, const int4* __restrict__ tets,
   const float qv[4] = {quat.x, quat.y, quat.z, quat.w};
 #pragma unroll
   for (int k = 0; k < 4; ++k) g_f[4L * t + k] = make_float4(f[k][0], f[k][1], f[k][2], qv[k]);
+}
+
+// The rotation words of the tiles from the FP32 orientations (re_f), after
+// the tiles were laid out anew.
+__global__ void k_tile_quats_from_re(int T, const float* __restrict__ re_f, float* tile_f, int tile_tets) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  float R[9];
+  for (int q = 0; q < 9; ++q) R[q] = re_f[(long)q * T + t];
+  const float4 quat = rotation_to_quaternion(R);
+  tile_f[tile_word(tile_tets, t, 4)] = quat.x;
+  tile_f[tile_word(tile_tets, t, 5)] = quat.y;
+  tile_f[tile_word(tile_tets, t, 6)] = quat.z;
+  tile_f[tile_word(tile_tets, t, 7)] = quat.w;
 }
 
 __global__ void k_identity_f32(int T, float* re_f, float* tile_f, int tile_tets) {
@@ -3018,8 +3079,9 @@ __global__ void k_wait_timeout(DeviceSync* sync, long long limit, int* status_ou
   *status_out = ok ? 0 : ld_status(&sync->status);
 }
 
-// Rest-frame edges x0_k - x0_0 of every tet (k = 1..3), FP32 (SoA 9 x T):
-// the orientation kernel's rest term, recomputed whenever the model
+// Rest-frame edges x0_k - x0_0 of every tet (k = 1..3) as (hi, lo) float
+// pairs of the FP64 differences (SoA: 9 x T high parts, then 9 x T low
+// parts): the orientation kernel's rest term, recomputed whenever the model
 // coordinates change.
 __global__ void k_rest_edges(int T, const int4* __restrict__ tets, const double* __restrict__ x0, float* e0_f) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -3027,7 +3089,12 @@ __global__ void k_rest_edges(int T, const int4* __restrict__ tets, const double*
   const int4 n = tets[t];
   const int nn[4] = {n.x, n.y, n.z, n.w};
   for (int k = 0; k < 3; ++k)
-    for (int c = 0; c < 3; ++c) e0_f[long(3 * k + c) * T + t] = float(x0[3 * nn[k + 1] + c] - x0[3 * nn[0] + c]);
+    for (int c = 0; c < 3; ++c) {
+      const double d = x0[3 * nn[k + 1] + c] - x0[3 * nn[0] + c];
+      const float hi = float(d);
+      e0_f[long(3 * k + c) * T + t] = hi;
+      e0_f[long(9 + 3 * k + c) * T + t] = float(d - double(hi));
+    }
 }
 
 // Node stiffness scale of the Jacobi preconditioner: k_i = sum over the
@@ -3297,48 +3364,120 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
   return cudaSuccess;
 }
 
+int tile_candidates(const Context& c, int* out, size_t* floats) {
+  const int fixed_sizes[3] = {128, 256, 512};
+  int n = 0;
+  out[n++] = c.tile_tets;  // the balanced size (staged_tiles)
+  for (int s : fixed_sizes) {
+    if (s > kTileMaxTets) continue;
+    bool seen = false;
+    for (int k = 0; k < n; ++k) seen = seen || out[k] == s;
+    if (!seen) out[n++] = s;
+  }
+  size_t most = 0;
+  for (int k = 0; k < n; ++k) {
+    const size_t tiles = (size_t(c.T) + out[k] - 1) / out[k];
+    most = std::max(most, tiles * kTileWords * size_t(out[k]));
+  }
+  if (floats) *floats = std::max<size_t>(most, 1);
+  return n;
+}
+
+cudaError_t set_tile_layout(Context& c, int tile_tets) {
+  const size_t tiles = (size_t(c.T) + tile_tets - 1) / tile_tets;
+  if (tiles * kTileWords * size_t(tile_tets) > c.tile_capacity) return cudaErrorInvalidValue;
+  c.tile_tets = tile_tets;
+  c.tile_magic = tile_magic_of(tile_tets);
+  c.num_tiles = int(tiles);
+  if (c.T == 0) return cudaSuccess;
+  const int nb = (c.T + 255) / 256;
+  // padding tets of the last tile: node 0, no stiffness (never computed)
+  cudaError_t e = cudaMemsetAsync(c.tile_f, 0, sizeof(float) * kTileWords * tiles * size_t(tile_tets), c.stream);
+  if (e != cudaSuccess) return e;
+  k_prepare<<<nb, 256, 0, c.stream>>>(c.T, c.tets, c.Bv, c.D, c.V, c.b_f, c.c_f, c.b_d, c.c_d, c.tile_f,
+                                      c.tile_tets);
+  k_tile_quats_from_re<<<nb, 256, 0, c.stream>>>(c.T, c.re_f, c.tile_f, c.tile_tets);
+  return cudaGetLastError();
+}
+
+// The search: the patch variants (single meshes; they do not read the
+// tiles) once, the tiled variants (tets, staged) at every candidate tile
+// size, each as the best of 3 timings of 4 back-to-back sweeps after one
+// warm-up sweep; the fastest combination wins.  Representative operands:
+// identity orientations and the node positions.  Batches time masked
+// sweeps (every fourth mesh, as late in a step) of the variants that take
+// masks.
 cudaError_t autotune_apply(Context& c) {
   if (c.T == 0) return cudaSuccess;
   int nb = (c.T + 255) / 256, nbn = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
-  // representative operands: identity orientations, the node positions
   k_identity_f32<<<nb, 256, 0, c.stream>>>(c.T, c.re_f, c.tile_f, c.tile_tets);
   k_pack_operand<float4><<<nbn, 256, 0, c.stream>>>(c.N, c.fixed, c.x, c.p_f, c.p_lo, c.q_f);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   cudaEvent_t e0, e1;
   if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
-  if ((e = cudaEventCreate(&e1)) != cudaSuccess) return e;
-  const int saved = c.apply_variant;
-  int best = 0;
+  if ((e = cudaEventCreate(&e1)) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return e;
+  }
   if (c.num_meshes > 1) {
-    best = kApplyTets;
-    // batches time masked sweeps: every fourth mesh, as late in a step
     std::vector<unsigned char> mask(size_t(3) * c.num_meshes, 0);
     for (int m = 0; m < c.num_meshes; m += 4) mask[size_t(m)] = 1;
-    if ((e = cudaMemcpy(c.bmask, mask.data(), mask.size(), cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    e = cudaMemcpy(c.bmask, mask.data(), mask.size(), cudaMemcpyHostToDevice);
   }
-  for (int v = 0; v < kApplyVariants; ++v) {
-    c.apply_variant = v;
-    float best_ms = 1e30f;
-    if (c.num_meshes > 1 && v != kApplyTets && v != kApplyStaged) {
-      c.apply_ms[v] = 0.0;  // batches use the variants that take mesh masks
-      continue;
-    }
+  auto time_sweep = [&](float* best_ms) -> cudaError_t {
+    *best_ms = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
-      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1, true);
+      cudaError_t r = launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 1, true);
+      if (r != cudaSuccess) return r;
       cudaEventRecord(e0, c.stream);
-      launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 4, true);
+      if ((r = launch_apply_sweeps(c, OTFEM_SOLVER_MIXED, 0.01, 4, true)) != cudaSuccess) return r;
       cudaEventRecord(e1, c.stream);
-      if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+      if ((r = cudaEventSynchronize(e1)) != cudaSuccess) return r;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      best_ms = std::min(best_ms, ms / 4.f);
+      *best_ms = std::min(*best_ms, ms / 4.f);
     }
-    c.apply_ms[v] = best_ms;
-    if (best_ms < c.apply_ms[best] || c.apply_ms[best] <= 0.0) best = v;
+    return cudaSuccess;
+  };
+  c.tune_rows = 0;
+  for (int v = 0; v < kApplyVariants; ++v) c.apply_ms[v] = 0.0;
+  int cand[4];
+  const int nc = tile_candidates(c, cand, nullptr);
+  const int balanced = cand[0];
+  int best_v = -1, best_tt = balanced;
+  float best = 1e30f;
+  auto record = [&](int v, int tt, float ms) {
+    if (c.tune_rows < Context::kMaxTuneRows) {
+      c.tune_variant[c.tune_rows] = v;
+      c.tune_tile[c.tune_rows] = tt;
+      c.tune_ms[c.tune_rows] = ms;
+      ++c.tune_rows;
+    }
+    if (c.apply_ms[v] <= 0.0 || ms < c.apply_ms[v]) c.apply_ms[v] = ms;
+    if (ms < best) best = ms, best_v = v, best_tt = tt;
+  };
+  if (c.num_meshes == 1)
+    for (int v = kApplyAtomics; v <= kApplyGather && e == cudaSuccess; ++v) {
+      c.apply_variant = v;
+      float ms;
+      if ((e = time_sweep(&ms)) == cudaSuccess) record(v, 0, ms);
+    }
+  for (int k = 0; k < nc && e == cudaSuccess; ++k) {
+    if ((e = set_tile_layout(c, cand[k])) != cudaSuccess) break;
+    for (int v = kApplyTets; v <= kApplyStaged && e == cudaSuccess; ++v) {
+      c.apply_variant = v;
+      float ms;
+      if ((e = time_sweep(&ms)) == cudaSuccess) record(v, cand[k], ms);
+    }
   }
-  (void)saved;
-  c.apply_variant = best;
+  if (e == cudaSuccess) {
+    c.apply_variant = best_v >= 0 ? best_v : kApplyTets;
+    // the patch variants keep the balanced layout (the tiles still serve the
+    // batch masks and the diagnostics)
+    const int tt = best_v >= kApplyTets ? best_tt : balanced;
+    if (tt != c.tile_tets) e = set_tile_layout(c, tt);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return e == cudaSuccess ? cudaGetLastError() : e;

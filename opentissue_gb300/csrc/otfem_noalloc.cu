@@ -38,7 +38,11 @@ extern "C" {
 OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt, double mass_damping,
                                            const double* x_device, double* y_device) {
   otfem::Context* c = otfem::context_of(h);
-  if (!c || !x_device || !y_device) return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  if (!c) return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  // x_device == y_device == NULL: the per-device set-up alone (below), so a
+  // caller can run it before capturing a stream without real buffers
+  const bool setup_only = !x_device && !y_device;
+  if (!setup_only && (!x_device || !y_device)) return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   if (c->N > kNoAllocMaxNodes)
     return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT,
                         "mesh has " + std::to_string(c->N) + " nodes; otfem_apply_operator_noalloc supports at most " +
@@ -65,6 +69,23 @@ OTFEM_API int otfem_apply_operator_noalloc(otfem_handle h, int solver, double dt
       g_scratch_ptr[dev] = ptr;
     }
     scratch = g_scratch_ptr[dev];
+  }
+  if (setup_only) return OTFEM_OK;
+  // both arrays must be device (or managed) memory of the handle's device:
+  // a host pointer or another device's pointer would fault inside the
+  // kernels instead of returning an error (the query allocates nothing)
+  const double* ptrs[2] = {x_device, y_device};
+  for (const double* ptr : ptrs) {
+    cudaPointerAttributes at;
+    e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT,
+                          std::string("x_device/y_device: not a device pointer (") + cudaGetErrorString(e) + ")");
+    }
+    if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != c->device)
+      return noalloc_fail(OTFEM_ERR_INVALID_ARGUMENT,
+                          "x_device and y_device must be device memory of the handle's device");
   }
   // the pack kernel clears the accumulator before the sweep
   e = otfem::launch_apply_operator_scratch(*c, solver, dt, mass_damping, x_device, y_device, scratch);

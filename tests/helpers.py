@@ -229,3 +229,62 @@ def irregular_mesh(shape=(8, 4, 4), h=0.1, jitter=0.35, seed=0):
     coord = np.ascontiguousarray(pts[used])
     fixed = (coord[:, 0] < 1e-9).astype(np.uint8)
     return tets, coord, fixed
+
+
+class Batch:
+    def __init__(self, beams):
+        self.lib = capi.lib()
+        self.beams = beams
+        self.keep = []
+        descs = (capi.MeshDesc * len(beams))()
+        for k, b in enumerate(beams):
+            tets = np.ascontiguousarray(b["tets"], np.int32)
+            coord = np.ascontiguousarray(b["coord"], np.float64)
+            fixed = np.ascontiguousarray(b["fixed"], np.uint8)
+            self.keep += [tets, coord, fixed]
+            descs[k] = capi.MeshDesc(coord.shape[0], tets.shape[0], tets.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                     coord.ctypes.data_as(_dp), coord.ctypes.data_as(_dp),
+                                     fixed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+        self.h = ctypes.c_void_p()
+        capi.check(self.lib.otfem_batch_create(descs, len(beams), None, ctypes.byref(self.h)))
+        e = np.array([b["young"] for b in beams])
+        nu = np.array([b["poisson"] for b in beams])
+        rho = np.array([b["density"] for b in beams])
+        capi.check(self.lib.otfem_batch_init(self.h, e.ctypes.data_as(_dp), nu.ctypes.data_as(_dp),
+                                             rho.ctypes.data_as(_dp), 1e30, 0.0, 0.0))
+        cnt = ctypes.c_int32()
+        self.noff = np.zeros(len(beams) + 1, np.int32)
+        self.toff = np.zeros(len(beams) + 1, np.int32)
+        capi.check(self.lib.otfem_batch_layout(self.h, ctypes.byref(cnt),
+                                               self.noff.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                               self.toff.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))))
+        assert cnt.value == len(beams)
+        self.N = int(self.noff[-1])
+
+    def get(self, field):
+        out = np.zeros(self.N if field == capi.MASS else (self.N, 3))
+        capi.check(self.lib.otfem_get_nodes(self.h, field, out.ctypes.data_as(_dp), out.size))
+        return out
+
+    def set(self, field, arr):
+        a = np.ascontiguousarray(arr, np.float64).reshape(-1)
+        capi.check(self.lib.otfem_set_nodes(self.h, field, a.ctypes.data_as(_dp), a.size))
+
+    def per_mesh(self, arr):
+        return [arr[self.noff[m]:self.noff[m + 1]] for m in range(len(self.beams))]
+
+    def stats(self):
+        M = len(self.beams)
+        its = np.zeros(M, np.int32)
+        st = np.zeros(M, np.int32)
+        rel = np.zeros(M)
+        rel0 = np.zeros(M)
+        capi.check(self.lib.otfem_batch_stats(self.h, its.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                              st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                              rel.ctypes.data_as(_dp), rel0.ctypes.data_as(_dp)))
+        return its, st, rel, rel0
+
+    def close(self):
+        if self.h:
+            self.lib.otfem_destroy(self.h)
+            self.h = None

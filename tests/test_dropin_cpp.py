@@ -9,10 +9,10 @@ import pytest
 
 from helpers import golden, step_hash
 from opentissue_gb300 import build as ext_build
+from oracle.build import REFERENCE_ROOT as REF_ROOT
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
-REF_ROOT = os.environ.get("OTFEM_REFERENCE_ROOT", "/root/reference")
 HAVE_REF = os.path.exists(os.path.join(REF_ROOT, "OpenTissue", "dynamics", "fem", "fem.h"))
 LIBDIR = os.path.dirname(ext_build.LIB)
 

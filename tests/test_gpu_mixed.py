@@ -1,4 +1,4 @@
-"""The matrix-free solver (FP32 element apply, FP64 CG) against the
+"""The matrix-free solver (FP32 element apply, float-pair CG) against the
 reference's relative-residual runs.  Tolerance from the target: position
 error below 1e-5 relative to the FP64 oracle, measured here against the
 largest displacement of the step (stricter than relative to the positions),

@@ -1,6 +1,8 @@
 """otfem_apply_operator_noalloc: the operator apply with its scratch in the
 library's static device array, checked against otfem_apply_operator (which
-allocates) on two calls in a row, through the C ABI."""
+allocates) on two calls in a row, through the C ABI, for every element-apply
+variant and for a batch handle; and its argument checks (node limit, host
+pointers, the set-up-only call)."""
 import ctypes
 
 import numpy as np
@@ -33,12 +35,7 @@ def _allocating(m, solver, dt, damping, x):
     return y
 
 
-@pytest.mark.parametrize("solver,tol", [(capi.SOLVER_MIXED, 2e-6), (capi.SOLVER_FP64, 1e-13)])
-def test_noalloc_matches_apply_operator(gpu, solver, tol):
-    tets, coord, fixed = beam(12, 5, 4, jitter_seed=6)
-    m = GpuMesh(tets, coord, fixed)
-    m.init()
-    m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
+def _compare(m, fixed, solver, tol):
     dt, damping = 0.01, 2.0
     p = capi.default_params(solver=solver, max_iterations=2000, rtol=1e-6)
     capi.check(m.lib.otfem_simulate_phase(m.h, dt, 1, ctypes.byref(p), capi.PHASE_ORIENT))
@@ -51,6 +48,48 @@ def test_noalloc_matches_apply_operator(gpu, solver, tol):
         assert np.isfinite(got).all()
         assert np.abs(got - want).max() <= tol * np.abs(want).max()
         assert (got[fixed == 1] == 0).all()
+
+
+# every element-apply variant (0, 1: patches; 2: one tet per thread; 3: tiles
+# staged by bulk copies, which the FP64 solver runs as 2), forced as the
+# autotuner would pick it
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("solver,tol", [(capi.SOLVER_MIXED, 2e-6), (capi.SOLVER_FP64, 1e-13)])
+def test_noalloc_matches_apply_operator(gpu, solver, tol, variant):
+    tets, coord, fixed = beam(12, 5, 4, jitter_seed=6)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
+    m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
+    _compare(m, fixed, solver, tol)
+    m.close()
+
+
+def test_noalloc_matches_apply_operator_on_a_batch(gpu):
+    """A batch handle (its node count is every mesh's nodes)."""
+    from helpers import Batch
+    from opentissue_gb300.workloads import random_beams
+    beams = random_beams(3, seed=41, nx=(8, 12), nyz=(3, 4))
+    b = Batch(beams)
+    b.set(capi.F_EXTERNAL, np.zeros((b.N, 3)))
+    fixed = np.concatenate([bm["fixed"] for bm in beams])
+    _compare(b, fixed, capi.SOLVER_MIXED, 2e-6)
+    b.close()
+
+
+def test_noalloc_setup_call_and_pointer_checks(gpu):
+    """x = y = NULL runs only the per-device set-up; host pointers are refused
+    before any kernel runs."""
+    tets, coord, fixed = beam(6, 3, 3, jitter_seed=2)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    capi.check(m.lib.otfem_apply_operator_noalloc(m.h, capi.SOLVER_MIXED, 0.01, 2.0, None, None))
+    x = np.ones((m.N, 3))
+    y = np.zeros((m.N, 3))
+    rc = m.lib.otfem_apply_operator_noalloc(m.h, capi.SOLVER_MIXED, 0.01, 2.0, ctypes.c_void_p(x.ctypes.data),
+                                            ctypes.c_void_p(y.ctypes.data))
+    assert rc == capi.ERR_INVALID_ARGUMENT
+    assert (y == 0).all()
     m.close()
 
 
