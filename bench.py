@@ -550,6 +550,9 @@ def run_ours(args, world, rank, local):
     # the FP64 element apply (the precision the scope names for the CG
     # scalars, at FP64 cost)
     fp64_jacobi = solver_params(solver=capi.SOLVER_FP64)
+    # the network's correction in place of the oldest history direction: the
+    # same four search directions as the projected start
+    learned_h3 = solver_params(warm_start=capi.WARM_START_LEARNED, warm_history=3)
     learned = solver_params(warm_start=capi.WARM_START_LEARNED)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -624,9 +627,14 @@ def run_ours(args, world, rank, local):
     r_learn = timed_run(h_learn, learned)
     clocks = sampler.stop()
     ablations = {}
-    for name, prm in (("plain_jacobi", plain_jacobi), ("projected", projected), ("fp64_jacobi", fp64_jacobi)):
+    for name, prm in (("plain_jacobi", plain_jacobi), ("projected", projected), ("fp64_jacobi", fp64_jacobi),
+                      ("learned_history3", learned_h3)):
         h_ab = make_handle(lib, capi, tets, coord, fixed, stream)
+        if prm.warm_start == capi.WARM_START_LEARNED:
+            net.attach(h_ab)
         ablations[name] = timed_run(h_ab, prm)
+        if prm.warm_start == capi.WARM_START_LEARNED:
+            net.detach(h_ab)
         capi.check(lib.otfem_destroy(h_ab))
     disp = np.abs(r_plain["x"] - coord).max()
     pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))

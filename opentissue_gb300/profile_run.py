@@ -6,10 +6,15 @@ matrix-free steps (OTFEM_SOLVER_MIXED, CG to rel. residual 1e-6) and then
 and the autotuner's choice.  Run it plainly first, then under ncu, e.g.
 
   python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
-  ncu --set full --clock-control none -k regex:k_apply_sweep -s 60 -c 2 -o prof \\
+  ncu --set full --clock-control none -k regex:k_apply_sweep -s 150 -c 2 -o prof \\
       python opentissue_gb300/profile_run.py --dims 128 32 64 --steps 2 --sweeps 4
 
-(the autotuner at otfem_init launches 60 apply sweeps (15 per variant) before the step).
+(the autotuner at otfem_init launches 15 apply sweeps per measured shape before
+the step: 150 on a single mesh -- the two patch variants, the two tiled
+variants at four tile sizes -- and 120 on a batch).  With --batch M the
+mesh is a batch of the first M beams of the 256-beam workload (seed
+20261203; dt 0.005, gravity and each beam's tip force), stepped by one
+persistent launch per step.
 """
 import argparse
 import ctypes
@@ -34,9 +39,12 @@ def main():
     ap.add_argument("--warm-start", default="previous", choices=["previous", "projected"])
     ap.add_argument("--trace", action="store_true",
                     help="print the last step's phases and per-iteration breakdown (SM clock stamps)")
+    ap.add_argument("--batch", type=int, default=0, help="a batch of the first M beams of the batch workload")
     args = ap.parse_args()
     build.build()
     lib = capi.lib()
+    if args.batch:
+        return run_batch(lib, args)
     I, J, K = args.dims
     tets, coord = generate_blocks(I, J, K, 0.1, 0.1, 0.1)
     coord = coord + np.random.default_rng(20261203).uniform(-0.01, 0.01, coord.shape)
@@ -70,8 +78,58 @@ def main():
     if args.sweeps:
         capi.check(lib.otfem_apply_sweeps(h, solver, 0.01, args.sweeps))
     capi.check(lib.otfem_synchronize(h))
-    print(f"tets {T}, nodes {N}, apply variant {variant.value}, sweep ms per variant {ms.tolist()}")
+    print(f"tets {T}, nodes {N}, apply variant {variant.value}, sweep ms per variant {ms.tolist()}, "
+          f"tuner sweeps {15 * tuning_rows(lib, h)}")
     capi.check(lib.otfem_destroy(h))
+
+
+def run_batch(lib, args):
+    from opentissue_gb300 import workloads as wl
+    beams = wl.random_beams(wl.BATCH["count"], seed=wl.BATCH["seed"])[:args.batch]
+    dp = ctypes.POINTER(ctypes.c_double)
+    descs = (capi.MeshDesc * len(beams))()
+    keep = []
+    for k, b in enumerate(beams):
+        t = np.ascontiguousarray(b["tets"], np.int32)
+        c = np.ascontiguousarray(b["coord"], np.float64)
+        f = np.ascontiguousarray(b["fixed"], np.uint8)
+        keep += [t, c, f]
+        descs[k] = capi.MeshDesc(c.shape[0], t.shape[0], t.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                 c.ctypes.data_as(dp), c.ctypes.data_as(dp), f.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    h = ctypes.c_void_p()
+    capi.check(lib.otfem_batch_create(descs, len(beams), None, ctypes.byref(h)))
+    e = np.array([b["young"] for b in beams])
+    nu = np.array([b["poisson"] for b in beams])
+    rho = np.array([b["density"] for b in beams])
+    capi.check(lib.otfem_batch_init(h, e.ctypes.data_as(dp), nu.ctypes.data_as(dp), rho.ctypes.data_as(dp),
+                                    1e30, 0.0, 0.0))
+    if args.variant >= 0:
+        capi.check(lib.otfem_set_apply_variant(h, args.variant))
+    N = sum(b["coord"].shape[0] for b in beams)
+    T = sum(b["tets"].shape[0] for b in beams)
+    mass = np.zeros(N)
+    capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(dp), N))
+    f = wl.batch_forces(beams, mass, 0, 0.005, False)
+    capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
+    p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6, graph=0)
+    st = capi.StepStats()
+    for _ in range(args.steps):
+        capi.check(lib.otfem_simulate_ex(h, 0.005, 1, ctypes.byref(p), ctypes.byref(st)))
+        print(f"batch step: largest iteration count {st.iterations}, rel. residual {st.rel_residual:.3e}")
+    if args.sweeps:
+        capi.check(lib.otfem_apply_sweeps(h, capi.SOLVER_MIXED, 0.005, args.sweeps))
+    capi.check(lib.otfem_synchronize(h))
+    variant = ctypes.c_int32()
+    capi.check(lib.otfem_tuning(h, ctypes.byref(variant), None))
+    print(f"batch of {len(beams)} beams: tets {T}, nodes {N}, apply variant {variant.value}, "
+          f"tuner sweeps {15 * tuning_rows(lib, h)}")
+    capi.check(lib.otfem_destroy(h))
+
+
+def tuning_rows(lib, h):
+    rows = ctypes.c_int32()
+    capi.check(lib.otfem_tuning_search(h, 0, ctypes.byref(rows), None, None, None, None))
+    return rows.value
 
 
 def trace_report(lib, h, dp):

@@ -111,6 +111,7 @@ def test_batch_against_the_fp64_oracle(gpu, oracle):
         x_ref, v_ref = oracle_state(oracle, bm, steps, 1e-11)
         err_x = np.abs(xs[k] - x_ref).max() / np.abs(x_ref - bm["coord"]).max()
         err_v = np.abs(vs[k] - v_ref).max() / np.abs(v_ref).max()
+        print(f"batch mesh {k} E {bm['young']:.3g}: x {err_x:.2e} v {err_v:.2e}")
         assert err_x <= 1e-5 and err_v <= 1e-5, (k, bm["young"], err_x, err_v)
     b.close()
 
