@@ -7,8 +7,13 @@ x = 0 face fixed, E = 5e5 Pa, nu = 0.33, rho = 1000 kg/m^3, mass damping 2.0,
 dt = 0.01 s, gravity -9.81 in y, stiffness warping on, CG to relative
 residual 1e-6.  A "step" is one fem::simulate time step of the whole mesh.
 
-Metric: tet-steps/s = tets x steps / seconds with the learned warm start,
-next to the plain CG (previous-velocity start) on the same trajectory.  The
+Metric: tet-steps/s = tets x steps / seconds.  `value` is the headline arm,
+the projected warm start (CG from the least-energy point on the span of the
+last four velocity changes, Jacobi PCG), next to the plain CG (the
+reference's method: previous-velocity start, no preconditioner) and the
+learned warm start (the trained network's correction added to the same
+search space) on the same trajectory; the learned start measures slower
+than the projected one (config.learned), so it is not the headline.  The
 run first builds the network's training set with the plain solver on beams
 of the workload's family (other jitter seeds; gravity, every other beam
 with a sinusoidal tip load; 2M node samples) and trains it on the GPU
@@ -234,11 +239,18 @@ class OracleError:
         self.errs[step] = (ex, ev)
 
     def result(self):
+        """Largest errors over the sampled steps, per step, and the FP64
+        reference pipeline's own errors when stopped at rel. residual 1e-6
+        (the same tolerance) at those steps."""
         if not self.errs:
             return None
+        f = self.fix
+        e6 = {k: (float(f[f"rtol6_x_err_{k}"]), float(f[f"rtol6_v_err_{k}"])) for k in self.errs}
         return {"x": max(e[0] for e in self.errs.values()), "v": max(e[1] for e in self.errs.values()),
-                "steps": sorted(self.errs), "per_step": {str(k): {"x": e[0], "v": e[1]} for k, e in
-                                                         sorted(self.errs.items())}}
+                "steps": sorted(self.errs),
+                "per_step": {str(k): {"x": e[0], "v": e[1], "fp64_rtol1e6_x": e6[k][0], "fp64_rtol1e6_v": e6[k][1]}
+                             for k, e in sorted(self.errs.items())},
+                "fp64_rtol1e6": {"x": max(e[0] for e in e6.values()), "v": max(e[1] for e in e6.values())}}
 
 
 def get_xv(lib, capi, h, N):
@@ -461,13 +473,16 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
             x, v = get_xv(lib, capi, h, N)
             tag = "sine" if vary else "const"
             ex = ev_ = 0.0
+            ex6 = ev6 = 0.0
             for i in fix["beams"]:
                 i = int(i)
-                xr, vr = fix[f"b{i}_{tag}_x_{step}"], fix[f"b{i}_{tag}_v_{step}"]
-                sl = slice(noff[i], noff[i + 1])
-                ex = max(ex, float(np.abs(x[sl] - xr).max() / np.abs(xr - beams[i]["coord"]).max()))
-                ev_ = max(ev_, float(np.abs(v[sl] - vr).max() / np.abs(vr).max()))
-            errs[step] = (ex, ev_)
+                pre, smp = f"b{i}_{tag}_", noff[i] + fix[f"b{i}_sample"]
+                xr, vr = fix[f"{pre}x_{step}"], fix[f"{pre}v_{step}"]
+                ex = max(ex, float(np.abs(x[smp] - xr).max() / float(fix[f"{pre}disp_{step}"])))
+                ev_ = max(ev_, float(np.abs(v[smp] - vr).max() / float(fix[f"{pre}vmax_{step}"])))
+                ex6 = max(ex6, float(fix[f"{pre}rtol6_x_err_{step}"]))
+                ev6 = max(ev6, float(fix[f"{pre}rtol6_v_err_{step}"]))
+            errs[step] = (ex, ev_, ex6, ev6)
         steps = args.batch_steps
         pre_steps = args.lead_in + args.warmup
         timed_steps(lib, capi, torch, stream, h, p, pre_steps, forces, 0.005, flush_l2, after=after)
@@ -492,7 +507,8 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
         if errs:
             res[name]["oracle_error"] = {
                 "x": max(e[0] for e in errs.values()), "v": max(e[1] for e in errs.values()), "steps": sorted(errs),
-                "beams": [int(i) for i in fix["beams"]]}
+                "beams": [int(i) for i in fix["beams"]],
+                "fp64_rtol1e6": {"x": max(e[2] for e in errs.values()), "v": max(e[3] for e in errs.values())}}
         if name == "plain":
             # the element apply over all 4M tets (325 MB of tiles: beyond the
             # 129 MB L2, the HBM-bound regime), L2 flushed before each sweep
@@ -614,20 +630,20 @@ def run_ours(args, world, rank, local):
         return {"dev_s": dev_s, "its": its, "res": res, "applies": applies, "launches": int(n1.value - n0.value),
                 "x": x, "fext": fext, "oracle_error": check.result()}
 
-    # ---- plain CG (the reference's method), Jacobi-preconditioned CG, the
-    # projected start without the network and the learned start, each on the
-    # same trajectory
+    # ---- plain CG (the reference's method) and the headline arm, the
+    # projected start; then the learned start (the network's correction in the
+    # same search space), Jacobi-preconditioned CG and the other ablations,
+    # each on the same trajectory
     h_plain = make_handle(lib, capi, tets, coord, fixed, stream)
-    h_learn = make_handle(lib, capi, tets, coord, fixed, stream)
-    net.attach(h_learn)
+    h_head = make_handle(lib, capi, tets, coord, fixed, stream)
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
     r_plain = timed_run(h_plain, plain)
-    r_learn = timed_run(h_learn, learned)
+    r_head = timed_run(h_head, projected)
     clocks = sampler.stop()
     ablations = {}
-    for name, prm in (("plain_jacobi", plain_jacobi), ("projected", projected), ("fp64_jacobi", fp64_jacobi),
+    for name, prm in (("learned", learned), ("plain_jacobi", plain_jacobi), ("fp64_jacobi", fp64_jacobi),
                       ("learned_history3", learned_h3)):
         h_ab = make_handle(lib, capi, tets, coord, fixed, stream)
         if prm.warm_start == capi.WARM_START_LEARNED:
@@ -637,7 +653,8 @@ def run_ours(args, world, rank, local):
             net.detach(h_ab)
         capi.check(lib.otfem_destroy(h_ab))
     disp = np.abs(r_plain["x"] - coord).max()
-    pos_diff = float(np.abs(r_learn["x"] - r_plain["x"]).max() / max(disp, 1e-300))
+    pos_diff = float(np.abs(r_head["x"] - r_plain["x"]).max() / max(disp, 1e-300))
+    r_learn = ablations["learned"]
 
     # ---- roofline: the persistent CG kernel timed on its own ---------------
     cg_ms, cg_bytes, cg_applies = [], [], []
@@ -690,27 +707,27 @@ def run_ours(args, world, rank, local):
     sweep_bytes = tet_bytes * T + BYTES_PER_NODE_APPLY * n_free
     sweep_gbs = sweep_bytes / (float(np.median(sweep_ms)) * 1e-3) / 1e9
 
-    # ---- end to end through the C ABI with host buffers (learned) ----------
+    # ---- end to end through the C ABI with host buffers (headline arm) -----
     pin_x = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     pin_v = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     pin_f = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
-    capi.check(lib.otfem_get_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-    capi.check(lib.otfem_get_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
-    pin_f[:] = r_learn["fext"]
+    capi.check(lib.otfem_get_nodes(h_head, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+    capi.check(lib.otfem_get_nodes(h_head, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+    pin_f[:] = r_head["fext"]
     e2e_ms = []
     dist_barrier(world)
     for k in range(args.steps):
         flush_l2()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        capi.check(lib.otfem_set_nodes(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-        capi.check(lib.otfem_set_nodes(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
-        capi.check(lib.otfem_set_nodes(h_learn, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
-        capi.check(lib.otfem_simulate_ex(h_learn, w["dt"], 1, ctypes.byref(learned), None))
+        capi.check(lib.otfem_set_nodes(h_head, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+        capi.check(lib.otfem_set_nodes(h_head, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        capi.check(lib.otfem_set_nodes(h_head, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
+        capi.check(lib.otfem_simulate_ex(h_head, w["dt"], 1, ctypes.byref(projected), None))
         # both downloads queued back to back, one wait
-        capi.check(lib.otfem_get_nodes_async(h_learn, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
-        capi.check(lib.otfem_get_nodes_async(h_learn, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
-        capi.check(lib.otfem_synchronize(h_learn))
+        capi.check(lib.otfem_get_nodes_async(h_head, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
+        capi.check(lib.otfem_get_nodes_async(h_head, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
+        capi.check(lib.otfem_synchronize(h_head))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_s = dist_max(world, sum(e2e_ms) / 1e3)
     dist_barrier(world)
@@ -726,42 +743,62 @@ def run_ours(args, world, rank, local):
             sw["peak_gbs"] = peak
 
     total_tet_steps = T * args.steps * world
-    value = total_tet_steps / r_learn["dev_s"]
+    value = total_tet_steps / r_head["dev_s"]
     plain_value = total_tet_steps / r_plain["dev_s"]
+    learned_value = total_tet_steps / r_learn["dev_s"]
     e2e_value = total_tet_steps / e2e_s
     if rank != 0:
         return
+    fix_note = ("the reference's fem::simulate pipeline in FP64, CG to rel. residual 1e-10 "
+                "(tests/golden/traj_beam128.npz); x over the largest displacement, v over the largest velocity, "
+                "at the sampled steps of 200 from rest; fp64_rtol1e-6: the same pipeline stopped at the GPU's "
+                "tolerance, against the same run")
     line = {
         "metric": METRIC, "value": value, "unit": "tet-steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * r_learn["dev_s"] / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * r_head["dev_s"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 element apply and CG vectors (velocity as f32 hi/lo pairs), f32-pair reductions and scalars, bf16/f32 warm-start network",
+        "dtype": "f32 element apply and CG vectors (velocity as f32 hi/lo pairs), f32-pair reductions and scalars",
         "data": "synthetic",
         "config": {"workload": WORKLOAD["name"],
-                   "warm_start": "learned (node MLP on 1-ring mean inputs, trained in this run) in the projected search space",
+                   "warm_start": "projected: CG starts from the least-energy point on v + span{last "
+                                 f"{projected.warm_history} velocity changes}}.  The learned start (the trained "
+                                 "network's correction added to the same search space) is measured below "
+                                 "(config.learned) and is slower: the network adds no direction the history "
+                                 "does not already span, and costs a features-and-network kernel and one more "
+                                 "search direction per step",
                    "solver": "matrix-free persistent CG (OTFEM_SOLVER_MIXED), CUDA graph per step",
                    "preconditioner": "node Jacobi (OTFEM_PRECONDITIONER_JACOBI, the default)",
-                   "search_space": f"v + span{{network correction, last {learned.warm_history} velocity changes}}",
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
                    "trajectory": f"timed steps {args.lead_in + args.warmup + 1}..{args.lead_in + args.warmup + args.steps} "
                                  f"of the beam's motion from rest (every arm), after {args.lead_in} untimed lead-in "
                                  f"and {args.warmup} warm-up steps",
-                   "iterations_per_step": float(np.mean(r_learn["its"])),
-                   "max_rel_residual": float(np.max(r_learn["res"])),
+                   "iterations_per_step": float(np.mean(r_head["its"])),
+                   "max_rel_residual": float(np.max(r_head["res"])),
                    "plain": {"method": "CG, no preconditioner, previous-velocity start (the reference's)",
                              "value": plain_value, "unit": "tet-steps/s",
                              "ms_per_step": 1e3 * r_plain["dev_s"] / args.steps,
                              "iterations_per_step": float(np.mean(r_plain["its"])),
                              "max_rel_residual": float(np.max(r_plain["res"])),
                              "oracle_error": r_plain["oracle_error"]},
+                   "learned": {"method": "node MLP (v, dv_prev, f_ext, 1-ring mean of Re; 3x64 GELU, BF16 "
+                                         "tensor cores) trained in this run on 2M (state, converged dv) pairs; its "
+                                         "correction joins the last 4 velocity changes in the search space",
+                               "value": learned_value, "unit": "tet-steps/s",
+                               "ms_per_step": 1e3 * r_learn["dev_s"] / args.steps,
+                               "iterations_per_step": float(np.mean(r_learn["its"])),
+                               "learned_over_plain": learned_value / plain_value,
+                               "learned_over_projected": learned_value / value,
+                               "oracle_error": r_learn["oracle_error"]},
                    "ablations": {k: {"value": total_tet_steps / r["dev_s"], "unit": "tet-steps/s",
                                      "ms_per_step": 1e3 * r["dev_s"] / args.steps,
                                      "iterations_per_step": float(np.mean(r["its"])),
                                      "max_rel_residual": float(np.max(r["res"])),
-                                     "oracle_error": r["oracle_error"]} for k, r in ablations.items()},
-                   "learned_over_plain": value / plain_value,
-                   "learned_over_projected": ablations["projected"]["dev_s"] / r_learn["dev_s"],
-                   "position_difference_learned_vs_plain": pos_diff,
+                                     "oracle_error": r["oracle_error"]} for k, r in ablations.items()
+                                 if k != "learned"},
+                   "projected_over_plain": value / plain_value,
+                   "learned_over_plain": learned_value / plain_value,
+                   "learned_over_projected": learned_value / value,
+                   "position_difference_vs_plain": pos_diff,
                    "training": train_info,
                    "other_configurations": extra},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -774,10 +811,8 @@ def run_ours(args, world, rank, local):
                                      "l2": "flushed before each sweep"}},
         "e2e": {"value": e2e_value, "unit": "tet-steps/s", "h2d_bytes_per_step": 3 * 24 * N,
                 "d2h_bytes_per_step": 2 * 24 * N},
-        "oracle_error": dict(r_learn["oracle_error"] or {}, reference="the reference's fem::simulate pipeline in "
-                             "FP64, CG to rel. residual 1e-10 (tests/golden/traj_beam128.npz); x over the largest "
-                             "displacement, v over the largest velocity, at the sampled steps of 200 from rest"),
-        "gpu_launches": r_learn["launches"],
+        "oracle_error": dict(r_head["oracle_error"] or {}, reference=fix_note),
+        "gpu_launches": r_head["launches"],
         "clocks": clocks,
     }
     if not args.no_cpu_baseline:
@@ -787,9 +822,8 @@ def run_ours(args, world, rank, local):
                                 "sample": f"{args.cpu_steps} steps of the full workload from rest, converged CG "
                                           f"({float(np.mean(cits)):.0f} iterations/step), one host core"}
     print(json.dumps(line), flush=True)
-    net.detach(h_learn)
     capi.check(lib.otfem_destroy(h_plain))
-    capi.check(lib.otfem_destroy(h_learn))
+    capi.check(lib.otfem_destroy(h_head))
     net.close()
 
 

@@ -8,6 +8,8 @@
 //  * for every pattern block the ascending-tet list of (tet, local i, local j)
 //    contributions, used by the reference-order assembly gather.
 // All steps are deterministic: counts by atomics, then per-node sorting.
+#include <climits>
+
 #include "otfem_internal.h"
 
 namespace otfem {
@@ -127,32 +129,111 @@ __device__ void insertion_sort(int* a, int n) {
   }
 }
 
+// Warp-wide sorts of short lists: a warp sorts one list of up to kWarpSortMax
+// ints in its shared-memory segment by a bitonic network (lists padded with
+// INT_MAX to the next power of two, at least 32), each lane taking every
+// 32nd compare-exchange of a step.  Longer lists (not met on block meshes,
+// whose nodes touch at most 24 tets) fall back to lane 0's insertion sort.
+constexpr int kWarpSortMax = 256;
+constexpr int kSortWarps = 8;  // warps per CTA of the warp-sort kernels
+
+__device__ void warp_bitonic_sort(int* s, int P) {
+  const int lane = threadIdx.x & 31;
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < P; i += 32) {
+        const int l = i ^ j;
+        if (l > i) {
+          const int a = s[i], b = s[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            s[i] = b;
+            s[l] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+}
+
+__device__ __forceinline__ int sort_size(int m) {
+  int P = 32;
+  while (P < m) P <<= 1;
+  return P;
+}
+
+// Node i's incidence entries (tet << 2 | slot) in ascending order, in place.
 __global__ void k_sort_incidence(int N, const int* __restrict__ ptr, int* ent) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int seg[kSortWarps][kWarpSortMax];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kSortWarps + w;
   if (i >= N) return;
-  insertion_sort(ent + ptr[i], ptr[i + 1] - ptr[i]);
+  int* a = ent + ptr[i];
+  const int m = ptr[i + 1] - ptr[i];
+  if (m > kWarpSortMax) {
+    if (lane == 0) insertion_sort(a, m);
+    return;
+  }
+  int* s = seg[w];
+  const int P = sort_size(m);
+  for (int k = lane; k < P; k += 32) s[k] = k < m ? a[k] : INT_MAX;
+  __syncwarp();
+  warp_bitonic_sort(s, P);
+  for (int k = lane; k < m; k += 32) a[k] = s[k];
 }
 
 // Candidate neighbours of node i (the 4 nodes of each incident tet) sorted and
 // de-duplicated in place in scratch[4*ptr[i] ...]; cnt[i] = distinct count.
+// One warp per node: the node ids of its incident tets gathered into the
+// warp's shared-memory segment, sorted (warp_bitonic_sort), and the distinct
+// ids compacted by ballots into scratch[4*ptr[i] ...] in ascending order.
 __global__ void k_row_unique(int N, const int4* __restrict__ tets, const int* __restrict__ ptr,
                              const int* __restrict__ ent, int* scratch, int* cnt) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int seg[kSortWarps][kWarpSortMax];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kSortWarps + w;
   if (i >= N) return;
-  int* s = scratch + 4L * ptr[i];
-  int m = 0;
-  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
-    int4 n = tets[ent[q] >> 2];
-    s[m++] = n.x;
-    s[m++] = n.y;
-    s[m++] = n.z;
-    s[m++] = n.w;
+  int* out = scratch + 4L * ptr[i];
+  const int q0 = ptr[i], deg = ptr[i + 1] - q0, m = 4 * deg;
+  if (m > kWarpSortMax) {
+    if (lane == 0) {
+      int k = 0;
+      for (int q = q0; q < q0 + deg; ++q) {
+        const int4 n = tets[ent[q] >> 2];
+        out[k++] = n.x;
+        out[k++] = n.y;
+        out[k++] = n.z;
+        out[k++] = n.w;
+      }
+      insertion_sort(out, m);
+      int u = 0;
+      for (int k2 = 0; k2 < m; ++k2)
+        if (k2 == 0 || out[k2] != out[k2 - 1]) out[u++] = out[k2];
+      cnt[i] = u;
+    }
+    return;
   }
-  insertion_sort(s, m);
+  int* s = seg[w];
+  const int P = sort_size(m);
+  for (int q = lane; q < deg; q += 32) {
+    const int4 n = tets[ent[q0 + q] >> 2];
+    s[4 * q] = n.x;
+    s[4 * q + 1] = n.y;
+    s[4 * q + 2] = n.z;
+    s[4 * q + 3] = n.w;
+  }
+  for (int k = m + lane; k < P; k += 32) s[k] = INT_MAX;
+  __syncwarp();
+  warp_bitonic_sort(s, P);
   int u = 0;
-  for (int k = 0; k < m; ++k)
-    if (k == 0 || s[k] != s[k - 1]) s[u++] = s[k];
-  cnt[i] = u;
+  for (int base = 0; base < m; base += 32) {
+    const int k = base + lane;
+    const bool first = k < m && (k == 0 || s[k] != s[k - 1]);
+    const unsigned mask = __ballot_sync(0xffffffffu, first);
+    if (first) out[u + __popc(mask & ((1u << lane) - 1u))] = s[k];
+    u += __popc(mask);
+  }
+  if (lane == 0) cnt[i] = u;
 }
 
 __global__ void k_row_fill(int N, const int* __restrict__ ptr, const int* __restrict__ scratch,
@@ -221,7 +302,8 @@ cudaError_t build_incidence(Context& c) {
   OT_TRY(scan_exclusive(c, c.N, cnt, c.inc_ptr));
   OT_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * (c.N + 1), c.stream));
   k_fill_incidence<<<blocks_for(c.T), kThreads, 0, c.stream>>>(c.T, c.tets, c.inc_ptr, cnt, c.inc_ent);
-  k_sort_incidence<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.inc_ptr, c.inc_ent);
+  k_sort_incidence<<<(c.N + kSortWarps - 1) / kSortWarps, 32 * kSortWarps, 0, c.stream>>>(c.N, c.inc_ptr,
+                                                                                         c.inc_ent);
   OT_TRY(cudaGetLastError());
   OT_TRY(cudaFreeAsync(cnt, c.stream));
   return cudaSuccess;
@@ -232,7 +314,8 @@ cudaError_t build_pattern(Context& c) {
   OT_TRY(cudaMallocAsync(&scratch, sizeof(int) * (16L * c.T + 1), c.stream));
   OT_TRY(cudaMallocAsync(&cnt, sizeof(int) * (c.N + 1), c.stream));
   OT_TRY(cudaMallocAsync(&c.row_ptr, sizeof(int) * (c.N + 1), c.stream));
-  k_row_unique<<<blocks_for(c.N), kThreads, 0, c.stream>>>(c.N, c.tets, c.inc_ptr, c.inc_ent, scratch, cnt);
+  k_row_unique<<<(c.N + kSortWarps - 1) / kSortWarps, 32 * kSortWarps, 0, c.stream>>>(c.N, c.tets, c.inc_ptr,
+                                                                                     c.inc_ent, scratch, cnt);
   OT_TRY(scan_exclusive(c, c.N, cnt, c.row_ptr));
   int nnz = 0;
   OT_TRY(cudaMemcpyAsync(&nnz, c.row_ptr + c.N, sizeof(int), cudaMemcpyDeviceToHost, c.stream));

@@ -51,10 +51,15 @@ def test_search_covers_the_shapes_and_keeps_the_fastest(gpu, dims):
     k = int(np.argmin(ms))
     assert variant == v[k] and (v[k] < 2 or chosen == tt[k]), (v, tt, ms, variant, chosen)
     print(dims, "kept variant", variant, "tile", chosen, dict(zip(zip(v.tolist(), tt.tolist()), ms.round(4))))
-    # every shape computes the same operator
+    # every shape computes the same operator: after one step, the FP64
+    # orientation phase sets the rotations every apply reads (FP64 and FP32
+    # copies and the tiles' quaternions), and the FP64 element apply is the
+    # reference
     m.set(capi.F_EXTERNAL, gravity_force(m.get(capi.MASS), fixed))
     p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6)
     m.step(0.01, True, p)
+    p64 = capi.default_params(solver=capi.SOLVER_FP64, max_iterations=2000, rtol=1e-6)
+    capi.check(m.lib.otfem_simulate_phase(m.h, 0.01, 1, ctypes.byref(p64), capi.PHASE_ORIENT))
     x = np.random.default_rng(4).normal(size=(m.N, 3))
     ref = apply(m, capi.SOLVER_FP64, x)
     for vv, t in zip(v, tt):
