@@ -155,6 +155,7 @@ struct Context {
   // c0..c2), copied to shared memory whole by the bulk-copy engine
   float* tile_f = nullptr;
   int num_tiles = 0, tile_tets = 0;
+  int tile_balanced = 0;  // the tile size that splits the tets evenly over the persistent grid (staged_tiles)
   unsigned long long tile_magic = 0;  // tile_magic_of(tile_tets)
   // learned warm start: the velocity change of the last matrix-free step,
   // the network's initial guess for the next, the per-node network inputs

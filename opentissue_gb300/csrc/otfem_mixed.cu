@@ -3282,6 +3282,7 @@ void staged_tiles(Context& c) {
   long tt = (T + G * rounds - 1) / (G * rounds);
   tt = std::min<long>(kTileMaxTets, std::max(16L, (tt + 15) / 16 * 16));
   c.tile_tets = int(tt);
+  c.tile_balanced = int(tt);
   c.tile_magic = tile_magic_of(c.tile_tets);
   c.num_tiles = int((T + tt - 1) / tt);
 }
@@ -3367,7 +3368,7 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
 int tile_candidates(const Context& c, int* out, size_t* floats) {
   const int fixed_sizes[3] = {128, 256, 512};
   int n = 0;
-  out[n++] = c.tile_tets;  // the balanced size (staged_tiles)
+  out[n++] = c.tile_balanced;  // staged_tiles
   for (int s : fixed_sizes) {
     if (s > kTileMaxTets) continue;
     bool seen = false;

@@ -236,12 +236,13 @@ def test_learned_warm_start_cuts_iterations_at_equal_accuracy(gpu):
 def test_network_gain_over_the_projected_start(gpu):
     """What the trained network adds to the method without it: the learned
     start (the network's correction in the search space) against the
-    projected start alone, with the same history length, on a load not in the
-    training set.  Both reach the same answer (CG to the same tolerance).
-    With four history directions the network's correction lies (nearly) in
-    the span of the history and saves no iteration; with one it adds a
-    direction the history does not hold.  The iteration counts are printed
-    and bounded on both sides of what was measured."""
+    projected start alone, with the same history length (one and four
+    velocity changes), on a load not in the training set.  Both reach the
+    same answer (CG to the same tolerance).  Measured on GB300 (steps 11-50):
+    history 4: 13.50 iterations per step projected, 13.45 learned; history 1:
+    27.3 projected, 28.3 learned.  The network's correction adds nothing the
+    history does not already provide, so the test asserts what was measured:
+    with four history directions the counts agree within 10%."""
     from opentissue_gb300.warmstart import WarmStartNet
     dims = (24, 6, 6)
     tets, coord, fixed = beam(*dims, jitter_seed=11)
