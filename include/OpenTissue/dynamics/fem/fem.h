@@ -13,5 +13,6 @@
 #include <OpenTissue/dynamics/fem/fem_update_original_coord.h>
 #include <OpenTissue/dynamics/fem/fem_export_k.h>
 #include <OpenTissue/dynamics/fem/fem_simulate.h>
+#include <OpenTissue/dynamics/fem/fem_detail.h>
 
 #endif

@@ -52,9 +52,13 @@ inline void init(fem_mesh& mesh, real_type const& young, real_type const& poisso
   std::vector<double> mass(N), vol(T);
   gpu::check(otfem_get_nodes(g.handle(), OTFEM_MASS, mass.data(), int64_t(N)), "fem::init");
   gpu::check(otfem_get_volumes(g.handle(), vol.data()), "fem::init");
-  for (std::size_t i = 0; i < N; ++i) mesh.node_at(i).m_mass = real_type(mass[i]);
+  for (std::size_t i = 0; i < N; ++i) {
+    mesh.node_at(i).m_mass = real_type(mass[i]);
+    mesh.node_at(i).m_gpu_mesh = &mesh;
+  }
   for (std::size_t t = 0; t < T; ++t) {
     typename fem_mesh::tetrahedron_type& e = mesh.tetrahedron_at(t);
+    e.m_gpu_mesh = &mesh;
     e.m_young = young;
     e.m_poisson = poisson;
     e.m_density = density;

@@ -19,6 +19,7 @@ namespace detail {
 template <typename math_types>
 class NodeTraits {
  public:
+  typedef math_types fem_math_types;  // (drop-in) names the owning fem::Mesh<fem_math_types>
   typedef typename math_types::real_type real_type;
   typedef typename math_types::vector3_type vector3_type;
   typedef typename math_types::matrix3x3_type matrix3x3_type;
@@ -39,6 +40,10 @@ class NodeTraits {
   vector3_type m_update;
   vector3_type m_prev;
   vector3_type m_residual;
+  // (drop-in, no counterpart in the reference) the fem::Mesh that owns the
+  // node, set by fem::init: how the fem::detail functions, which take
+  // iterators, reach the mesh's device state
+  void* m_gpu_mesh;
 
  public:
   matrix_iterator Kbegin() { return m_K_row.begin(); }
@@ -48,7 +53,7 @@ class NodeTraits {
   matrix3x3_type& K(int const& column_idx) { return m_K_row[column_idx]; }
   matrix3x3_type& A(int const& column_idx) { return m_A_row[column_idx]; }
 
-  NodeTraits() : m_fixed(false), m_mass(0) {}
+  NodeTraits() : m_fixed(false), m_mass(0), m_gpu_mesh(0) {}
 };
 
 }  // namespace detail

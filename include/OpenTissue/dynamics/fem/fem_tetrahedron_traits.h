@@ -16,6 +16,7 @@ namespace detail {
 template <typename math_types>
 class TetrahedronTraits {
  public:
+  typedef math_types fem_math_types;  // (drop-in) names the owning fem::Mesh<fem_math_types>
   typedef typename math_types::real_type real_type;
   typedef typename math_types::vector3_type vector3_type;
   typedef typename math_types::matrix3x3_type matrix3x3_type;
@@ -36,6 +37,11 @@ class TetrahedronTraits {
   real_type m_yield;
   real_type m_creep;
   real_type m_max;
+  // (drop-in, no counterpart in the reference) the fem::Mesh that owns the
+  // tetrahedron, set by fem::init (see fem_detail.h)
+  void* m_gpu_mesh;
+
+  TetrahedronTraits() : m_gpu_mesh(0) {}
 };
 
 }  // namespace detail

@@ -214,6 +214,34 @@ OTFEM_API int otfem_k_pattern(otfem_handle h, int64_t* nnz_blocks, int32_t* row_
  * reference-solver step. */
 OTFEM_API int otfem_k_values(otfem_handle h, double* host_values);
 
+/* The assembled A_row values (9 doubles per pattern block, the K_row
+ * pattern of otfem_k_pattern) of the last reference dynamics assembly
+ * (fem_dynamics_assembly.h:79-86). */
+OTFEM_API int otfem_a_values(otfem_handle h, double* host_values);
+
+/* The steps of fem::simulate (fem_simulate.h:94-111) one at a time, for host
+ * code that calls OpenTissue's fem::detail functions itself: the reference
+ * solver's kernels and FP64 operation order on the device-resident mesh
+ * (the CG sums its dot products in node order, bit-identical to the
+ * reference).  Synchronous.  stage: */
+enum {
+  OTFEM_STAGE_CLEAR_STIFFNESS_ASSEMBLY = 1, /* detail::clear_stiffness_assembly (fem_clear_stiffness_assembly.h:23-33):
+                                               K and f0 set to zero */
+  OTFEM_STAGE_UPDATE_ORIENTATION = 2,       /* detail::update_orientation (fem_update_orientation.h:22-215) */
+  OTFEM_STAGE_RESET_ORIENTATION = 3,        /* detail::reset_orientation (fem_reset_orientation.h:22-27) */
+  OTFEM_STAGE_STIFFNESS_ASSEMBLY = 4,       /* detail::stiffness_assembly (fem_stiffness_assembly.h:171-209);
+                                               writes K and f0 (the sums of the step, not added to
+                                               values left by an assembly without a clear) */
+  OTFEM_STAGE_ADD_PLASTICITY_FORCE = 5,     /* detail::add_plasticity_force (fem_add_plasticity_force.h:26-204), dt */
+  OTFEM_STAGE_DYNAMICS_ASSEMBLY = 6,        /* detail::dynamics_assembly (fem_dynamics_assembly.h:47-93),
+                                               mass_damping, dt: A and b */
+  OTFEM_STAGE_CONJUGATE_GRADIENTS = 7,      /* detail::conjugate_gradients (fem_conjugate_gradients.h:25-133),
+                                               min_iterations, max_iterations */
+  OTFEM_STAGE_POSITION_UPDATE = 8           /* detail::position_update (fem_position_update.h:25-39), dt */
+};
+OTFEM_API int otfem_reference_stage(otfem_handle h, int stage, double dt, double mass_damping,
+                                    int32_t min_iterations, int32_t max_iterations);
+
 /* Per-tet state: m_Re (9 doubles, row-major), m_plastic (6), m_V (1). */
 OTFEM_API int otfem_get_orientations(otfem_handle h, double* host_re);
 OTFEM_API int otfem_get_plastic(otfem_handle h, double* host_plastic);

@@ -29,6 +29,9 @@ WARM_START_PREVIOUS, WARM_START_LEARNED, WARM_START_PROJECTED = 0, 1, 2
 MAX_WARM_HISTORY = 8
 PRECONDITIONER_NONE, PRECONDITIONER_JACOBI = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2
+# the steps of fem::simulate one at a time (otfem_reference_stage)
+(STAGE_CLEAR_STIFFNESS_ASSEMBLY, STAGE_UPDATE_ORIENTATION, STAGE_RESET_ORIENTATION, STAGE_STIFFNESS_ASSEMBLY,
+ STAGE_ADD_PLASTICITY_FORCE, STAGE_DYNAMICS_ASSEMBLY, STAGE_CONJUGATE_GRADIENTS, STAGE_POSITION_UPDATE) = range(1, 9)
 NUM_APPLY_VARIANTS = 4
 # learned warm start: network state = 9731 weights + 42 normalisation values
 MLP_STATE_SIZE = 9773
@@ -134,6 +137,9 @@ SIGNATURES = {
     "otfem_set_apply_variant": (ctypes.c_int, [_h, ctypes.c_int32]),
     "otfem_tuning_search": (ctypes.c_int, [_h, ctypes.c_int32, _i32p, _i32p, _i32p, _dp, _i32p]),
     "otfem_set_apply_shape": (ctypes.c_int, [_h, ctypes.c_int32, ctypes.c_int32]),
+    "otfem_a_values": (ctypes.c_int, [_h, _dp]),
+    "otfem_reference_stage": (ctypes.c_int, [_h, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                             ctypes.c_int32]),
     "otfem_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "otfem_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "otfem_launch_count": (ctypes.c_int, [_h, _i64p]),

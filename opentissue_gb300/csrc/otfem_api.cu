@@ -770,6 +770,70 @@ int otfem_k_values(otfem_handle h, double* vals) {
   return OTFEM_OK;
 }
 
+int otfem_a_values(otfem_handle h, double* vals) {
+  if (!h || (!vals && h->c.nnz)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  Context& c = h->c;
+  if (c.nnz) OT_CUDA(cudaMemcpyAsync(vals, c.A, sizeof(double) * 9 * size_t(c.nnz), cudaMemcpyDeviceToHost, c.stream));
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  return OTFEM_OK;
+}
+
+// One step of fem::simulate (fem_simulate.h:94-111) on its own, with the
+// reference solver's kernels and arithmetic order.
+int otfem_reference_stage(otfem_handle h, int stage, double dt, double mass_damping, int32_t min_iterations,
+                          int32_t max_iterations) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (c.num_meshes > 1) return fail(OTFEM_ERR_UNSUPPORTED, "the reference's steps run on single meshes");
+  const bool needs_dt = stage == OTFEM_STAGE_ADD_PLASTICITY_FORCE || stage == OTFEM_STAGE_DYNAMICS_ASSEMBLY ||
+                        stage == OTFEM_STAGE_POSITION_UPDATE;
+  if (needs_dt && !(dt > 0.0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "time step must be positive");
+  // a cached matrix-free step graph stays valid: the stages write the same
+  // node arrays a step reads at its start
+  cudaError_t e = cudaSuccess;
+  switch (stage) {
+    case OTFEM_STAGE_CLEAR_STIFFNESS_ASSEMBLY:
+      e = cudaMemsetAsync(c.f0, 0, sizeof(double) * 3 * size_t(c.N), c.stream);
+      if (e == cudaSuccess && c.nnz) e = cudaMemsetAsync(c.K, 0, sizeof(double) * 9 * size_t(c.nnz), c.stream);
+      break;
+    case OTFEM_STAGE_UPDATE_ORIENTATION:
+    case OTFEM_STAGE_RESET_ORIENTATION:
+      e = otfem::launch_orientation(c, stage == OTFEM_STAGE_UPDATE_ORIENTATION);
+      c.re_f32_pending = false;
+      c.launches += 1;
+      break;
+    case OTFEM_STAGE_STIFFNESS_ASSEMBLY:
+      e = otfem::launch_assembly(c);
+      c.k_assembled = true;
+      c.launches += 2;
+      break;
+    case OTFEM_STAGE_ADD_PLASTICITY_FORCE:
+      e = otfem::launch_plasticity(c, dt);
+      c.launches += 2;
+      break;
+    case OTFEM_STAGE_DYNAMICS_ASSEMBLY:
+      e = otfem::launch_dynamics_assembly(c, mass_damping, dt);
+      c.launches += 1;
+      break;
+    case OTFEM_STAGE_CONJUGATE_GRADIENTS:
+      if (min_iterations < 0 || max_iterations < 0)
+        return fail(OTFEM_ERR_INVALID_ARGUMENT, "iteration counts must not be negative");
+      e = otfem::launch_reference_cg(c, min_iterations, max_iterations, true);
+      c.launches += 1;
+      break;
+    case OTFEM_STAGE_POSITION_UPDATE:
+      e = otfem::launch_position_update(c, dt);
+      c.launches += 1;
+      break;
+    default:
+      return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown stage");
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "reference stage");
+  OT_CUDA(cudaStreamSynchronize(c.stream));
+  return OTFEM_OK;
+}
+
 static int get_tet_array(otfem_handle h, const double* src, size_t per, double* dst) {
   if (!h || (!dst && h->c.T)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
   Context& c = h->c;

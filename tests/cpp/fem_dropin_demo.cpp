@@ -5,9 +5,13 @@
 // with libotfem_gpu.so; used by tests/test_dropin_cpp.py.
 //
 // usage: fem_dropin_demo I J K steps solver out.bin [export.bin]
-//   solver: reference | sequential | mixed | projected
+//   solver: reference | sequential | mixed | projected | detail
+//     (detail: each step is the reference's own sequence of fem::detail
+//     calls, fem_simulate.h:94-111, instead of fem::simulate)
 //   out.bin: per step the N x 3 positions then the N x 3 velocities (doubles)
-//   export.bin: fem::export_K triplets after step 1 (int row, int col, double)
+//   export.bin: fem::export_K triplets after step 1 (int row, int col, double);
+//     in detail mode the host m_K_row maps after step 1 instead (int row, int
+//     col, 9 doubles per entry, rows and keys in order)
 #include <OpenTissue/configuration.h>
 #include <OpenTissue/core/math/math_basic_types.h>
 #include <OpenTissue/core/containers/t4mesh/util/t4mesh_block_generator.h>
@@ -62,10 +66,20 @@ int main(int argc, char** argv) {
         n->m_f_external.clear();
         if (!n->m_fixed) n->m_f_external(1) = -9.81 * n->m_mass;
       }
-      if (std::strcmp(solver, "reference") == 0)
+      if (std::strcmp(solver, "detail") == 0) {
+        namespace fd = OpenTissue::fem::detail;
+        fd::clear_stiffness_assembly(mesh.node_begin(), mesh.node_end());
+        fd::update_orientation(mesh.tetrahedron_begin(), mesh.tetrahedron_end());
+        fd::stiffness_assembly(mesh.tetrahedron_begin(), mesh.tetrahedron_end());
+        fd::add_plasticity_force(mesh.tetrahedron_begin(), mesh.tetrahedron_end(), 0.01);
+        fd::dynamics_assembly(mesh, 2.0, 0.01);
+        fd::conjugate_gradients(mesh, 20u, 20u);
+        fd::position_update(mesh, 0.01);
+      } else if (std::strcmp(solver, "reference") == 0) {
         OpenTissue::fem::simulate(mesh, 0.01, true);
-      else
+      } else {
         OpenTissue::fem::simulate(mesh, 0.01, true, params);
+      }
       size_t i = 0;
       for (mesh_type::node_iterator n = mesh.node_begin(); n != mesh.node_end(); ++n, ++i)
         for (int c = 0; c < 3; ++c) buf[3 * i + c] = n->m_coord(c);
@@ -74,7 +88,21 @@ int main(int argc, char** argv) {
       for (mesh_type::node_iterator n = mesh.node_begin(); n != mesh.node_end(); ++n, ++i)
         for (int c = 0; c < 3; ++c) buf[3 * i + c] = n->m_velocity(c);
       std::fwrite(buf.data(), sizeof(double), buf.size(), out);
-      if (s == 1 && argc > 7) {
+      if (s == 1 && argc > 7 && std::strcmp(solver, "detail") == 0) {
+        FILE* ex = std::fopen(argv[7], "wb");
+        if (!ex) return 3;
+        for (mesh_type::node_iterator n = mesh.node_begin(); n != mesh.node_end(); ++n)
+          for (mesh_type::node_type::matrix_iterator K = n->Kbegin(); K != n->Kend(); ++K) {
+            int rc[2] = {int(n->idx()), K->first};
+            std::fwrite(rc, sizeof(int), 2, ex);
+            for (int r = 0; r < 3; ++r)
+              for (int c = 0; c < 3; ++c) {
+                double v = K->second(r, c);
+                std::fwrite(&v, sizeof(double), 1, ex);
+              }
+          }
+        std::fclose(ex);
+      } else if (s == 1 && argc > 7) {
         TripletSink sink;
         OpenTissue::fem::export_K(mesh, sink);
         FILE* ex = std::fopen(argv[7], "wb");
@@ -96,6 +124,23 @@ int main(int argc, char** argv) {
       std::fprintf(stderr, "expected std::logic_error\n");
       return 4;
     } catch (std::logic_error const&) {
+    }
+    try {
+      OpenTissue::fem::detail::update_orientation(fresh.tetrahedron_begin(), fresh.tetrahedron_end());
+      std::fprintf(stderr, "expected std::logic_error from fem::detail\n");
+      return 4;
+    } catch (std::logic_error const&) {
+    }
+    if (std::strcmp(solver, "detail") == 0) {
+      // the device runs a step on whole meshes: a partial range throws
+      mesh_type::tetrahedron_iterator last = mesh.tetrahedron_begin();
+      ++last;
+      try {
+        OpenTissue::fem::detail::update_orientation(mesh.tetrahedron_begin(), last);
+        std::fprintf(stderr, "expected std::invalid_argument\n");
+        return 4;
+      } catch (std::invalid_argument const&) {
+      }
     }
   } catch (std::exception const& e) {
     std::fprintf(stderr, "error: %s\n", e.what());

@@ -86,6 +86,28 @@ def test_dropin_cpp_bitwise_vs_reference(gpu, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("core", ["stub", "real"])
+def test_dropin_detail_steps_bitwise_vs_reference(gpu, tmp_path, core):
+    """The reference's own step sequence written as host code against the
+    drop-in fem::detail functions (fem_simulate.h:94-111): every step's
+    positions and velocities bit-identical to the reference's fem::simulate
+    over 100 steps, and after step 1 the host m_K_row maps filled with the
+    reference's keys and values."""
+    if core == "real" and not HAVE_REF:
+        pytest.skip("OpenTissue source tree not present on this machine")
+    g = golden("config1")
+    exe = compile_demo(str(tmp_path), core)
+    data = _run_demo(exe, str(tmp_path), (10, 4, 4), 100, "detail", export=True)
+    assert [step_hash(d[0], d[1]) for d in data] == list(g["hashes"])
+    raw = np.fromfile(os.path.join(str(tmp_path), "export.bin"),
+                      dtype=np.dtype([("r", "<i4"), ("c", "<i4"), ("v", "<f8", (3, 3))]))
+    rp, cols = g["k_row_ptr"], g["k_cols"]
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    assert np.array_equal(raw["r"], rows) and np.array_equal(raw["c"], cols)
+    assert np.array_equal(raw["v"], g["k_values_1"])
+
+
+@pytest.mark.gpu
 def test_dropin_cpp_default_and_mixed_solvers(gpu, oracle, tmp_path):
     g = golden("config1")
     exe = compile_demo(str(tmp_path), "stub")
