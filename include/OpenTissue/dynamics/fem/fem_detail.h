@@ -73,12 +73,15 @@ struct TetCount {
   std::size_t operator()(mesh_type& m) const { return m.size_tetrahedra(); }
 };
 
-// Host node field -> device.
+// Host node field -> device.  The copy is queued asynchronously from the
+// field's own page-locked staging buffer; every stage ends with a stream
+// synchronisation, so a buffer is rewritten only after its last copy ran.
 template <typename mesh_type>
 inline void upload(mesh_type& mesh, int field, char const* where) {
   gpu::State& g = mesh.gpu_state();
   std::size_t const N = mesh.size_nodes();
-  double* buf = g.x();
+  double* buf = field == OTFEM_COORD ? g.x() : field == OTFEM_MODEL_COORD ? g.x0() : field == OTFEM_VELOCITY ? g.v()
+                                                                                                         : g.f();
   for (std::size_t i = 0; i < N; ++i) {
     typename mesh_type::node_type& n = mesh.node_at(i);
     typename mesh_type::vector3_type const& v = field == OTFEM_COORD         ? n.m_coord
@@ -99,7 +102,8 @@ inline void upload_fixed(mesh_type& mesh, char const* where) {
   gpu::check(otfem_set_fixed(g.handle(), fx, int64_t(N)), where);
 }
 
-// Device node field -> host.
+// Device node field -> host (synchronous; after the stage's synchronisation,
+// so the staging buffer it uses has no copy in flight).
 template <typename mesh_type>
 inline void download(mesh_type& mesh, int field, char const* where) {
   typedef typename mesh_type::real_type real_type;
