@@ -373,7 +373,10 @@ OTFEM_API int otfem_check_wait_timeout(otfem_handle h, int64_t cycles, int32_t* 
  * beta, then six stamps in SM clock cycles since the kernel started (taken by
  * the middle CTA of the grid): apply sweep done, its barrier passed,
  * reduction phase done, reduction complete, update phase done, update
- * synchronised. */
+ * synchronised.  For a batch, one row per iteration of its persistent launch
+ * with the number of meshes still iterating in column 0 and 1 in column 2
+ * where a residual-refresh sweep follows (columns 1 and 3 are 0), then the
+ * same six stamps. */
 OTFEM_API int otfem_solver_trace(otfem_handle h, double* out, int32_t max_rows, int32_t* rows);
 /* Phases of the last OTFEM_SOLVER_MIXED solve of one mesh: 8 stamps in SM
  * clock cycles since the kernel started (middle CTA): b done, the

@@ -147,6 +147,7 @@ struct MixedArgs {
   int num_meshes;
   const int* mesh_of_node;
   const int* mesh_of_tet;
+  const int* mesh_tet_start;            // num_meshes + 1: the first tet of each mesh (batches)
   BatchMesh* bm;
   double* bacc;
   unsigned char* bmask;
@@ -1321,8 +1322,75 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
 __device__ __forceinline__ bool tet_in_sweep(const MixedArgs& a, const unsigned char* mask, int t) {
   return t < a.T && (!mask || mask[a.mesh_of_tet[t]]);
 }
+// A batch's masked sweep over the meshes in the sweep only (at most kBlock
+// meshes): every CTA lists them with a CTA-wide scan of the mask (meshes
+// without tets left out) and walks their tets as one virtual range, mesh j's
+// tets at [s_pref[j], s_pref[j + 1]), so that a sweep late in a step, when a
+// few meshes still iterate, costs in proportion to their tets instead of
+// reading the mesh id of every tet of the batch.
+__device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                                    const unsigned char* mask) {
+  __shared__ int s_beg[kBlock], s_pref[kBlock + 1], s_wsum[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, m = threadIdx.x;
+  __syncthreads();  // the previous sweep's readers of the lists are done
+  int beg = 0, cnt = 0;
+  if (m < a.num_meshes && mask[m]) {
+    beg = a.mesh_tet_start[m];
+    cnt = a.mesh_tet_start[m + 1] - beg;
+  }
+  // CTA-wide inclusive scans of the flags and of the tet counts (warp
+  // shuffles, then the warp totals by warp 0)
+  int f = cnt > 0 ? 1 : 0, c = f ? cnt : 0;
+  int fi = f, ci = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yf = __shfl_up_sync(0xffffffffu, fi, o), yc = __shfl_up_sync(0xffffffffu, ci, o);
+    if (lane >= o) fi += yf, ci += yc;
+  }
+  __shared__ int s_wcnt[kBlock / 32];
+  if (lane == 31) s_wsum[warp] = fi, s_wcnt[warp] = ci;
+  __syncthreads();
+  if (warp == 0) {
+    int tf = lane < kBlock / 32 ? s_wsum[lane] : 0, tc = lane < kBlock / 32 ? s_wcnt[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int yf = __shfl_up_sync(0xffffffffu, tf, o), yc = __shfl_up_sync(0xffffffffu, tc, o);
+      if (lane >= o) tf += yf, tc += yc;
+    }
+    if (lane < kBlock / 32) s_wsum[lane] = tf, s_wcnt[lane] = tc;  // inclusive totals through each warp
+  }
+  __syncthreads();
+  const int f_before = (warp ? s_wsum[warp - 1] : 0) + fi - f, c_before = (warp ? s_wcnt[warp - 1] : 0) + ci - c;
+  const int n = s_wsum[kBlock / 32 - 1], total = s_wcnt[kBlock / 32 - 1];
+  if (f) {
+    s_beg[f_before] = beg;
+    s_pref[f_before] = c_before;
+  }
+  if (threadIdx.x == 0) s_pref[n] = total;
+  __syncthreads();
+  const int TT = a.tile_tets, stride = gridDim.x * blockDim.x;
+  for (int v = int(sweep_first()); v < total; v += stride) {
+    // the list entry holding v: the last j with s_pref[j] <= v (the counts
+    // are positive, so s_pref increases strictly)
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_pref[mid] <= v) lo = mid;
+      else hi = mid - 1;
+    }
+    const int t = s_beg[lo] + (v - s_pref[lo]);
+    const int tile = tile_of(t, a.tile_magic);
+    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
+  }
+}
+
 __device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
                                  const unsigned char* mask) {
+  if (mask && a.mesh_tet_start && a.num_meshes <= kBlock && blockDim.x == kBlock) {
+    apply_active_meshes(a, u4, ulo, q4, scale, mask);
+    return;
+  }
   const int T = a.T, TT = a.tile_tets, stride = gridDim.x * blockDim.x;
   int t = int(sweep_first());
   bool act = tet_in_sweep(a, mask, t);
@@ -2657,12 +2725,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   if (!batch_reduce(a, round, FinBatchStart(), counts)) return;
   if (tracer) phase_stamp(a, 2, t_start);
   int n_active = counts[0];
+  __shared__ double stamp[6];  // trace stamps, written by the tracer thread only
 
   for (int it = 0; n_active > 0 && it < a.max_it; ++it) {
+    const int active_before = n_active;
     // q += dt^2 K' p for the meshes still iterating
     apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_apply);
     ++sweeps;
+    if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (tracer) stamp[1] = double(cycles_now() - t_start);
     // q = diag p + q; the totals of FinPcgF per mesh
     {
       SegSum<7> ss;
@@ -2691,7 +2763,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       }
       ss.flush(acc_half(round + 1));
     }
+    if (tracer) stamp[2] = double(cycles_now() - t_start);
     if (!batch_reduce(a, round, FinBatchIter(), counts)) return;
+    if (tracer) stamp[3] = double(cycles_now() - t_start);
     n_active = counts[0];
     const bool any_refresh = counts[1] > 0;
     // v += alpha p, r -= alpha q, p = r + beta p with each mesh's scalars
@@ -2714,7 +2788,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
       a.q_f[i] = zero4;
     }
+    if (tracer) stamp[4] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    // trace row: the meshes iterating, whether a refresh sweep follows
+    if (tracer) trace_row(a, it, double(active_before), 0.0, any_refresh ? 1.0 : 0.0, 0.0, stamp, t_start);
     if (any_refresh) {
       // r = b - A v (residual replacement, FP64) for the meshes due
       apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem, mask_refresh);
@@ -2769,8 +2846,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     a.dv_last[i] = make_float4(dv[0].hi, dv[1].hi, dv[2].hi, 0.f);
     if (a.hist) record_velocity_change(a, i, dv);
   }
+  if (tracer) phase_stamp(a, 4, t_start);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    phase_stamp(a, 4, t_start);
     // batch summary: the largest iteration count and relative residual, the
     // worst status
     int its = 0, st = ld_status(&a.sync->status), warn = 0;
@@ -3564,6 +3641,7 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.num_meshes = c.num_meshes;
   a.mesh_of_node = c.mesh_of_node;
   a.mesh_of_tet = c.mesh_of_tet;
+  a.mesh_tet_start = c.mesh_tet_start;
   a.bm = c.bmesh;
   a.bacc = c.bacc;
   a.bmask = c.bmask;

@@ -111,11 +111,16 @@ def run_batch(lib, args):
     capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(dp), N))
     f = wl.batch_forces(beams, mass, 0, 0.005, False)
     capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
-    p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6, graph=0)
+    warm = capi.WARM_START_PROJECTED if args.warm_start == "projected" else capi.WARM_START_PREVIOUS
+    p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6, graph=0, warm_start=warm)
     st = capi.StepStats()
-    for _ in range(args.steps):
+    for k in range(args.steps):
+        f = wl.batch_forces(beams, mass, k, 0.005, False)
+        capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
         capi.check(lib.otfem_simulate_ex(h, 0.005, 1, ctypes.byref(p), ctypes.byref(st)))
         print(f"batch step: largest iteration count {st.iterations}, rel. residual {st.rel_residual:.3e}")
+    if args.trace:
+        batch_trace_report(lib, h, dp, len(beams))
     if args.sweeps:
         capi.check(lib.otfem_apply_sweeps(h, capi.SOLVER_MIXED, 0.005, args.sweeps))
     capi.check(lib.otfem_synchronize(h))
@@ -130,6 +135,42 @@ def tuning_rows(lib, h):
     rows = ctypes.c_int32()
     capi.check(lib.otfem_tuning_search(h, 0, ctypes.byref(rows), None, None, None, None))
     return rows.value
+
+
+def sm_mhz():
+    import subprocess
+    try:
+        return float(subprocess.run(["nvidia-smi", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits", "-i",
+                                     "0"], capture_output=True, text=True, timeout=20).stdout.split()[0])
+    except (OSError, ValueError, IndexError, subprocess.SubprocessError):
+        return 2070.0
+
+
+def batch_trace_report(lib, h, dp, meshes):
+    """Per iteration of the last batch step: the meshes still iterating and
+    the time of the iteration and of its apply sweep (middle CTA's stamps,
+    microseconds), summed over groups of iterations."""
+    mhz = sm_mhz()
+    ph = np.zeros(8)
+    capi.check(lib.otfem_solver_phases(h, ph.ctypes.data_as(dp)))
+    tr = np.zeros((256, 10))
+    rows = ctypes.c_int32()
+    capi.check(lib.otfem_solver_trace(h, tr.ctypes.data_as(dp), 256, ctypes.byref(rows)))
+    tr = tr[:rows.value]
+    if rows.value == 0:
+        return
+    start = np.concatenate([[ph[2]], tr[:-1, 9]])
+    it_us = (tr[:, 9] - start) / mhz
+    sweep_us = (tr[:, 4] - start) / mhz
+    print(f"batch phases (us): b {ph[0] / mhz:.1f}, start sweeps {(ph[1] - ph[0]) / mhz:.1f}, "
+          f"start {(ph[2] - ph[1]) / mhz:.1f}, CG loop {(ph[3] - ph[2]) / mhz:.1f}, update {(ph[4] - ph[3]) / mhz:.1f}")
+    for lo, hi in ((0, 5), (5, 10), (10, 20), (20, 40), (40, 80), (80, 256)):
+        sel = slice(lo, min(hi, rows.value))
+        if lo >= rows.value:
+            break
+        print(f"iterations {lo}-{min(hi, rows.value) - 1}: meshes iterating {tr[sel, 0].min():.0f}-{tr[sel, 0].max():.0f} "
+              f"of {meshes}, per iteration {it_us[sel].mean():.1f} us (apply sweep {sweep_us[sel].mean():.1f} us), "
+              f"{it_us[sel].sum():.0f} us in all")
 
 
 def trace_report(lib, h, dp):
