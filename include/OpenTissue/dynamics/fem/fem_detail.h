@@ -40,6 +40,7 @@
 #include <cstddef>
 #include <iterator>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 namespace OpenTissue {
