@@ -195,6 +195,7 @@ struct Context {
   unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
   size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
+  bool stream_tiles = false;      // the tiles exceed L2: tiled sweeps read them past L1 (set_tile_layout)
   double apply_ms[OTFEM_NUM_APPLY_VARIANTS] = {};  // measured time of one sweep per variant (best tile size)
   // the autotuner's search (autotune_apply): every measured (variant, tile
   // size; 0 for the patch variants, which do not read tiles) and its time

@@ -128,6 +128,7 @@ struct MixedArgs {
   const int* patch_inc_ptr;             // per patch node: offsets into patch_inc
   const unsigned short* patch_inc;      // (patch-local tet << 2) | slot, ascending tet
   int apply_variant;                    // kApplyAtomics / kApplyGather / kApplyTets / kApplyStaged
+  int stream_tiles;                     // tiled sweeps read the tile words past L1 (tiles beyond L2)
   const float* tile_f;                  // staged apply tiles (see Context::tile_f)
   int tile_tets, num_tiles;
   unsigned long long tile_magic;        // tile_of(t, tile_magic) = t / tile_tets
@@ -1249,17 +1250,36 @@ __device__ void staged_sweep(const MixedArgs& a, unsigned char* smem, const unsi
   }
 }
 
+// One tile word.  Stream: for sweeps whose tiles do not fit in L2 and stream
+// from HBM, the word is read past L1 and marked first to be evicted from L2
+// (ld.global.nc.L1::no_allocate with an L2::evict_first cache policy): a tile
+// word is read once per sweep, so L2 is left to the node vectors, which the
+// sweep gathers and accumulates and the node passes read again.
+template <bool Stream>
+__device__ __forceinline__ float ld_tile_word(const float* p) {
+  if constexpr (Stream) {
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    float v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+  } else {
+    return *p;
+  }
+}
+
 // A staged tile's words for tet `tid`: node ids, rotation, B-vectors, constants.
-struct StagedTet {
+template <bool Stream = false>
+struct StagedTetT {
   int nn[4];
   float Re[9], b[9], c0, c1, c2;
-  __device__ __forceinline__ StagedTet(const float* w, int TT, int tid) {
+  __device__ __forceinline__ StagedTetT(const float* w, int TT, int tid) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) nn[k] = __float_as_int(w[k * TT + tid]);
+    for (int k = 0; k < 4; ++k) nn[k] = __float_as_int(ld_tile_word<Stream>(w + k * TT + tid));
     load_rest(w, TT, tid);
   }
   // with the node ids already loaded (the tets variant loads them one tet ahead)
-  __device__ __forceinline__ StagedTet(const float* w, int TT, int tid, const int4& ids) {
+  __device__ __forceinline__ StagedTetT(const float* w, int TT, int tid, const int4& ids) {
     nn[0] = ids.x;
     nn[1] = ids.y;
     nn[2] = ids.z;
@@ -1267,21 +1287,26 @@ struct StagedTet {
     load_rest(w, TT, tid);
   }
   __device__ __forceinline__ void load_rest(const float* w, int TT, int tid) {
-    quaternion_to_rotation(make_float4(w[4 * TT + tid], w[5 * TT + tid], w[6 * TT + tid], w[7 * TT + tid]), Re);
+    quaternion_to_rotation(make_float4(ld_tile_word<Stream>(w + 4 * TT + tid), ld_tile_word<Stream>(w + 5 * TT + tid),
+                                       ld_tile_word<Stream>(w + 6 * TT + tid), ld_tile_word<Stream>(w + 7 * TT + tid)),
+                           Re);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT + tid];
-    c0 = w[17 * TT + tid];
-    c1 = w[18 * TT + tid];
-    c2 = w[19 * TT + tid];
+    for (int k = 0; k < 9; ++k) b[k] = ld_tile_word<Stream>(w + (8 + k) * TT + tid);
+    c0 = ld_tile_word<Stream>(w + 17 * TT + tid);
+    c1 = ld_tile_word<Stream>(w + 18 * TT + tid);
+    c2 = ld_tile_word<Stream>(w + 19 * TT + tid);
   }
 };
+using StagedTet = StagedTetT<false>;
 
 // Node ids of tet t from its tile (words 0..3), or zeros past the end.
+template <bool Stream = false>
 __device__ __forceinline__ int4 tile_node_ids(const MixedArgs& a, int t) {
   if (t >= a.T) return make_int4(0, 0, 0, 0);
   const int TT = a.tile_tets, tile = tile_of(t, a.tile_magic);
   const float* w = a.tile_f + size_t(tile) * kTileWords * TT + (t - tile * TT);
-  return make_int4(__float_as_int(w[0]), __float_as_int(w[TT]), __float_as_int(w[2 * TT]), __float_as_int(w[3 * TT]));
+  return make_int4(__float_as_int(ld_tile_word<Stream>(w)), __float_as_int(ld_tile_word<Stream>(w + TT)),
+                   __float_as_int(ld_tile_word<Stream>(w + 2 * TT)), __float_as_int(ld_tile_word<Stream>(w + 3 * TT)));
 }
 
 // q += dt^2 K_e u for one tet (FP32; u with an optional lo part).
@@ -1328,6 +1353,7 @@ __device__ __forceinline__ bool tet_in_sweep(const MixedArgs& a, const unsigned 
 // tets at [s_pref[j], s_pref[j + 1]), so that a sweep late in a step, when a
 // few meshes still iterate, costs in proportion to their tets instead of
 // reading the mesh id of every tet of the batch.
+template <bool Stream>
 __device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
                                     const unsigned char* mask) {
   __shared__ int s_beg[kBlock], s_pref[kBlock + 1], s_wsum[kBlock / 32];
@@ -1380,31 +1406,40 @@ __device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const 
     }
     const int t = s_beg[lo] + (v - s_pref[lo]);
     const int tile = tile_of(t, a.tile_magic);
-    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
+    const StagedTetT<Stream> e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
   }
 }
 
-__device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
-                                 const unsigned char* mask) {
+template <bool Stream>
+__device__ void apply_tets_tiled_impl(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4,
+                                      float scale, const unsigned char* mask) {
   if (mask && a.mesh_tet_start && a.num_meshes <= kBlock && blockDim.x == kBlock) {
-    apply_active_meshes(a, u4, ulo, q4, scale, mask);
+    apply_active_meshes<Stream>(a, u4, ulo, q4, scale, mask);
     return;
   }
   const int T = a.T, TT = a.tile_tets, stride = gridDim.x * blockDim.x;
   int t = int(sweep_first());
   bool act = tet_in_sweep(a, mask, t);
-  int4 ids = act ? tile_node_ids(a, t) : make_int4(0, 0, 0, 0);
+  int4 ids = act ? tile_node_ids<Stream>(a, t) : make_int4(0, 0, 0, 0);
   for (; t < T; t += stride) {
     const int4 cur = ids;
     const bool cur_act = act;
     act = tet_in_sweep(a, mask, t + stride);
-    ids = act ? tile_node_ids(a, t + stride) : make_int4(0, 0, 0, 0);
+    ids = act ? tile_node_ids<Stream>(a, t + stride) : make_int4(0, 0, 0, 0);
     if (!cur_act) continue;
     const int tile = tile_of(t, a.tile_magic);
-    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT, cur);
+    const StagedTetT<Stream> e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT, cur);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
   }
+}
+// AllowStream: the caller may meet tiles beyond L2 (batches, standalone
+// sweeps); the single-mesh solver keeps one, non-streaming, copy of the sweep.
+template <bool AllowStream>
+__device__ void apply_tets_tiled(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                                 const unsigned char* mask) {
+  if (AllowStream && a.stream_tiles) apply_tets_tiled_impl<true>(a, u4, ulo, q4, scale, mask);
+  else apply_tets_tiled_impl<false>(a, u4, ulo, q4, scale, mask);
 }
 
 // Search direction j of the projected start: basis vector j of the
@@ -1432,17 +1467,26 @@ __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
     const int4 cur = ids;
     ids = tile_node_ids(a, t + stride);
     const int tile = tile_of(t, a.tile_magic);
-    const StagedTet e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT, cur);
-    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, a.v_f, a.v_lo, a.q_f);
-    for (int j = 0; j < a.nwarm; ++j)
-      tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
+    const float* w = a.tile_f + size_t(tile) * kTileWords * TT + (t - tile * TT);
+    const float4 quat = make_float4(w[4 * TT], w[5 * TT], w[6 * TT], w[7 * TT]);
+    float b[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT];
+    const float c0 = w[17 * TT], c1 = w[18 * TT], c2 = w[19 * TT];
+    const int nn[4] = {cur.x, cur.y, cur.z, cur.w};
+    for (int j = -1; j < a.nwarm; ++j) {
+      float Re[9];
+      quaternion_to_rotation(quat, Re);
+      if (j < 0) tet_apply(Re, b, c0, c1, c2, scale, nn, a.v_f, a.v_lo, a.q_f);
+      else tet_apply(Re, b, c0, c1, c2, scale, nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
+    }
   }
 }
 
 // One element-apply sweep with the mesh's variant.  `mask` (batched solves
 // only, variants kApplyTets and kApplyStaged) selects the meshes whose tets
 // take part.
-template <typename R>
+template <typename R, bool AllowStream = true>
 __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename ApplyOps<R>::V4* u4,
                                             const typename ApplyOps<R>::V4* ulo, typename ApplyOps<R>::V4* q4,
                                             const R* re, const R* bb, const R* cc, R scale, unsigned char* smem,
@@ -1453,7 +1497,7 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
       return;
     }
     if (a.apply_variant == kApplyTets || mask) {
-      apply_tets_tiled(a, u4, ulo, q4, scale, mask);
+      apply_tets_tiled<AllowStream>(a, u4, ulo, q4, scale, mask);
       return;
     }
   }
@@ -1466,6 +1510,7 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
 // Projected start: A v (into q) and A W_j for every search direction
 // (products into a.wprod).  Tets and staged variants do all operands in one
 // pass; the patch variants sweep once per operand.
+template <bool AllowStream>
 __device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round) {
   if (a.apply_variant == kApplyStaged) {
     apply_staged_dirs(a, scale, smem);
@@ -1475,10 +1520,10 @@ __device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned c
     apply_tets_dirs(a, scale);
     return true;
   }
-  apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+  apply_sweep<float, AllowStream>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   for (int j = 0; j < a.nwarm; ++j) {
     if (!grid_barrier(a.sync, a.spin_limit, round)) return false;
-    apply_sweep<float>(a, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N, a.re_f, a.b_f, a.c_f, scale, smem);
+    apply_sweep<float, AllowStream>(a, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N, a.re_f, a.b_f, a.c_f, scale, smem);
   }
   return true;
 }
@@ -1920,10 +1965,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   // r - sum_j g_j A W_j.
   int applies = 1;
   if (a.nwarm) {
-    if (!apply_start_operands(a, scale, smem, round)) return;
+    if (!apply_start_operands<false>(a, scale, smem, round)) return;
     applies += a.nwarm;
   } else {
-    apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+    apply_sweep<float, false>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
   }
   if (!grid_barrier(a.sync, a.spin_limit, round)) return;
   if (tracer) phase_stamp(a, 1, t_start);
@@ -2012,29 +2057,66 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
   bool restart = false;
   int stalls = 0;
 
+  // With at most one node per thread (N <= threads), the thread's node values
+  // that the sweep does not change (p, r, the diagonal, v) are loaded before
+  // the barrier after the sweep and stay in registers until the update.
+  const bool one_node = long(N) <= gstride;
+  auto node_dots = [&](const float4& q4, const float4& p4, const float4& r4, float d, DF (&s7)[7]) {
+    const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+    const float rq = r4.x * qx + r4.y * qy + r4.z * qz, qq = qx * qx + qy * qy + qz * qz;
+    const float rr2 = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, sp = r4.w;
+    s7[0] = df_add(s7[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
+    s7[1] = df_add(s7[1], DF{sp * rq, 0.f});
+    s7[2] = df_add(s7[2], DF{sp * qq, 0.f});
+    s7[3] = df_add(s7[3], DF{sp * rr2, 0.f});
+    s7[4] = df_add(s7[4], DF{rq, 0.f});
+    s7[5] = df_add(s7[5], DF{qq, 0.f});
+    s7[6] = df_add(s7[6], DF{rr2, 0.f});
+  };
+  auto node_update = [&](long i, const float4& q4, const float4& p4, const float4& r4, float d, float4 vh, float4 vl,
+                         float alpha, float beta) {
+    const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
+    df_inc(vh.x, vl.x, alpha * p4.x);
+    df_inc(vh.y, vl.y, alpha * p4.y);
+    df_inc(vh.z, vl.z, alpha * p4.z);
+    const float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
+    const float sp = r4.w;
+    a.v_f[i] = vh;
+    a.v_lo[i] = vl;
+    a.r_f[i] = make_float4(rx, ry, rz, sp);
+    a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
+    a.q_f[i] = zero4;
+  };
+
   while (!converged && it < a.max_it) {
     // q += dt^2 K' p
-    apply_sweep<float>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+    apply_sweep<float, false>(a, a.p_f, nullptr, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
     ++applies;
     if (tracer) stamp[0] = double(cycles_now() - t_start);
+    const bool mine = one_node && n0 < N && !a.fixed[n0];
+    float4 np4 = zero4, nr4 = zero4, nq4 = zero4, nvh = zero4, nvl = zero4;
+    float nd = 0.f;
+    if (mine) {
+      np4 = a.p_f[n0];
+      nr4 = a.r_f[n0];
+      nd = a.diag_f[n0];
+      nvh = a.v_f[n0];
+      nvl = a.v_lo[n0];
+    }
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
     // q = diag p + q; the totals of FinPcgF (r.w = the node's scalar s)
     DF s7[7] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (long i = n0; i < N; i += gstride) {
-      if (a.fixed[i]) continue;
-      float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
-      const float d = a.diag_f[i];
-      float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
-      const float rq = r4.x * qx + r4.y * qy + r4.z * qz, qq = qx * qx + qy * qy + qz * qz;
-      const float rr2 = r4.x * r4.x + r4.y * r4.y + r4.z * r4.z, sp = r4.w;
-      s7[0] = df_add(s7[0], DF{p4.x * qx + p4.y * qy + p4.z * qz, 0.f});
-      s7[1] = df_add(s7[1], DF{sp * rq, 0.f});
-      s7[2] = df_add(s7[2], DF{sp * qq, 0.f});
-      s7[3] = df_add(s7[3], DF{sp * rr2, 0.f});
-      s7[4] = df_add(s7[4], DF{rq, 0.f});
-      s7[5] = df_add(s7[5], DF{qq, 0.f});
-      s7[6] = df_add(s7[6], DF{rr2, 0.f});
+    if (one_node) {
+      if (mine) {
+        nq4 = load_acc(a.q_f + n0);
+        node_dots(nq4, np4, nr4, nd, s7);
+      }
+    } else {
+      for (long i = n0; i < N; i += gstride) {
+        if (a.fixed[i]) continue;
+        node_dots(load_acc(a.q_f + i), a.p_f[i], a.r_f[i], a.diag_f[i], s7);
+      }
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
     float sc[5];
@@ -2053,36 +2135,28 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_mixed(MixedArgs a) {
     const float alpha = sc[0], beta = sc[1];
     const int row = it;
     ++it;
-    for (long i = n0; i < N; i += gstride) {
-      if (a.fixed[i]) continue;
-      float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
-      float4 vh = a.v_f[i], vl = a.v_lo[i];
-      const float d = a.diag_f[i];
-      float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
-      df_inc(vh.x, vl.x, alpha * p4.x);
-      df_inc(vh.y, vl.y, alpha * p4.y);
-      df_inc(vh.z, vl.z, alpha * p4.z);
-      float rx = r4.x - alpha * qx, ry = r4.y - alpha * qy, rz = r4.z - alpha * qz;
-      const float sp = r4.w;
-      a.v_f[i] = vh;
-      a.v_lo[i] = vl;
-      a.r_f[i] = make_float4(rx, ry, rz, sp);
-      a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
-      a.q_f[i] = zero4;
+    if (one_node) {
+      if (mine) node_update(n0, nq4, np4, nr4, nd, nvh, nvl, alpha, beta);
+    } else {
+      for (long i = n0; i < N; i += gstride) {
+        if (a.fixed[i]) continue;
+        node_update(i, load_acc(a.q_f + i), a.p_f[i], a.r_f[i], a.diag_f[i], a.v_f[i], a.v_lo[i], alpha, beta);
+      }
     }
     if (tracer) stamp[4] = double(cycles_now() - t_start);
     // The exact r.r of the new r comes with the next reduction; here the
     // update needs only a barrier (p must be complete before the next
     // apply).  The estimate of the new r.r triggers the residual recompute,
     // which alone declares convergence.
+    const bool periodic = a.refresh > 0 && it % a.refresh == 0;
+    const bool refresh_now = periodic || sc[2] <= thresh;
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) trace_row(a, row, rho, 0.0, sc[0], sc[1], stamp, t_start);
     rho = sc[2];
-    const bool periodic = a.refresh > 0 && it % a.refresh == 0;
-    if (periodic || sc[2] <= thresh) {
+    if (refresh_now) {
       // r = b - A v (residual replacement, FP64); q is zero here and the
       // (hi, lo) velocity is the apply operand.
-      apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
+      apply_sweep<float, false>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
       ++applies;
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       DF tr[1] = {{0.f, 0.f}};
@@ -2625,7 +2699,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
   // initial residual r = b - A v (FP64), p = S r, for every mesh; with the
   // projected or learned start also A W_j and each mesh's start (k_cg_mixed)
   if (a.nwarm) {
-    if (!apply_start_operands(a, scale, smem, round)) return;
+    if (!apply_start_operands<true>(a, scale, smem, round)) return;
     sweeps += 1 + a.nwarm;
   } else {
     apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
@@ -3241,6 +3315,7 @@ void set_patch_args(MixedArgs& a, const Context& c) {
   a.patch_inc_ptr = c.patch_inc_ptr;
   a.patch_inc = c.patch_inc;
   a.apply_variant = c.apply_variant;
+  a.stream_tiles = c.stream_tiles ? 1 : 0;
 }
 
 template <typename R>
@@ -3467,6 +3542,10 @@ cudaError_t set_tile_layout(Context& c, int tile_tets) {
   c.tile_tets = tile_tets;
   c.tile_magic = tile_magic_of(tile_tets);
   c.num_tiles = int(tiles);
+  // tiles that do not fit in L2 stream from HBM in every sweep
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) == cudaSuccess)
+    c.stream_tiles = tiles * kTileWords * size_t(tile_tets) * sizeof(float) > size_t(l2);
   if (c.T == 0) return cudaSuccess;
   const int nb = (c.T + 255) / 256;
   // padding tets of the last tile: node 0, no stiffness (never computed)
