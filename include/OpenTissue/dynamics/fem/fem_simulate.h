@@ -44,15 +44,12 @@ inline StepStats simulate(fem_mesh& mesh, real_type const& time_step, bool use_s
   otfem_handle h = g.handle();
   int64_t const n3 = int64_t(3 * N);
   gpu::check(otfem_set_fixed(h, fx, int64_t(N)), "fem::simulate");
-  gpu::check(otfem_set_nodes(h, OTFEM_COORD, x, n3), "fem::simulate");
   gpu::check(otfem_set_nodes(h, OTFEM_MODEL_COORD, x0, n3), "fem::simulate");
-  gpu::check(otfem_set_nodes(h, OTFEM_VELOCITY, v, n3), "fem::simulate");
-  gpu::check(otfem_set_nodes(h, OTFEM_F_EXTERNAL, f, n3), "fem::simulate");
-  gpu::check(otfem_simulate_ex(h, double(time_step), use_stiffness_warping ? 1 : 0, &params, &g.stats()),
+  // positions, velocities and external forces in and out of the page-locked
+  // staging buffers around the step (one graph, copies overlapped)
+  gpu::check(otfem_simulate_host(h, double(time_step), use_stiffness_warping ? 1 : 0, &params, &g.stats(), x, v, f),
              "fem::simulate");
-  // queued back to back; the last, blocking download waits for all three
-  gpu::check(otfem_get_nodes_async(h, OTFEM_COORD, x, n3), "fem::simulate");
-  gpu::check(otfem_get_nodes_async(h, OTFEM_VELOCITY, v, n3), "fem::simulate");
+  // the external forces as the step left them (plasticity adds to them)
   gpu::check(otfem_get_nodes(h, OTFEM_F_EXTERNAL, f, n3), "fem::simulate");
   for (std::size_t i = 0; i < N; ++i) {
     typename fem_mesh::node_type& n = mesh.node_at(i);

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 6
+#define OTFEM_ABI_VERSION 7
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -187,6 +187,26 @@ OTFEM_API int otfem_simulate(otfem_handle h, double time_step, int use_stiffness
  * filled after a stream synchronisation. */
 OTFEM_API int otfem_simulate_ex(otfem_handle h, double time_step, int use_stiffness_warping,
                       const otfem_solver_params* params, otfem_step_stats* stats);
+/* fem::simulate on host arrays (fem_simulate.h:49-113 with the node fields
+ * read from and written back to the reference's nodes, which the drop-in
+ * headers do around each step): the same result as
+ *   otfem_set_nodes(COORD, coord), otfem_set_nodes(VELOCITY, velocity),
+ *   otfem_set_nodes(F_EXTERNAL, f_external), otfem_simulate_ex,
+ *   otfem_get_nodes(COORD, coord), otfem_get_nodes(VELOCITY, velocity)
+ * (3 * node count doubles each; returns once coord and velocity hold the new
+ * state, with stats (optional) filled).  The positions are copied first; the
+ * velocity and the external forces are copied on a second stream while the
+ * orientation phase runs (it reads only the positions), and the two
+ * downloads run at once.  With page-locked host arrays the whole step,
+ * copies included, is one CUDA graph, kept per set of array addresses: keep
+ * the same arrays from step to step.  With plasticity or the learned start
+ * (whose orientation phase reads the velocity and forces) and with the
+ * reference solver the inputs are copied before the step.  No counterpart in
+ * the reference's interface: the reference's step works in the host arrays
+ * themselves. */
+OTFEM_API int otfem_simulate_host(otfem_handle h, double time_step, int use_stiffness_warping,
+                                  const otfem_solver_params* params, otfem_step_stats* stats, double* coord,
+                                  double* velocity, const double* f_external);
 /* The two kernels of a matrix-free step enqueued separately (same result as
  * otfem_simulate_ex when ORIENT is followed by SOLVE), so a caller can time
  * them or insert work between them.  ORIENT: orientation, element forces and

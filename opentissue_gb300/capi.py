@@ -112,6 +112,8 @@ SIGNATURES = {
                                          ctypes.POINTER(StepStats)]),
     "otfem_simulate_phase": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverParams),
                                             ctypes.c_int]),
+    "otfem_simulate_host": (ctypes.c_int, [_h, ctypes.c_double, ctypes.c_int, ctypes.POINTER(SolverParams),
+                                           ctypes.POINTER(StepStats), _dp, _dp, _dp]),
     "otfem_last_stats": (ctypes.c_int, [_h, ctypes.POINTER(StepStats)]),
     "otfem_synchronize": (ctypes.c_int, [_h]),
     "otfem_update_original_coord": (ctypes.c_int, [_h]),

@@ -72,6 +72,10 @@ void free_all(Context& c) {
     if (p) cudaFree(p);
   if (c.graph) cudaGraphExecDestroy(c.graph);
   if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+  if (c.host_graph) cudaGraphExecDestroy(c.host_graph);
+  if (c.io_stream) cudaStreamDestroy(c.io_stream);
+  if (c.io_fork) cudaEventDestroy(c.io_fork);
+  if (c.io_join) cudaEventDestroy(c.io_join);
 }
 
 double* node_field(Context& c, int field) {
@@ -150,6 +154,17 @@ cudaError_t launch_warm_start(Context& c, const otfem_solver_params& p) {
 }
 
 // Enqueues one step on c.stream (no host synchronisation).
+// The matrix-free step's orientation phase (orientation, element forces,
+// plasticity, the learned start's inputs) and its solve (K2), which
+// enqueue_step runs back to back.
+cudaError_t enqueue_orient(Context& c, double dt, bool warp, const otfem_solver_params& p) {
+  cudaError_t e = otfem::launch_mixed_orient(c, dt, warp, p.solver);
+  return e != cudaSuccess ? e : launch_warm_start(c, p);
+}
+cudaError_t enqueue_solve(Context& c, double dt, const otfem_solver_params& p) {
+  return c.num_meshes > 1 ? otfem::launch_batch_solve(c, dt, p) : otfem::launch_mixed_solve(c, dt, p);
+}
+
 cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_params& p) {
   cudaError_t e;
   if (p.solver == OTFEM_SOLVER_REFERENCE) {
@@ -163,13 +178,68 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
       return e;
     if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
   } else {
-    if ((e = otfem::launch_mixed_orient(c, dt, warp, p.solver)) != cudaSuccess) return e;
-    if ((e = launch_warm_start(c, p)) != cudaSuccess) return e;
-    if (c.num_meshes > 1) e = otfem::launch_batch_solve(c, dt, p);
-    else e = otfem::launch_mixed_solve(c, dt, p);
-    if (e != cudaSuccess) return e;
+    if ((e = enqueue_orient(c, dt, warp, p)) != cudaSuccess) return e;
+    if ((e = enqueue_solve(c, dt, p)) != cudaSuccess) return e;
   }
   return cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream);
+}
+
+struct HostArrays {
+  double* coord;
+  double* velocity;
+  const double* f_external;
+};
+
+// Page-locked (or registered) host memory: its copies are asynchronous and
+// can be captured into a graph.
+bool page_locked(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+// One step on host arrays: the positions are copied in first (the
+// orientation phase reads only them), the velocity and the external forces
+// on the second stream while the orientation phase runs, and the solve waits
+// for them; the new positions and velocities go back on the two streams at
+// once.  Where plasticity or the learned start's inputs read the velocity or
+// the forces in the orientation phase, and for the reference solver, they are
+// copied before it.
+cudaError_t enqueue_host_step(Context& c, double dt, bool warp, const otfem_solver_params& p, const HostArrays& io) {
+  const size_t bytes = sizeof(double) * 3 * size_t(c.N);
+  if (!bytes) return enqueue_step(c, dt, warp, p);
+  const bool late_inputs = p.solver != OTFEM_SOLVER_REFERENCE && !c.plastic_active &&
+                           p.warm_start != OTFEM_WARM_START_LEARNED && !c.collect;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(c.x, io.coord, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
+  if (late_inputs) {
+    if ((e = cudaEventRecord(c.io_fork, c.stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(c.io_stream, c.io_fork, 0)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c.v, io.velocity, bytes, cudaMemcpyHostToDevice, c.io_stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c.fext, io.f_external, bytes, cudaMemcpyHostToDevice, c.io_stream)) != cudaSuccess)
+      return e;
+    if ((e = cudaEventRecord(c.io_join, c.io_stream)) != cudaSuccess) return e;
+    if ((e = enqueue_orient(c, dt, warp, p)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(c.stream, c.io_join, 0)) != cudaSuccess) return e;
+    if ((e = enqueue_solve(c, dt, p)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream)) !=
+        cudaSuccess)
+      return e;
+  } else {
+    if ((e = cudaMemcpyAsync(c.v, io.velocity, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c.fext, io.f_external, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
+      return e;
+    if ((e = enqueue_step(c, dt, warp, p)) != cudaSuccess) return e;
+  }
+  if ((e = cudaEventRecord(c.io_fork, c.stream)) != cudaSuccess) return e;
+  if ((e = cudaStreamWaitEvent(c.io_stream, c.io_fork, 0)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(io.velocity, c.v, bytes, cudaMemcpyDeviceToHost, c.io_stream)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(io.coord, c.x, bytes, cudaMemcpyDeviceToHost, c.stream)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(c.io_join, c.io_stream)) != cudaSuccess) return e;
+  return cudaStreamWaitEvent(c.stream, c.io_join, 0);
 }
 
 std::string step_key(const Context& c, double dt, bool warp, const otfem_solver_params& p) {
@@ -418,11 +488,7 @@ static int init_impl(Context& c, double young, double poisson, double density, d
   OT_CUDA(cudaStreamSynchronize(c.stream));
   c.plastic_active = c_creep > 0.0 && c_max > 0.0;
   c.initialized = true;
-  if (c.graph) {
-    cudaGraphExecDestroy(c.graph);
-    c.graph = nullptr;
-    c.graph_key.clear();
-  }
+  drop_step_graphs(c);
   // fem_initialize_stiffness_elements.h:48
   for (int t = 0; t < c.T; ++t)
     if (!(vol[t] > 0.0))
@@ -647,6 +713,62 @@ int otfem_simulate_ex(otfem_handle h, double dt, int warp, const otfem_solver_pa
 }
 
 int otfem_simulate(otfem_handle h, double dt, int warp) { return otfem_simulate_ex(h, dt, warp, nullptr, nullptr); }
+
+int otfem_simulate_host(otfem_handle h, double dt, int warp, const otfem_solver_params* params,
+                        otfem_step_stats* stats, double* coord, double* velocity, const double* f_external) {
+  if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
+  Context& c = h->c;
+  if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
+  if (!(dt > 0.0)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "time step must be positive");
+  const int64_t n3 = 3 * int64_t(c.N);
+  if (n3 && (!coord || !velocity || !f_external)) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null argument");
+  otfem_solver_params p;
+  if (params) p = *params;
+  else otfem_default_params(&p);
+  int rc = check_params(c, p);
+  if (rc != OTFEM_OK) return rc;
+  cudaError_t e0 = ensure_history(c, p);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "warm-start history");
+  if (!c.io_stream) {
+    OT_CUDA(cudaStreamCreateWithFlags(&c.io_stream, cudaStreamNonBlocking));
+    OT_CUDA(cudaEventCreateWithFlags(&c.io_fork, cudaEventDisableTiming));
+    OT_CUDA(cudaEventCreateWithFlags(&c.io_join, cudaEventDisableTiming));
+  }
+  const HostArrays io{coord, velocity, f_external};
+  const bool use_warp = warp != 0;
+  cudaError_t e;
+  // one graph for page-locked arrays (pageable copies cannot be captured)
+  if (p.graph && n3 && page_locked(coord) && page_locked(velocity) && page_locked(f_external)) {
+    char ptrs[80];
+    snprintf(ptrs, sizeof(ptrs), "|%p|%p|%p", static_cast<void*>(coord), static_cast<void*>(velocity),
+             static_cast<const void*>(f_external));
+    const std::string key = step_key(c, dt, use_warp, p) + ptrs;
+    if (!c.host_graph || key != c.host_graph_key) {
+      if (c.host_graph) {
+        cudaGraphExecDestroy(c.host_graph);
+        c.host_graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      OT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ee = enqueue_host_step(c, dt, use_warp, p, io);
+      cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
+      if (ee != cudaSuccess) return cuda_fail(ee, "capture step");
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+      e = cudaGraphInstantiate(&c.host_graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+      c.host_graph_key = key;
+    }
+    OT_CUDA(cudaGraphLaunch(c.host_graph, c.stream));
+  } else if ((e = enqueue_host_step(c, dt, use_warp, p, io)) != cudaSuccess) {
+    return cuda_fail(e, "enqueue step");
+  }
+  if (p.solver == OTFEM_SOLVER_REFERENCE) c.k_assembled = true;
+  c.last_solver = p.solver;
+  c.launches += kernels_per_step(c, p);
+  otfem_step_stats local;
+  return otfem_last_stats(h, stats ? stats : &local);
+}
 
 int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver_params* params, int phase) {
   if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
@@ -967,11 +1089,7 @@ int otfem_set_apply_variant(otfem_handle h, int32_t variant) {
   if (c.num_meshes > 1 && variant < 2)
     return fail(OTFEM_ERR_UNSUPPORTED, "a batch of meshes uses apply variant 2 or 3");
   c.apply_variant = variant;
-  if (c.graph) {
-    cudaGraphExecDestroy(c.graph);
-    c.graph = nullptr;
-    c.graph_key.clear();
-  }
+  drop_step_graphs(c);
   return OTFEM_OK;
 }
 

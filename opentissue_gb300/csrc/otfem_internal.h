@@ -87,6 +87,13 @@ struct Context {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;            // stream created by otfem_create
+  // otfem_simulate_host: a second stream for the copies that overlap the
+  // orientation phase and each other, the events that fork and join it, and
+  // the step graph of page-locked host arrays (created by the first call)
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t io_fork = nullptr, io_join = nullptr;
+  cudaGraphExec_t host_graph = nullptr;
+  std::string host_graph_key;
   int N = 0, T = 0;
   bool initialized = false;
   bool k_assembled = false;
@@ -217,6 +224,16 @@ struct Context {
   std::string graph_key;
   int last_status = 0;
 };
+
+// Drops the cached step graphs (the kernels' arguments changed).
+inline void drop_step_graphs(Context& c) {
+  if (c.graph) cudaGraphExecDestroy(c.graph);
+  if (c.host_graph) cudaGraphExecDestroy(c.host_graph);
+  c.graph = nullptr;
+  c.host_graph = nullptr;
+  c.graph_key.clear();
+  c.host_graph_key.clear();
+}
 
 // ---- pattern / incidence (otfem_pattern.cu) ------------------------------
 cudaError_t build_incidence(Context& c);

@@ -1199,11 +1199,7 @@ int otfem_set_warm_start_smoothing(otfem_handle h, int32_t passes) {
     if (e != cudaSuccess) return mlp_cuda(e, "cudaMalloc");
   }
   c->warm_smoothing = passes;
-  if (c->graph) {
-    cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
-    c->graph_key.clear();
-  }
+  drop_step_graphs(*c);
   return OTFEM_OK;
 }
 
