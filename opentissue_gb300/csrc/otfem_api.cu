@@ -66,7 +66,7 @@ void free_all(Context& c) {
     if (p) cudaFree(p);
   if (c.stats_host) cudaFreeHost(c.stats_host);
   if (c.bmesh_host) cudaFreeHost(c.bmesh_host);
-  void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.mesh_tet_start, c.bmesh, c.bacc, c.bmask,
+  void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.mesh_tet_start, c.mesh_node_start, c.bmesh, c.bacc, c.bmask,
                    c.warm_hist, c.warm_prod, c.warm_part, c.warm_bacc};
   for (void* p : batch)
     if (p) cudaFree(p);
@@ -551,6 +551,9 @@ int otfem_batch_create(const otfem_mesh_desc* meshes, int32_t count, void* strea
   if (e == cudaSuccess) e = cudaMalloc(&c.mesh_tet_start, sizeof(int) * toff.size());
   if (e == cudaSuccess)
     e = cudaMemcpy(c.mesh_tet_start, toff.data(), sizeof(int) * toff.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&c.mesh_node_start, sizeof(int) * noff.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c.mesh_node_start, noff.data(), sizeof(int) * noff.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&c.bmesh, sizeof(otfem::BatchMesh) * size_t(count));
   if (e == cudaSuccess) e = cudaMallocHost(&c.bmesh_host, sizeof(otfem::BatchMesh) * size_t(count));
   if (e == cudaSuccess) e = cudaMalloc(&c.bacc, sizeof(double) * 16 * size_t(count));

@@ -196,6 +196,7 @@ struct Context {
   int* mesh_of_node = nullptr;                    // N
   int* mesh_of_tet = nullptr;                     // T
   int* mesh_tet_start = nullptr;                  // num_meshes + 1: mesh_tet_off on the device
+  int* mesh_node_start = nullptr;                 // num_meshes + 1: mesh_node_off on the device
   BatchMesh* bmesh = nullptr;                     // num_meshes
   BatchMesh* bmesh_host = nullptr;                // num_meshes, pinned
   double* bacc = nullptr;                         // 2 x num_meshes x 8 accumulators

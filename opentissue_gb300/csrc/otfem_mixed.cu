@@ -149,6 +149,7 @@ struct MixedArgs {
   const int* mesh_of_node;
   const int* mesh_of_tet;
   const int* mesh_tet_start;            // num_meshes + 1: the first tet of each mesh (batches)
+  const int* mesh_node_start;           // num_meshes + 1: the first node of each mesh (batches)
   BatchMesh* bm;
   double* bacc;
   unsigned char* bmask;
@@ -1347,25 +1348,39 @@ __device__ void apply_staged(const MixedArgs& a, const float4* u4, const float4*
 __device__ __forceinline__ bool tet_in_sweep(const MixedArgs& a, const unsigned char* mask, int t) {
   return t < a.T && (!mask || mask[a.mesh_of_tet[t]]);
 }
-// A batch's masked sweep over the meshes in the sweep only (at most kBlock
-// meshes): every CTA lists them with a CTA-wide scan of the mask (meshes
-// without tets left out) and walks their tets as one virtual range, mesh j's
-// tets at [s_pref[j], s_pref[j + 1]), so that a sweep late in a step, when a
-// few meshes still iterate, costs in proportion to their tets instead of
-// reading the mesh id of every tet of the batch.
-template <bool Stream>
-__device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
-                                    const unsigned char* mask) {
-  __shared__ int s_beg[kBlock], s_pref[kBlock + 1], s_wsum[kBlock / 32];
+// The meshes of a batch selected by a mask (at most kBlock meshes), as one
+// virtual range of their tets or nodes: every CTA lists them with a CTA-wide
+// scan of the mask (meshes without elements left out), list entry j holding
+// mesh mesh[j] whose elements starts[m] ... lie at [pref[j], pref[j + 1]) of
+// the virtual range.  The lists live in shared memory until the next call.
+struct MeshList {
+  const int* beg;   // first element of entry j's mesh
+  const int* pref;  // n + 1 virtual offsets
+  const int* mesh;  // mesh id of entry j
+  int n, total;
+  // the list entry holding virtual element v < total: the last j with
+  // pref[j] <= v (the counts are positive, so pref increases strictly)
+  __device__ __forceinline__ int entry(int v) const {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (pref[mid] <= v) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  }
+};
+__device__ MeshList masked_meshes(const MixedArgs& a, const int* starts, const unsigned char* mask) {
+  __shared__ int s_beg[kBlock], s_pref[kBlock + 1], s_mesh[kBlock], s_wsum[kBlock / 32], s_wcnt[kBlock / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, m = threadIdx.x;
-  __syncthreads();  // the previous sweep's readers of the lists are done
+  __syncthreads();  // the previous list's readers are done
   int beg = 0, cnt = 0;
   if (m < a.num_meshes && mask[m]) {
-    beg = a.mesh_tet_start[m];
-    cnt = a.mesh_tet_start[m + 1] - beg;
+    beg = starts[m];
+    cnt = starts[m + 1] - beg;
   }
-  // CTA-wide inclusive scans of the flags and of the tet counts (warp
-  // shuffles, then the warp totals by warp 0)
+  // CTA-wide inclusive scans of the flags and of the counts (warp shuffles,
+  // then the warp totals by warp 0)
   int f = cnt > 0 ? 1 : 0, c = f ? cnt : 0;
   int fi = f, ci = c;
 #pragma unroll
@@ -1373,7 +1388,6 @@ __device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const 
     const int yf = __shfl_up_sync(0xffffffffu, fi, o), yc = __shfl_up_sync(0xffffffffu, ci, o);
     if (lane >= o) fi += yf, ci += yc;
   }
-  __shared__ int s_wcnt[kBlock / 32];
   if (lane == 31) s_wsum[warp] = fi, s_wcnt[warp] = ci;
   __syncthreads();
   if (warp == 0) {
@@ -1387,24 +1401,34 @@ __device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const 
   }
   __syncthreads();
   const int f_before = (warp ? s_wsum[warp - 1] : 0) + fi - f, c_before = (warp ? s_wcnt[warp - 1] : 0) + ci - c;
-  const int n = s_wsum[kBlock / 32 - 1], total = s_wcnt[kBlock / 32 - 1];
+  MeshList L;
+  L.n = s_wsum[kBlock / 32 - 1];
+  L.total = s_wcnt[kBlock / 32 - 1];
   if (f) {
     s_beg[f_before] = beg;
     s_pref[f_before] = c_before;
+    s_mesh[f_before] = m;
   }
-  if (threadIdx.x == 0) s_pref[n] = total;
+  if (threadIdx.x == 0) s_pref[L.n] = L.total;
   __syncthreads();
+  L.beg = s_beg;
+  L.pref = s_pref;
+  L.mesh = s_mesh;
+  return L;
+}
+
+// A batch's masked sweep over the meshes in the sweep only: their tets as
+// one virtual range, so that a sweep late in a step, when a few meshes still
+// iterate, costs in proportion to their tets instead of reading the mesh id
+// of every tet of the batch.
+template <bool Stream>
+__device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const float4* ulo, float4* q4, float scale,
+                                    const unsigned char* mask) {
+  const MeshList L = masked_meshes(a, a.mesh_tet_start, mask);
   const int TT = a.tile_tets, stride = gridDim.x * blockDim.x;
-  for (int v = int(sweep_first()); v < total; v += stride) {
-    // the list entry holding v: the last j with s_pref[j] <= v (the counts
-    // are positive, so s_pref increases strictly)
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (s_pref[mid] <= v) lo = mid;
-      else hi = mid - 1;
-    }
-    const int t = s_beg[lo] + (v - s_pref[lo]);
+  for (int v = int(sweep_first()); v < L.total; v += stride) {
+    const int j = L.entry(v);
+    const int t = L.beg[j] + (v - L.pref[j]);
     const int tile = tile_of(t, a.tile_magic);
     const StagedTetT<Stream> e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
     tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
@@ -2419,6 +2443,44 @@ __device__ __forceinline__ NodeRange warp_node_range(int N) {
   return r;
 }
 
+// Walks the nodes of the meshes selected by `mask` in contiguous chunks per
+// warp, 32 lanes at a time, calling fn(valid, i, m) on every lane with the
+// node i and its mesh m (used only where valid); the mesh ids grow along each
+// warp's walk.  With at most kBlock meshes the walk covers the selected
+// meshes' nodes only (masked_meshes), so that a pass late in a step, when a
+// few meshes still iterate, costs in proportion to their nodes; otherwise it
+// reads the mesh of every node of the batch.
+template <typename Fn>
+__device__ __forceinline__ void masked_node_walk(const MixedArgs& a, const unsigned char* mask, Fn fn) {
+  const int lane = threadIdx.x & 31;
+  if (a.num_meshes <= kBlock && blockDim.x == kBlock) {
+    const MeshList L = masked_meshes(a, a.mesh_node_start, mask);
+    const NodeRange vr = warp_node_range(L.total);
+    // the lane's list entry: searched once, then advanced as the walk
+    // passes mesh boundaries
+    int j = vr.beg + lane < vr.end ? L.entry(int(vr.beg + lane)) : 0;
+    for (long base = vr.beg; base < vr.end; base += 32) {
+      const long v = base + lane;
+      const bool valid = v < vr.end;
+      long i = 0;
+      int m = -1;
+      if (valid) {
+        while (j + 1 < L.n && L.pref[j + 1] <= v) ++j;
+        m = L.mesh[j];
+        i = L.beg[j] + (v - L.pref[j]);
+      }
+      fn(valid, i, m);
+    }
+  } else {
+    const NodeRange nr = warp_node_range(a.N);
+    for (long base = nr.beg; base < nr.end; base += 32) {
+      const long i = base + lane;
+      const int m = i < nr.end ? a.mesh_of_node[i] : -1;
+      fn(i < nr.end && mask[m], i, m);
+    }
+  }
+}
+
 // Running per-mesh sums of a warp (mesh ids are non-decreasing along nodes).
 template <int NV, int Stride = kBatchSlots>
 struct SegSum {
@@ -2809,18 +2871,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     if (tracer) stamp[0] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     if (tracer) stamp[1] = double(cycles_now() - t_start);
-    // q = diag p + q; the totals of FinPcgF per mesh
+    // q = diag p + q; the totals of FinPcgF per mesh, over the meshes in the sweep
     {
       SegSum<7> ss;
-      ss.start(first_mesh);
-      for (long base = nr.beg; base < nr.end; base += 32) {
-        const long i = base + lane;
-        const bool valid = i < nr.end;
-        int m = -1;
+      ss.start(-1);
+      masked_node_walk(a, mask_apply, [&](bool valid, long i, int m) {
         float s7[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (valid) {
-          m = a.mesh_of_node[i];
-          if (mask_apply[m] && !a.fixed[i]) {
+          if (!a.fixed[i]) {
             const float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
             const float d = a.diag_f[i];
             const float qx = d * p4.x + q4.x, qy = d * p4.y + q4.y, qz = d * p4.z + q4.z;
@@ -2834,7 +2892,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           }
         }
         ss.add(valid, m, s7, acc_half(round + 1));
-      }
+      });
       ss.flush(acc_half(round + 1));
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
@@ -2843,9 +2901,8 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
     n_active = counts[0];
     const bool any_refresh = counts[1] > 0;
     // v += alpha p, r -= alpha q, p = r + beta p with each mesh's scalars
-    for (long i = nr.beg + lane; i < nr.end; i += 32) {
-      const int m = a.mesh_of_node[i];
-      if (!mask_update[m] || a.fixed[i]) continue;
+    masked_node_walk(a, mask_update, [&](bool valid, long i, int m) {
+      if (!valid || a.fixed[i]) return;
       const float alpha = a.bm[m].alpha, beta = a.bm[m].beta;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
@@ -2861,7 +2918,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       a.r_f[i] = make_float4(rx, ry, rz, sp);
       a.p_f[i] = make_float4(sp * rx + beta * p4.x, sp * ry + beta * p4.y, sp * rz + beta * p4.z, 1.f);
       a.q_f[i] = zero4;
-    }
+    });
     if (tracer) stamp[4] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
     // trace row: the meshes iterating, whether a refresh sweep follows
@@ -2872,15 +2929,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
       ++sweeps;
       if (!grid_barrier(a.sync, a.spin_limit, round)) return;
       SegSum<1> ss;
-      ss.start(first_mesh);
-      for (long base = nr.beg; base < nr.end; base += 32) {
-        const long i = base + lane;
-        const bool valid = i < nr.end;
-        int m = -1;
+      ss.start(-1);
+      masked_node_walk(a, mask_refresh, [&](bool valid, long i, int m) {
         float tr[1] = {0.f};
         if (valid) {
-          m = a.mesh_of_node[i];
-          if (mask_refresh[m] && !a.fixed[i]) {
+          if (!a.fixed[i]) {
             const float4 q4 = load_acc(a.q_f + i), vh = a.v_f[i], vl = a.v_lo[i];
             float rr3[3];
             node_residual(a, i, vh, vl, q4, rr3);
@@ -2894,7 +2947,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_cg_batch(MixedArgs a) {
           }
         }
         ss.add(valid, m, tr, acc_half(round + 1));
-      }
+      });
       ss.flush(acc_half(round + 1));
       if (!batch_reduce(a, round, FinBatchRefresh(), counts)) return;
       n_active = counts[0];
@@ -3721,6 +3774,7 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.mesh_of_node = c.mesh_of_node;
   a.mesh_of_tet = c.mesh_of_tet;
   a.mesh_tet_start = c.mesh_tet_start;
+  a.mesh_node_start = c.mesh_node_start;
   a.bm = c.bmesh;
   a.bacc = c.bacc;
   a.bmask = c.bmask;
