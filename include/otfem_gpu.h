@@ -420,8 +420,8 @@ OTFEM_API int otfem_set_apply_variant(otfem_handle h, int32_t variant);
 /* The autotuner's search at otfem_init (no counterpart in the reference):
  * the patch variants 0 and 1 once (single meshes; tile_tets reported as 0),
  * the tiled variants 2 and 3 at every candidate tile size (the size that
- * splits the tets evenly over the persistent grid, then 128, 256 and 512
- * tets per tile), each timed as the best of 3 x 4 sweeps; the fastest
+ * splits the tets evenly over the persistent grid, then 128, 256, 512 and
+ * 1024 tets per tile), each timed as the best of 3 x 4 sweeps; the fastest
  * combination is kept.  rows: the number of measured combinations (at most
  * 16); the first max_rows are written to variant, tile_tets and ms (each may
  * be NULL); chosen_tile_tets (may be NULL): the tile size in use. */

@@ -394,7 +394,7 @@ int otfem_create(const otfem_mesh_desc* d, void* stream, otfem_handle* out) {
   otfem::mixed_grid_shape(c, &c.mf_grid, &c.mf_block);
   otfem::staged_tiles(c);
   {
-    int cand[4];
+    int cand[5];
     otfem::tile_candidates(c, cand, &c.tile_capacity);
   }
   OT_ALLOC(c.tile_f, c.tile_capacity);
@@ -1071,7 +1071,7 @@ int otfem_set_apply_shape(otfem_handle h, int32_t variant, int32_t tile_tets) {
   if (!h) return fail(OTFEM_ERR_INVALID_ARGUMENT, "null handle");
   Context& c = h->c;
   if (!c.initialized) return fail(OTFEM_ERR_NOT_INITIALIZED, "otfem_init has not been called");
-  int cand[4];
+  int cand[5];
   size_t floats = 0;
   const int nc = otfem::tile_candidates(c, cand, &floats);
   bool ok = tile_tets == 0;

@@ -201,7 +201,8 @@ struct Context {
   BatchMesh* bmesh_host = nullptr;                // num_meshes, pinned
   double* bacc = nullptr;                         // 2 x num_meshes x 8 accumulators
   unsigned char* bmask = nullptr;                 // 3 x num_meshes: apply, update, refresh
-  size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes)
+  size_t apply_smem = 0;          // dynamic shared memory of the apply (bytes): the most any variant needs
+  size_t patch_smem[2] = {0, 0};  // that of the patch variants (atomics, gather); see launch_smem
   int apply_variant = 0;          // element-apply variant chosen by the autotuner
   bool stream_tiles = false;      // the tiles exceed L2: tiled sweeps read them past L1 (set_tile_layout)
   double apply_ms[OTFEM_NUM_APPLY_VARIANTS] = {};  // measured time of one sweep per variant (best tile size)
@@ -264,8 +265,8 @@ cudaError_t check_wait_timeout(Context& c, long long cycles, int* status);  // t
 // tets per CTA as a multiple of 16 allows.
 void staged_tiles(Context& c);
 // Candidate tile sizes of the autotuner's search: the balanced size of
-// staged_tiles first, then 128, 256 and 512 tets (each at most once).
-// Returns how many (at most 4) and, in *floats, the tile_f size the largest
+// staged_tiles first, then 128, 256, 512 and 1024 tets (each at most once).
+// Returns how many (at most 5) and, in *floats, the tile_f size the largest
 // layout needs.
 int tile_candidates(const Context& c, int* out, size_t* floats);
 // Lays the tiles out with tile_tets tets each (tile words from the init data,
@@ -289,7 +290,7 @@ constexpr int kFeatureStride = 20;
 // from the attached network.  After the orientation phase.
 cudaError_t launch_node_features(Context& c, bool predict);
 // Staged-apply tiles: at most kTileMaxTets tets of kTileWords 32-bit words.
-constexpr int kTileMaxTets = 512;
+constexpr int kTileMaxTets = 1024;
 constexpr int kTileWords = 20;
 
 // Rotation of a unit quaternion (x, y, z, w), row-major.

@@ -3494,11 +3494,12 @@ cudaError_t build_patches(Context& c, const int32_t* tets) {
   c.num_patches = P;
   c.patch_max_nodes = maxn;
   const int cap = (maxn + 3) / 4 * 4;
-  // the largest staging of all variants: atomics (operand + accumulators) or
-  // gather (operand + 12 forces per tet)
-  c.apply_smem = std::max(size_t(cap) * std::max(SmemOperand<float>::bytes, SmemOperand<double>::bytes),
-                          size_t(cap) * sizeof(double4) + size_t(kPatchTets) * 12 * sizeof(double));
-  c.apply_smem = std::max(c.apply_smem, kStagedSmem);
+  // the patch variants' staging: atomics (operand + accumulators) and gather
+  // (operand + 12 forces per tet); the kernels accept the largest staging of
+  // all variants, and each launch asks for its variant's (launch_smem)
+  c.patch_smem[0] = size_t(cap) * std::max(SmemOperand<float>::bytes, SmemOperand<double>::bytes);
+  c.patch_smem[1] = size_t(cap) * sizeof(double4) + size_t(kPatchTets) * 12 * sizeof(double);
+  c.apply_smem = std::max(std::max(c.patch_smem[0], c.patch_smem[1]), kStagedSmem);
   cudaError_t e;
   if ((e = cudaMalloc(&c.patch_node_ptr, sizeof(int) * ptr.size())) != cudaSuccess) return e;
   if ((e = cudaMalloc(&c.patch_nodes, sizeof(int) * std::max<size_t>(nodes.size(), 1))) != cudaSuccess) return e;
@@ -3542,6 +3543,17 @@ void staged_tiles(Context& c) {
   c.tile_balanced = int(tt);
   c.tile_magic = tile_magic_of(c.tile_tets);
   c.num_tiles = int((T + tt - 1) / tt);
+}
+
+// Dynamic shared memory of a launch with the mesh's apply variant: the
+// tiled-tets variant needs none, so L1 keeps the rest of the SM's 256 KB.
+size_t launch_smem(const Context& c) {
+  switch (c.apply_variant) {
+    case kApplyAtomics: return c.patch_smem[0];
+    case kApplyGather: return c.patch_smem[1];
+    case kApplyStaged: return kStagedSmem;
+    default: return 0;
+  }
 }
 
 int mixed_grid_shape(Context& c, int* grid, int* block) {
@@ -3623,7 +3635,7 @@ cudaError_t launch_mixed_orient(Context& c, double dt, bool warp, int solver) {
 }
 
 int tile_candidates(const Context& c, int* out, size_t* floats) {
-  const int fixed_sizes[3] = {128, 256, 512};
+  const int fixed_sizes[4] = {128, 256, 512, 1024};
   int n = 0;
   out[n++] = c.tile_balanced;  // staged_tiles
   for (int s : fixed_sizes) {
@@ -3704,7 +3716,7 @@ cudaError_t autotune_apply(Context& c) {
   };
   c.tune_rows = 0;
   for (int v = 0; v < kApplyVariants; ++v) c.apply_ms[v] = 0.0;
-  int cand[4];
+  int cand[5];
   const int nc = tile_candidates(c, cand, nullptr);
   const int balanced = cand[0];
   int best_v = -1, best_tt = balanced;
@@ -3856,7 +3868,7 @@ cudaError_t launch_mixed_solve(Context& c, double dt, const otfem_solver_params&
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(c.mf_grid);
   cfg.blockDim = dim3(c.mf_block);
-  cfg.dynamicSmemBytes = c.apply_smem;
+  cfg.dynamicSmemBytes = launch_smem(c);
   cfg.stream = c.stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -3889,7 +3901,7 @@ cudaError_t launch_batch_solve(Context& c, double dt, const otfem_solver_params&
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(c.mf_grid);
   cfg.blockDim = dim3(c.mf_block);
-  cfg.dynamicSmemBytes = c.apply_smem;
+  cfg.dynamicSmemBytes = launch_smem(c);
   cfg.stream = c.stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -3912,9 +3924,9 @@ cudaError_t launch_apply_sweeps(Context& c, int solver, double dt, int sweeps, b
     if (cudaError_t e = reset_tile_tickets(c)) return e;
   for (int k = 0; k < sweeps; ++k) {
     if (solver == OTFEM_SOLVER_FP64)
-      k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_d4, nullptr, c.q_d);
+      k_apply_sweep<double><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, c.p_d4, nullptr, c.q_d);
     else
-      k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.p_f, nullptr, c.q_f);
+      k_apply_sweep<float><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, c.p_f, nullptr, c.q_f);
   }
   return cudaGetLastError();
 }
@@ -3929,11 +3941,11 @@ cudaError_t launch_apply_operator(Context& c, int solver, double dt, double mass
   int nb = (c.N + 255) / 256 > 0 ? (c.N + 255) / 256 : 1;
   if (solver == OTFEM_SOLVER_FP64) {
     k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_d4, nullptr, c.q_d);
-    k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.v_d4, nullptr, c.q_d);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, c.v_d4, nullptr, c.q_d);
     k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_d, y);
   } else {
     k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, c.v_f, c.v_lo, c.q_f);
-    k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, c.v_f, c.v_lo, c.q_f);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, c.v_f, c.v_lo, c.q_f);
     k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, c.q_f, y);
   }
   return cudaGetLastError();
@@ -3951,14 +3963,14 @@ cudaError_t launch_apply_operator_scratch(Context& c, int solver, double dt, dou
     double4* u = static_cast<double4*>(scratch);
     double4* q = u + c.N;
     k_pack_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, u, nullptr, q);
-    k_apply_sweep<double><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, u, nullptr, q);
+    k_apply_sweep<double><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, u, nullptr, q);
     k_finalize_operand<double4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, q, y);
   } else {
     float4* u = static_cast<float4*>(scratch);
     float4* ulo = u + c.N;
     float4* q = ulo + c.N;
     k_pack_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, x, u, ulo, q);
-    k_apply_sweep<float><<<c.mf_grid, kBlock, c.apply_smem, c.stream>>>(a, u, ulo, q);
+    k_apply_sweep<float><<<c.mf_grid, kBlock, launch_smem(c), c.stream>>>(a, u, ulo, q);
     k_finalize_operand<float4><<<nb, 256, 0, c.stream>>>(c.N, c.fixed, c.mass, dt, mass_damping, x, q, y);
   }
   return cudaGetLastError();

@@ -46,7 +46,7 @@ def test_search_covers_the_shapes_and_keeps_the_fastest(gpu, dims):
     # patch variants once, the tiled variants at each candidate tile size
     assert list(v[:2]) == [0, 1] and list(tt[:2]) == [0, 0]
     cands = sorted(set(tt[2:].tolist()))
-    assert {128, 256, 512} <= set(cands) and all(t % 16 == 0 and 16 <= t <= 512 for t in cands)
+    assert {128, 256, 512, 1024} <= set(cands) and all(t % 16 == 0 and 16 <= t <= 1024 for t in cands)
     assert len(v) == 2 + 2 * len(cands) and np.all(ms > 0)
     k = int(np.argmin(ms))
     assert variant == v[k] and (v[k] < 2 or chosen == tt[k]), (v, tt, ms, variant, chosen)
