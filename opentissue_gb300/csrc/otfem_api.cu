@@ -201,11 +201,11 @@ bool page_locked(const void* p) {
   return at.type == cudaMemoryTypeHost;
 }
 
-// One step on host arrays: the positions are copied in first (the
-// orientation phase reads only them), the velocity and the external forces
-// on the second stream while the orientation phase runs, and the solve waits
-// for them; the new positions and velocities go back on the two streams at
-// once.  Where plasticity or the learned start's inputs read the velocity or
+// One step on host arrays: the positions are copied in first, half on each
+// stream (the orientation phase reads only them), the velocity and the
+// external forces on the second stream while the orientation phase runs, and
+// the solve waits for them; the new positions and velocities go back on the
+// two streams at once.  Where plasticity or the learned start's inputs read the velocity or
 // the forces in the orientation phase, and for the reference solver, they are
 // copied before it.
 cudaError_t enqueue_host_step(Context& c, double dt, bool warp, const otfem_solver_params& p, const HostArrays& io) {
@@ -214,10 +214,18 @@ cudaError_t enqueue_host_step(Context& c, double dt, bool warp, const otfem_solv
   const bool late_inputs = p.solver != OTFEM_SOLVER_REFERENCE && !c.plastic_active &&
                            p.warm_start != OTFEM_WARM_START_LEARNED && !c.collect;
   cudaError_t e;
-  if ((e = cudaMemcpyAsync(c.x, io.coord, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
   if (late_inputs) {
+    // the positions in two halves, one per stream (two copy engines), the
+    // orientation phase after both; then the velocity and forces
+    const size_t half = sizeof(double) * 3 * size_t(c.N / 2);
     if ((e = cudaEventRecord(c.io_fork, c.stream)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(c.io_stream, c.io_fork, 0)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(c.x, io.coord, half, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(reinterpret_cast<char*>(c.x) + half, reinterpret_cast<const char*>(io.coord) + half,
+                             bytes - half, cudaMemcpyHostToDevice, c.io_stream)) != cudaSuccess)
+      return e;
+    if ((e = cudaEventRecord(c.io_join, c.io_stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(c.stream, c.io_join, 0)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.v, io.velocity, bytes, cudaMemcpyHostToDevice, c.io_stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.fext, io.f_external, bytes, cudaMemcpyHostToDevice, c.io_stream)) != cudaSuccess)
       return e;
@@ -229,6 +237,7 @@ cudaError_t enqueue_host_step(Context& c, double dt, bool warp, const otfem_solv
         cudaSuccess)
       return e;
   } else {
+    if ((e = cudaMemcpyAsync(c.x, io.coord, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.v, io.velocity, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(c.fext, io.f_external, bytes, cudaMemcpyHostToDevice, c.stream)) != cudaSuccess)
       return e;
