@@ -84,3 +84,64 @@ def test_host_step_rejects_null_arrays(gpu):
     rc = m.lib.otfem_simulate_host(m.h, 0.01, 1, None, None, x.ctypes.data_as(_dp), None, None)
     assert rc == capi.ERR_INVALID_ARGUMENT
     m.close()
+
+
+def _pair_host_steps(seq, host, coord, fixed, params, steps, pinned, load):
+    """Steps `seq` by the copy sequence and `host` by otfem_simulate_host from
+    the same state; returns per step (seq x, seq v, host x, host v)."""
+    x, v, f = _arrays(coord.shape[0], pinned)
+    x[:] = coord
+    v[:] = 0.0
+    out = []
+    for s in range(steps):
+        f[:] = load(s)
+        seq.set(capi.F_EXTERNAL, f)
+        capi.check(seq.lib.otfem_simulate_ex(seq.h, 0.01, 1, ctypes.byref(params), None))
+        st = capi.StepStats()
+        capi.check(host.lib.otfem_simulate_host(host.h, 0.01, 1, ctypes.byref(params), ctypes.byref(st),
+                                                x.ctypes.data_as(_dp), v.ctypes.data_as(_dp), f.ctypes.data_as(_dp)))
+        assert np.array_equal(host.get(capi.COORD), x) and np.array_equal(host.get(capi.VELOCITY), v)
+        out.append((seq.get(capi.COORD), seq.get(capi.VELOCITY), x.copy(), v.copy()))
+    return out
+
+
+def test_host_step_on_a_batch(gpu):
+    """A batch handle (every mesh's nodes in one array), projected start."""
+    from helpers import Batch
+    from opentissue_gb300.workloads import random_beams
+    beams = random_beams(4, seed=7, nx=(8, 12), nyz=(3, 4))
+    seq, host = Batch(beams), Batch(beams)
+    coord = np.concatenate([b["coord"] for b in beams])
+    fixed = np.concatenate([b["fixed"] for b in beams])
+    mass = seq.get(capi.MASS)
+    params = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6,
+                                 warm_start=capi.WARM_START_PROJECTED)
+    out = _pair_host_steps(seq, host, coord, fixed, params, 5, True,
+                           lambda s: gravity_force(mass, fixed) * (1.0 + 0.3 * s))
+    for xs, vs, xh, vh in out:
+        assert np.abs(xh - xs).max() <= POS_TOL * np.abs(xs - coord).max()
+        assert np.abs(vh - vs).max() <= POS_TOL * np.abs(vs).max()
+    seq.close()
+    host.close()
+
+
+def test_host_step_with_plasticity(gpu):
+    """Plasticity adds to the external forces in the orientation phase, so the
+    host step copies the inputs before it: the same states as the sequence,
+    and the device forces as the step left them."""
+    tets, coord, fixed = beam(10, 4, 4, jitter_seed=4)
+    mat = (5e5, 0.33, 1000.0, 1e-4, 50.0, 1e-2)
+    seq, host = GpuMesh(tets, coord, fixed), GpuMesh(tets, coord, fixed)
+    seq.init(mat)
+    host.init(mat)
+    mass = seq.get(capi.MASS)
+    params = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=2000, rtol=1e-6)
+    out = _pair_host_steps(seq, host, coord, fixed, params, 6, False, lambda s: gravity_force(mass, fixed))
+    for xs, vs, xh, vh in out:
+        assert np.abs(xh - xs).max() <= POS_TOL * np.abs(xs - coord).max()
+        assert np.abs(vh - vs).max() <= POS_TOL * np.abs(vs).max()
+    assert np.abs(host.plastic()).max() > 0
+    assert np.abs(host.get(capi.F_EXTERNAL) - seq.get(capi.F_EXTERNAL)).max() <= \
+        POS_TOL * np.abs(seq.get(capi.F_EXTERNAL)).max()
+    seq.close()
+    host.close()
