@@ -2569,9 +2569,12 @@ struct SegSum {
   }
 };
 
-// Grid barrier whose last CTA runs fin(a, mesh, totals[kBatchSlots], counts)
-// for every mesh (totals: this round's accumulators, which it clears) and publishes
-// the 4 integer counts the finisher accumulates (e.g. meshes still active).
+// Grid barrier whose last CTA runs fin(a, mesh, totals[kBatchSlots], counts) for
+// every mesh (totals: this round's accumulators, which it clears afterwards)
+// and publishes the first two of the 4 integer counts the finisher
+// accumulates (e.g. meshes still active, each at most 65,535 here) in the
+// word that releases the round, so that the other CTAs read them with the
+// release instead of after it.
 template <typename Fin>
 __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (&counts)[4]) {
   __shared__ int s_flag;
@@ -2591,21 +2594,42 @@ __device__ bool batch_reduce(const MixedArgs& a, unsigned& round, Fin fin, int (
     for (int m = threadIdx.x; m < a.num_meshes; m += blockDim.x) {
       double t[kBatchSlots];
 #pragma unroll
-      for (int k = 0; k < kBatchSlots; ++k) {
-        t[k] = __ldcg(acc + kBatchSlots * m + k);
-        acc[kBatchSlots * m + k] = 0.0;  // for round r + 2
-      }
+      for (int k = 0; k < kBatchSlots; ++k) t[k] = __ldcg(acc + kBatchSlots * m + k);
       fin(a, m, t, s_cnt);
+#pragma unroll
+      for (int k = 0; k < kBatchSlots; ++k) acc[kBatchSlots * m + k] = 0.0;  // for round r + 2
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int k = 0; k < 4; ++k) a.sync->result[half][k] = double(s_cnt[k]);
-      release_round(a.sync, round);
+      clear_stale_acc(a.sync, round);
+      const unsigned long long packed =
+          (unsigned long long)min(s_cnt[0], 0xFFFF) | ((unsigned long long)min(s_cnt[1], 0xFFFF) << 16);
+      const unsigned long long word = (unsigned long long)round | (packed << 32);
+      asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(&a.sync->gen), "l"(word) : "memory");
     }
   } else if (threadIdx.x == 0 && s_flag == 1) {
-    const int ok = wait_released(a.sync, round, a.spin_limit) ? 1 : 0;
-    if (ok)
-      for (int k = 0; k < 4; ++k) s_cnt[k] = int(__ldcg(&a.sync->result[half][k]));
+    // wait for the release of this round; the counts come with it
+    const long long start = clock64();
+    unsigned polls = 0;
+    int ok = 1;
+    for (;;) {
+      unsigned long long w;
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(&a.sync->gen) : "memory");
+      if (int(unsigned(w) - round) >= 0) {
+        s_cnt[0] = int((w >> 32) & 0xFFFFull);
+        s_cnt[1] = int((w >> 48) & 0xFFFFull);
+        break;
+      }
+      if ((++polls & 63u) == 0u && ld_status(&a.sync->status) != 0) {
+        ok = 0;
+        break;
+      }
+      if (clock64() - start > a.spin_limit) {
+        atomicCAS(&a.sync->status, 0, OTFEM_ERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
+    }
     s_flag = ok;
   }
   __syncthreads();
