@@ -192,6 +192,43 @@ def oracle_sample(tets, coord, fixed, steps):
     return times, its
 
 
+def oracle_batch_sample(beams, steps, threads=None):
+    """The CPU baseline of the batch configuration: the C restatement of the
+    reference (converged CG, rel. residual 1e-6), each beam an independent
+    mesh, the beams spread over the host's cores (a pool of threads pulling
+    beams; the oracle's calls release the interpreter lock), `steps` steps
+    from rest under gravity and each beam's constant tip force, dt 0.005.
+    Returns (tet-steps/s, threads, wall seconds)."""
+    import concurrent.futures as cf
+    from oracle import build as obuild
+    from oracle import pyoracle as po
+    from opentissue_gb300 import workloads as wl
+    obuild.build_port()
+    threads = threads or os.cpu_count() or 1
+
+    def make(b):
+        m = po.OracleMesh(b["tets"], b["coord"], b["coord"], b["fixed"])
+        m.init(b["young"], b["poisson"], b["density"], 1e30, 0.0, 0.0)
+        return m, wl.batch_forces([b], m.get(po.MASS), 0, 0.005, False, [0.0])
+
+    def run(mf):
+        m, f = mf
+        for _ in range(steps):
+            m.set(po.F_EXTERNAL, f)
+            m.simulate_converged(0.005, True, WORKLOAD["mass_damping"], WORKLOAD["rtol"], 100000)
+
+    order = sorted(beams, key=lambda b: -b["tets"].shape[0])  # largest first
+    with cf.ThreadPoolExecutor(max_workers=threads) as pool:
+        meshes = list(pool.map(make, order))  # set-up, untimed
+        t0 = time.perf_counter()
+        list(pool.map(run, meshes))
+        wall = time.perf_counter() - t0
+    for m, _ in meshes:
+        m.close()
+    T = sum(b["tets"].shape[0] for b in beams)
+    return T * steps / wall, threads, wall
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -535,6 +572,13 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
         if warm == capi.WARM_START_LEARNED:
             net.detach(h)
         capi.check(lib.otfem_destroy(h))
+    if not args.no_cpu_baseline:
+        # the reference's method on the host: every beam an independent mesh,
+        # the beams spread over all host cores, 2 steps from rest
+        val, threads, wall = oracle_batch_sample(beams, 2)
+        res["cpu_baseline"] = {"value": val, "unit": "tet-steps/s", "cores": threads, "kind": "port",
+                               "sample": f"2 steps from rest of all {len(beams)} beams (constant tip force), "
+                                         f"converged CG, one beam per thread at a time, {wall:.1f} s wall"}
     res["projected_over_plain_cg"] = res["projected"]["tet_steps_per_s"] / res["plain_cg"]["tet_steps_per_s"]
     res["learned_over_plain_tip_sine"] = res["learned_tip_sine"]["tet_steps_per_s"] / res["plain_tip_sine"]["tet_steps_per_s"]
     res["timed_steps"] = f"steps {args.lead_in + args.warmup + 1}..{args.lead_in + args.warmup + args.batch_steps}"
