@@ -2755,6 +2755,119 @@ struct FinBatchRefresh {
   }
 };
 
+// Batches of at most kLocalMeshes meshes: every CTA runs each iteration's
+// scalar step (FinBatchIter's) itself, thread m for mesh m, on a shared-memory
+// copy of the meshes' iteration state and masks, right after the grid barrier
+// that completes the iteration's sums.  No CTA waits for a finisher to
+// release the round or reads the scalars and masks back from global memory.
+// All CTAs read the same totals and run the same FP32 code, so their copies
+// stay identical; CTA 0 writes its copy back to the BatchMesh records and the
+// global masks after the next grid barrier (when every CTA has read the
+// totals), for the finisher-style reductions (refresh, the end of the step)
+// that read them there.  Those reductions' results are loaded back into
+// every CTA's copy.
+constexpr int kLocalMeshes = 512;
+struct LocalMeshes {
+  unsigned char mask[3][kLocalMeshes];  // kMaskApply, kMaskUpdate, kMaskRefresh
+  unsigned char restart[kLocalMeshes];
+  float alpha[kLocalMeshes], beta[kLocalMeshes];
+  float prev_est[kLocalMeshes], thresh[kLocalMeshes], est[kLocalMeshes];
+  int iterations[kLocalMeshes], applies[kLocalMeshes];
+};
+
+// Every CTA: the copy of the meshes' state from the BatchMesh records and the
+// global masks (after a finisher-style reduction changed them).
+__device__ void local_load(const MixedArgs& a, LocalMeshes& L) {
+  const int m = threadIdx.x, M = a.num_meshes;
+  if (m < M) {
+    const BatchMesh& b = a.bm[m];
+    L.prev_est[m] = __ldcg(&b.prev_est);
+    L.thresh[m] = __ldcg(&b.thresh);
+    L.est[m] = __ldcg(&b.est);
+    L.iterations[m] = __ldcg(&b.iterations);
+    L.applies[m] = __ldcg(&b.applies);
+    L.restart[m] = __ldcg(&b.restart) != 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) L.mask[k][m] = __ldcg(a.bmask + k * M + m);
+  }
+  __syncthreads();
+}
+
+// The iteration's reduction without a finisher: a grid barrier, then every
+// CTA's scalar step for the meshes in the sweep (FinBatchIter on the copy).
+// counts[0]: meshes still iterating; counts[1]: meshes due for a refresh.
+__device__ bool batch_iter_local(const MixedArgs& a, unsigned& round, LocalMeshes& L, int (&counts)[4]) {
+  if (!grid_barrier(a.sync, a.spin_limit, round)) return false;
+  const int m = threadIdx.x, M = a.num_meshes;
+  bool active = false, refresh = false;
+  if (m < M) {
+    L.mask[kMaskUpdate][m] = 0;
+    L.mask[kMaskRefresh][m] = 0;
+    if (L.mask[kMaskApply][m]) {
+      const double* t = a.bacc + (size_t(round & 1u) * M + m) * kBatchSlots;
+      DF td[7];
+#pragma unroll
+      for (int k = 0; k < 7; ++k) td[k] = df_of(__ldcg(t + k));
+      float o[5];
+      FinPcgF{L.prev_est[m], L.restart[m] != 0}(td, o);
+      if (o[3] != 0.f) {
+        // 1: NaN/Inf in this mesh's system (an error, recorded by CTA 0 now:
+        // nothing reads the status during the solve); 2: finite breakdown
+        if (o[3] == 1.f && blockIdx.x == 0) a.bm[m].status = OTFEM_ERR_NONFINITE;
+        L.mask[kMaskApply][m] = 0;
+      } else {
+        L.alpha[m] = o[0];
+        L.beta[m] = o[1];
+        L.est[m] = o[2];
+        L.prev_est[m] = o[4];
+        L.restart[m] = 0;
+        const int its = ++L.iterations[m];
+        ++L.applies[m];
+        L.mask[kMaskUpdate][m] = 1;
+        // as FinBatchIter: refreshes at the next multiple of 4 iterations
+        // once the estimate reached the tolerance
+        refresh = (a.refresh > 0 && its % a.refresh == 0) || (o[2] <= L.thresh[m] && its % 4 == 0);
+        if (refresh) {
+          L.mask[kMaskRefresh][m] = 1;
+          ++L.applies[m];
+        } else if (its >= a.max_it) {
+          L.mask[kMaskApply][m] = 0;  // the update of this iteration is its last
+        }
+      }
+      active = L.mask[kMaskApply][m] != 0;
+    }
+  }
+  counts[0] = __syncthreads_count(active);
+  counts[1] = __syncthreads_count(refresh);
+  counts[2] = counts[3] = 0;
+  return true;
+}
+
+// CTA 0, after the grid barrier that follows the iteration of reduction
+// round `iter_round`: the copy into the BatchMesh records and the global
+// masks, and that round's totals cleared for round iter_round + 2.
+__device__ void local_store(const MixedArgs& a, const LocalMeshes& L, unsigned iter_round) {
+  const int m = threadIdx.x, M = a.num_meshes;
+  if (m >= M) return;
+  BatchMesh& b = a.bm[m];
+  if (L.mask[kMaskUpdate][m]) {
+    b.alpha = L.alpha[m];
+    b.beta = L.beta[m];
+    b.est = L.est[m];
+    b.rho = dfbits::widen(L.est[m]);
+    b.prev_est = L.prev_est[m];
+    b.restart = 0;
+    b.iterations = L.iterations[m];
+    b.applies = L.applies[m];
+  }
+  if (b.active && !L.mask[kMaskApply][m]) b.active = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) a.bmask[k * M + m] = L.mask[k][m];
+  double* t = a.bacc + (size_t(iter_round & 1u) * M + m) * kBatchSlots;
+#pragma unroll
+  for (int k = 0; k < kBatchSlots; ++k) t[k] = 0.0;
+}
+
 __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
   const int N = a.N, M = a.num_meshes;
   const float scale = float(a.dt * a.dt);
@@ -2935,6 +3048,16 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
     ss.flush(acc_half(round + 1));
   }
   if (!batch_reduce(a, round, FinBatchStart(), counts)) return;
+  // batches of at most kLocalMeshes meshes: the iterations' scalar steps in
+  // every CTA, and the sweeps' masks from shared memory
+  const bool local = M <= kLocalMeshes && blockDim.x == kBlock;
+  __shared__ LocalMeshes s_local;
+  if (local) {
+    local_load(a, s_local);
+    mask_apply = s_local.mask[kMaskApply];
+    mask_update = s_local.mask[kMaskUpdate];
+    mask_refresh = s_local.mask[kMaskRefresh];
+  }
   if (tracer) phase_stamp(a, 2, t_start);
   int n_active = counts[0];
   __shared__ double stamp[6];  // trace stamps, written by the tracer thread only
@@ -2972,14 +3095,19 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
       ss.flush(acc_half(round + 1));
     }
     if (tracer) stamp[2] = double(cycles_now() - t_start);
-    if (!batch_reduce(a, round, FinBatchIter(), counts)) return;
+    if (local) {
+      if (!batch_iter_local(a, round, s_local, counts)) return;
+    } else if (!batch_reduce(a, round, FinBatchIter(), counts)) {
+      return;
+    }
+    const unsigned iter_round = round;
     if (tracer) stamp[3] = double(cycles_now() - t_start);
     n_active = counts[0];
     const bool any_refresh = counts[1] > 0;
     // v += alpha p, r -= alpha q, p = r + beta p with each mesh's scalars
     masked_node_walk(a, mask_update, [&](bool valid, long i, int m) {
       if (!valid || a.fixed[i]) return;
-      const float alpha = a.bm[m].alpha, beta = a.bm[m].beta;
+      const float alpha = local ? s_local.alpha[m] : a.bm[m].alpha, beta = local ? s_local.beta[m] : a.bm[m].beta;
       float4 q4 = load_acc(a.q_f + i), p4 = a.p_f[i], r4 = a.r_f[i];
       float4 vh = a.v_f[i], vl = a.v_lo[i];
       const float d = a.diag_f[i];
@@ -2997,6 +3125,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
     });
     if (tracer) stamp[4] = double(cycles_now() - t_start);
     if (!grid_barrier(a.sync, a.spin_limit, round)) return;
+    if (local && blockIdx.x == 0) local_store(a, s_local, iter_round);
     // trace row: the meshes iterating, whether a refresh sweep follows
     if (tracer) trace_row(a, it, double(active_before), 0.0, any_refresh ? 1.0 : 0.0, 0.0, stamp, t_start);
     if (any_refresh) {
@@ -3026,6 +3155,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
       });
       ss.flush(acc_half(round + 1));
       if (!batch_reduce(a, round, FinBatchRefresh(), counts)) return;
+      if (local) local_load(a, s_local);
       n_active = counts[0];
     }
   }
