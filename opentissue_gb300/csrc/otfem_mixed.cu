@@ -1467,14 +1467,28 @@ __device__ void apply_active_meshes(const MixedArgs& a, const float4* u4, const 
                                     const unsigned char* mask) {
   const MeshList L = masked_meshes(a, a.mesh_tet_start, mask);
   const int TT = a.tile_tets, stride = gridDim.x * blockDim.x;
-  auto apply_v = [&](int v) {
+  // every mesh in the sweep: the virtual range is the tet range itself
+  const bool all = L.n == a.num_meshes;
+  auto tet_of = [&](int v) {
+    if (all) return v;
     const int j = L.entry(v);
-    const int t = L.beg[j] + (v - L.pref[j]);
-    const int tile = tile_of(t, a.tile_magic);
-    const StagedTetT<Stream> e(a.tile_f + size_t(tile) * kTileWords * TT, TT, t - tile * TT);
-    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
+    return L.beg[j] + (v - L.pref[j]);
   };
-  for (int v = int(sweep_first()); v < L.total; v += stride) apply_v(v);
+  // the next tet's node ids are loaded one tet ahead (as in the tets sweep)
+  int v = int(sweep_first());
+  int t = v < L.total ? tet_of(v) : 0;
+  int4 ids = v < L.total ? tile_node_ids<Stream>(a, t) : make_int4(0, 0, 0, 0);
+  for (; v < L.total; v += stride) {
+    const int cur_t = t;
+    const int4 cur = ids;
+    if (v + stride < L.total) {
+      t = tet_of(v + stride);
+      ids = tile_node_ids<Stream>(a, t);
+    }
+    const int tile = tile_of(cur_t, a.tile_magic);
+    const StagedTetT<Stream> e(a.tile_f + size_t(tile) * kTileWords * TT, TT, cur_t - tile * TT, cur);
+    tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, u4, ulo, q4);
+  }
 }
 
 template <bool Stream>
