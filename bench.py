@@ -8,12 +8,13 @@ dt = 0.01 s, gravity -9.81 in y, stiffness warping on, CG to relative
 residual 1e-6.  A "step" is one fem::simulate time step of the whole mesh.
 
 Metric: tet-steps/s = tets x steps / seconds.  `value` is the headline arm,
-the projected warm start (CG from the least-energy point on the span of the
-last four velocity changes, Jacobi PCG), next to the plain CG (the
-reference's method: previous-velocity start, no preconditioner) and the
-learned warm start (the trained network's correction added to the same
-search space) on the same trajectory; the learned start measures slower
-than the projected one (config.learned), so it is not the headline.  The
+the extrapolated warm start (CG from the velocity the degree-4 polynomial
+through the last five velocities predicts, Jacobi PCG), next to the plain CG
+(the reference's method: previous-velocity start, no preconditioner), the
+projected start (the least-energy point on the span of the last four
+velocity changes) and the learned warm start (the trained network's
+correction added to that search space) on the same trajectory; both measure
+slower than the extrapolated start (config.projected, config.learned).  The
 run first builds the network's training set with the plain solver on beams
 of the workload's family (other jitter seeds; gravity, every other beam
 with a sinusoidal tip load; 2M node samples) and trains it on the GPU
@@ -416,6 +417,7 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2):
     out = {}
     arms = (("plain", None, dict(preconditioner=capi.PRECONDITIONER_NONE)), ("plain_jacobi", None, {}),
             ("projected", None, dict(warm_start=capi.WARM_START_PROJECTED)),
+            ("extrapolated", None, dict(warm_start=capi.WARM_START_EXTRAPOLATED, warm_history=4)),
             ("learned", net, dict(warm_start=capi.WARM_START_LEARNED)))
     for name, mlp, kw in arms:
         h = make_handle(lib, capi, tets, coord, fixed, stream)
@@ -449,15 +451,17 @@ def run_inference_ab(lib, capi, torch, stream, net, args, flush_l2):
             res[k]["position_difference_vs_plain"] = float(np.abs(v["x"] - out["plain"]["x"]).max() / disp)
     res["learned_over_plain"] = out["learned"]["tet_steps_per_s"] / out["plain"]["tet_steps_per_s"]
     res["learned_over_projected"] = out["learned"]["tet_steps_per_s"] / out["projected"]["tet_steps_per_s"]
+    res["extrapolated_over_projected"] = (out["extrapolated"]["tet_steps_per_s"] /
+                                          out["projected"]["tet_steps_per_s"])
     return res
 
 
 def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
     """256 beams of uneven size (nx U{8..64}, ny, nz U{3..16}), per-beam
     material, random fixed face, gravity plus a tip force, dt 0.005, one
-    persistent launch per step: plain CG, Jacobi PCG and the projected start
-    under a constant tip force, then Jacobi PCG, projected and learned under a
-    sinusoidal tip force."""
+    persistent launch per step: plain CG, Jacobi PCG, the projected and the
+    extrapolated start under a constant tip force, then Jacobi PCG, projected,
+    extrapolated and learned under a sinusoidal tip force."""
     from opentissue_gb300 import workloads as wl
     from opentissue_gb300.workloads import random_beams
     beams = random_beams(args.batch_meshes, seed=args.seed)
@@ -483,8 +487,10 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
     arms = (("plain_cg", capi.WARM_START_PREVIOUS, False, capi.PRECONDITIONER_NONE),
             ("plain", capi.WARM_START_PREVIOUS, False, capi.PRECONDITIONER_JACOBI),
             ("projected", capi.WARM_START_PROJECTED, False, capi.PRECONDITIONER_JACOBI),
+            ("extrapolated", capi.WARM_START_EXTRAPOLATED, False, capi.PRECONDITIONER_JACOBI),
             ("plain_tip_sine", capi.WARM_START_PREVIOUS, True, capi.PRECONDITIONER_JACOBI),
             ("projected_tip_sine", capi.WARM_START_PROJECTED, True, capi.PRECONDITIONER_JACOBI),
+            ("extrapolated_tip_sine", capi.WARM_START_EXTRAPOLATED, True, capi.PRECONDITIONER_JACOBI),
             ("learned_tip_sine", capi.WARM_START_LEARNED, True, capi.PRECONDITIONER_JACOBI))
     for name, warm, vary, pre in arms:
         h = ctypes.c_void_p()
@@ -580,6 +586,7 @@ def run_batch_workload(lib, capi, torch, stream, net, args, flush_l2):
                                "sample": f"2 steps from rest of all {len(beams)} beams (constant tip force), "
                                          f"converged CG, one beam per thread at a time, {wall:.1f} s wall"}
     res["projected_over_plain_cg"] = res["projected"]["tet_steps_per_s"] / res["plain_cg"]["tet_steps_per_s"]
+    res["extrapolated_over_projected"] = res["extrapolated"]["tet_steps_per_s"] / res["projected"]["tet_steps_per_s"]
     res["learned_over_plain_tip_sine"] = res["learned_tip_sine"]["tet_steps_per_s"] / res["plain_tip_sine"]["tet_steps_per_s"]
     res["timed_steps"] = f"steps {args.lead_in + args.warmup + 1}..{args.lead_in + args.warmup + args.batch_steps}"
     return res
@@ -610,6 +617,10 @@ def run_ours(args, world, rank, local):
     plain = solver_params(preconditioner=capi.PRECONDITIONER_NONE)
     plain_jacobi = solver_params()
     projected = solver_params(warm_start=capi.WARM_START_PROJECTED)
+    # the headline: CG from the velocity extrapolated by the degree-4
+    # polynomial through the last five velocities (no extra element apply)
+    extrapolated = solver_params(warm_start=capi.WARM_START_EXTRAPOLATED, warm_history=4)
+    head = extrapolated
     # the same Jacobi PCG with every vector, reduction and scalar in FP64 and
     # the FP64 element apply (the precision the scope names for the CG
     # scalars, at FP64 cost)
@@ -680,9 +691,10 @@ def run_ours(args, world, rank, local):
                 "x": x, "fext": fext, "oracle_error": check.result()}
 
     # ---- plain CG (the reference's method) and the headline arm, the
-    # projected start; then the learned start (the network's correction in the
-    # same search space), Jacobi-preconditioned CG and the other ablations,
-    # each on the same trajectory
+    # extrapolated start; then the projected start, the learned start (the
+    # network's correction in the projected start's search space),
+    # Jacobi-preconditioned CG and the other ablations, each on the same
+    # trajectory
     h_plain = make_handle(lib, capi, tets, coord, fixed, stream)
     h_head = make_handle(lib, capi, tets, coord, fixed, stream)
     sampler = ClockSampler(local)
@@ -691,11 +703,11 @@ def run_ours(args, world, rank, local):
     r_plain = timed_run(h_plain, plain)
     # the headline handle stays at the timed steps' point of the trajectory:
     # the end-to-end steps below continue from there
-    r_head = timed_run(h_head, projected, continue_to_end=False)
+    r_head = timed_run(h_head, head, continue_to_end=False)
     clocks = sampler.stop()
     ablations = {}
-    for name, prm in (("learned", learned), ("plain_jacobi", plain_jacobi), ("fp64_jacobi", fp64_jacobi),
-                      ("learned_history3", learned_h3)):
+    for name, prm in (("projected", projected), ("learned", learned), ("plain_jacobi", plain_jacobi),
+                      ("fp64_jacobi", fp64_jacobi), ("learned_history3", learned_h3)):
         h_ab = make_handle(lib, capi, tets, coord, fixed, stream)
         if prm.warm_start == capi.WARM_START_LEARNED:
             net.attach(h_ab)
@@ -706,6 +718,7 @@ def run_ours(args, world, rank, local):
     disp = np.abs(r_plain["x"] - coord).max()
     pos_diff = float(np.abs(r_head["x"] - r_plain["x"]).max() / max(disp, 1e-300))
     r_learn = ablations["learned"]
+    r_proj = ablations["projected"]
 
     # ---- roofline: the persistent CG kernel timed on its own ---------------
     cg_ms, cg_bytes, cg_applies = [], [], []
@@ -775,7 +788,7 @@ def run_ours(args, world, rank, local):
         flush_l2()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        capi.check(lib.otfem_simulate_host(h_head, w["dt"], 1, ctypes.byref(projected), None,
+        capi.check(lib.otfem_simulate_host(h_head, w["dt"], 1, ctypes.byref(head), None,
                                            pin_x.ctypes.data_as(_dp), pin_v.ctypes.data_as(_dp),
                                            pin_f.ctypes.data_as(_dp)))
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
@@ -788,7 +801,7 @@ def run_ours(args, world, rank, local):
         capi.check(lib.otfem_set_nodes(h_head, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
         capi.check(lib.otfem_set_nodes(h_head, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
         capi.check(lib.otfem_set_nodes(h_head, capi.F_EXTERNAL, pin_f.ctypes.data_as(_dp), pin_f.size))
-        capi.check(lib.otfem_simulate_ex(h_head, w["dt"], 1, ctypes.byref(projected), None))
+        capi.check(lib.otfem_simulate_ex(h_head, w["dt"], 1, ctypes.byref(head), None))
         # both downloads queued back to back, one wait
         capi.check(lib.otfem_get_nodes_async(h_head, capi.COORD, pin_x.ctypes.data_as(_dp), pin_x.size))
         capi.check(lib.otfem_get_nodes_async(h_head, capi.VELOCITY, pin_v.ctypes.data_as(_dp), pin_v.size))
@@ -805,7 +818,7 @@ def run_ours(args, world, rank, local):
         capi.check(lib.otfem_set_nodes(h_chk, capi.F_EXTERNAL, fext_chk.ctypes.data_as(_dp), fext_chk.size))
         chk = OracleError(fix128)
         for step in range(1, max(chk.keep) + 1):
-            capi.check(lib.otfem_simulate_ex(h_chk, w["dt"], 1, ctypes.byref(projected), None))
+            capi.check(lib.otfem_simulate_ex(h_chk, w["dt"], 1, ctypes.byref(head), None))
             if chk.wants(step):
                 chk.record(step, *get_xv(lib, capi, h_chk, N))
         capi.check(lib.otfem_destroy(h_chk))
@@ -825,6 +838,7 @@ def run_ours(args, world, rank, local):
     value = total_tet_steps / r_head["dev_s"]
     plain_value = total_tet_steps / r_plain["dev_s"]
     learned_value = total_tet_steps / r_learn["dev_s"]
+    projected_value = total_tet_steps / r_proj["dev_s"]
     e2e_value = total_tet_steps / e2e_s
     e2e_staged_value = total_tet_steps / staged_s
     if rank != 0:
@@ -840,12 +854,13 @@ def run_ours(args, world, rank, local):
         "dtype": "f32 element apply and CG vectors (velocity as f32 hi/lo pairs), f32-pair reductions and scalars",
         "data": "synthetic",
         "config": {"workload": WORKLOAD["name"],
-                   "warm_start": "projected: CG starts from the least-energy point on v + span{last "
-                                 f"{projected.warm_history} velocity changes}}.  The learned start (the trained "
-                                 "network's correction added to the same search space) is measured below "
-                                 "(config.learned) and is slower: the network adds no direction the history "
-                                 "does not already span, and costs a features-and-network kernel and one more "
-                                 "search direction per step",
+                   "warm_start": "extrapolated: CG starts from v + the velocity change the polynomial of "
+                                 f"degree {head.warm_history} through the last {head.warm_history + 1} velocities "
+                                 "predicts (the sum of the newest change's backward differences), no extra "
+                                 "element apply.  The projected start (the least-energy point on v + span{last "
+                                 f"{projected.warm_history} velocity changes}}, one extra apply per direction) and "
+                                 "the learned start (the trained network's correction added to that search "
+                                 "space) are measured below (config.projected, config.learned) and are slower",
                    "solver": "matrix-free persistent CG (OTFEM_SOLVER_MIXED), CUDA graph per step",
                    "preconditioner": "node Jacobi (OTFEM_PRECONDITIONER_JACOBI, the default)",
                    "l2": "flushed (512 MiB write) before every timed step", "replicas": world,
@@ -860,6 +875,13 @@ def run_ours(args, world, rank, local):
                              "iterations_per_step": float(np.mean(r_plain["its"])),
                              "max_rel_residual": float(np.max(r_plain["res"])),
                              "oracle_error": r_plain["oracle_error"]},
+                   "projected": {"method": "CG from the least-energy point on v + span{last "
+                                           f"{projected.warm_history} velocity changes}}, Jacobi PCG",
+                                 "value": projected_value, "unit": "tet-steps/s",
+                                 "ms_per_step": 1e3 * r_proj["dev_s"] / args.steps,
+                                 "iterations_per_step": float(np.mean(r_proj["its"])),
+                                 "max_rel_residual": float(np.max(r_proj["res"])),
+                                 "oracle_error": r_proj["oracle_error"]},
                    "learned": {"method": "node MLP (v, dv_prev, f_ext, 1-ring mean of Re; 3x64 GELU, BF16 "
                                          "tensor cores) trained in this run on 2M (state, converged dv) pairs; its "
                                          "correction joins the last 4 velocity changes in the search space",
@@ -867,17 +889,19 @@ def run_ours(args, world, rank, local):
                                "ms_per_step": 1e3 * r_learn["dev_s"] / args.steps,
                                "iterations_per_step": float(np.mean(r_learn["its"])),
                                "learned_over_plain": learned_value / plain_value,
-                               "learned_over_projected": learned_value / value,
+                               "learned_over_projected": learned_value / projected_value,
                                "oracle_error": r_learn["oracle_error"]},
                    "ablations": {k: {"value": total_tet_steps / r["dev_s"], "unit": "tet-steps/s",
                                      "ms_per_step": 1e3 * r["dev_s"] / args.steps,
                                      "iterations_per_step": float(np.mean(r["its"])),
                                      "max_rel_residual": float(np.max(r["res"])),
                                      "oracle_error": r["oracle_error"]} for k, r in ablations.items()
-                                 if k != "learned"},
-                   "projected_over_plain": value / plain_value,
+                                 if k not in ("learned", "projected")},
+                   "extrapolated_over_plain": value / plain_value,
+                   "extrapolated_over_projected": value / projected_value,
+                   "projected_over_plain": projected_value / plain_value,
                    "learned_over_plain": learned_value / plain_value,
-                   "learned_over_projected": learned_value / value,
+                   "learned_over_projected": learned_value / projected_value,
                    "position_difference_vs_plain": pos_diff,
                    "training": train_info,
                    "other_configurations": extra},

@@ -52,6 +52,16 @@ inline SolverParams projected_solver(double rtol = 1e-6, int history = 4, int ma
   return p;
 }
 
+// The matrix-free solver starting from the velocity extrapolated by the
+// polynomial of degree `degree` through the last degree + 1 velocities (the
+// same stopping rule; no extra element-apply).
+inline SolverParams extrapolated_solver(double rtol = 1e-6, int degree = 4, int max_iterations = 10000) {
+  SolverParams p = mixed_solver(rtol, max_iterations);
+  p.warm_start = OTFEM_WARM_START_EXTRAPOLATED;
+  p.warm_history = degree;
+  return p;
+}
+
 namespace gpu {
 
 inline void check(int rc, char const* where) {

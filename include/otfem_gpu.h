@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define OTFEM_ABI_VERSION 7
+#define OTFEM_ABI_VERSION 8
 
 #if defined(__GNUC__)
 #define OTFEM_API __attribute__((visibility("default")))
@@ -85,10 +85,19 @@ enum {
   /* CG starts from the point of least energy on v + span{the last
    * warm_history velocity changes} (projection onto previous solutions);
    * one extra element-apply per vector and step */
-  OTFEM_WARM_START_PROJECTED = 2
+  OTFEM_WARM_START_PROJECTED = 2,
+  /* CG starts from v + the velocity change extrapolated by the polynomial of
+   * degree warm_history through the last warm_history + 1 velocities (the sum
+   * of the newest change's backward differences up to order warm_history - 1;
+   * the degree is lowered while fewer steps are recorded since otfem_init or
+   * since a step that recorded none).  No extra element-apply.  A smooth
+   * trajectory's next velocity is predicted well; after an abrupt change of
+   * the motion (a velocity set by hand, a jump of the load) the start can be
+   * poor for a few steps, and CG still stops at the same residual. */
+  OTFEM_WARM_START_EXTRAPOLATED = 3
 };
 
-/* Velocity changes kept for the projected and learned starts. */
+/* Velocity changes kept for the projected, learned and extrapolated starts. */
 #define OTFEM_MAX_WARM_HISTORY 8
 
 enum {
@@ -114,14 +123,15 @@ typedef struct otfem_solver_params {
                                totals in CTA order; 1 also orders the
                                projected start's Gram sums, the FP64 solver's and the
                                batches' sums, 0 = FP64 atomic accumulation of those */
-  int warm_start;           /* OTFEM_WARM_START_* (PROJECTED and LEARNED: OTFEM_SOLVER_MIXED,
+  int warm_start;           /* OTFEM_WARM_START_* (PROJECTED, LEARNED, EXTRAPOLATED: OTFEM_SOLVER_MIXED,
                                single meshes and batches; a batch solves each mesh's own
                                search space) */
   int graph;                /* 1 = replay the step from a CUDA graph (default) */
   int preconditioner;       /* matrix-free: OTFEM_PRECONDITIONER_* (default JACOBI);
                                the reference solver ignores it */
   int warm_history;         /* projected and learned starts: previous velocity changes in the
-                               search space, 0..OTFEM_MAX_WARM_HISTORY (default 4) */
+                               search space; extrapolated start: the polynomial degree;
+                               0..OTFEM_MAX_WARM_HISTORY (default 4) */
 } otfem_solver_params;
 
 typedef struct otfem_step_stats {

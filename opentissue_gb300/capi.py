@@ -25,7 +25,7 @@ ERR_UNSUPPORTED = -8
 COORD, MODEL_COORD, VELOCITY, F_EXTERNAL, MASS, F0, B, NODE_STIFFNESS = range(8)
 # solvers
 SOLVER_REFERENCE, SOLVER_MIXED, SOLVER_FP64 = 0, 1, 2
-WARM_START_PREVIOUS, WARM_START_LEARNED, WARM_START_PROJECTED = 0, 1, 2
+WARM_START_PREVIOUS, WARM_START_LEARNED, WARM_START_PROJECTED, WARM_START_EXTRAPOLATED = 0, 1, 2, 3
 MAX_WARM_HISTORY = 8
 PRECONDITIONER_NONE, PRECONDITIONER_JACOBI = 0, 1
 PHASE_ORIENT, PHASE_SOLVE = 1, 2

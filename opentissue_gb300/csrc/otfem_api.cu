@@ -67,7 +67,7 @@ void free_all(Context& c) {
   if (c.stats_host) cudaFreeHost(c.stats_host);
   if (c.bmesh_host) cudaFreeHost(c.bmesh_host);
   void* batch[] = {c.mesh_of_node, c.mesh_of_tet, c.mesh_tet_start, c.mesh_node_start, c.bmesh, c.bacc, c.bmask,
-                   c.warm_hist, c.warm_prod, c.warm_part, c.warm_bacc};
+                   c.warm_hist, c.warm_prod, c.warm_part, c.warm_bacc, c.hist_fill};
   for (void* p : batch)
     if (p) cudaFree(p);
   if (c.graph) cudaGraphExecDestroy(c.graph);
@@ -104,7 +104,7 @@ int check_params(const Context& c, const otfem_solver_params& p) {
   if (p.solver != OTFEM_SOLVER_REFERENCE && !(p.rtol >= 0.0))
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "rtol must be non-negative");
   if (p.warm_start != OTFEM_WARM_START_PREVIOUS && p.warm_start != OTFEM_WARM_START_LEARNED &&
-      p.warm_start != OTFEM_WARM_START_PROJECTED)
+      p.warm_start != OTFEM_WARM_START_PROJECTED && p.warm_start != OTFEM_WARM_START_EXTRAPOLATED)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown warm start");
   if (p.warm_history < 0 || p.warm_history > OTFEM_MAX_WARM_HISTORY)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "warm_history out of range");
@@ -118,18 +118,24 @@ int check_params(const Context& c, const otfem_solver_params& p) {
     return fail(OTFEM_ERR_UNSUPPORTED, "the projected start runs with OTFEM_SOLVER_MIXED");
   if (p.warm_start == OTFEM_WARM_START_PROJECTED && p.warm_history < 1)
     return fail(OTFEM_ERR_INVALID_ARGUMENT, "the projected start needs warm_history >= 1");
+  if (p.warm_start == OTFEM_WARM_START_EXTRAPOLATED && p.solver != OTFEM_SOLVER_MIXED)
+    return fail(OTFEM_ERR_UNSUPPORTED, "the extrapolated start runs with OTFEM_SOLVER_MIXED");
+  if (p.warm_start == OTFEM_WARM_START_EXTRAPOLATED && p.warm_history < 1)
+    return fail(OTFEM_ERR_INVALID_ARGUMENT, "the extrapolated start needs warm_history >= 1");
   if (p.warm_start == OTFEM_WARM_START_LEARNED && !c.mlp)
     return fail(OTFEM_ERR_NOT_INITIALIZED, "learned warm start without a network (otfem_set_mlp)");
   return OTFEM_OK;
 }
 
-// The projected and learned starts search previous velocity
-// changes: their history, the products and sums are allocated (the history
-// zeroed) by the first step that needs them; from then on every mixed step
-// of the mesh records its velocity change.
+// The projected and learned starts search previous velocity changes and
+// the extrapolated start sums them: their history, the products and sums are
+// allocated (the history and its fill count zeroed) by the first step that
+// needs them; from then on every mixed step of the mesh records its velocity
+// change.
 cudaError_t ensure_history(Context& c, const otfem_solver_params& p) {
   const bool needs = p.solver == OTFEM_SOLVER_MIXED &&
-                     (p.warm_start == OTFEM_WARM_START_PROJECTED || p.warm_start == OTFEM_WARM_START_LEARNED);
+                     (p.warm_start == OTFEM_WARM_START_PROJECTED || p.warm_start == OTFEM_WARM_START_LEARNED ||
+                      p.warm_start == OTFEM_WARM_START_EXTRAPOLATED);
   if (!needs || c.warm_hist) return cudaSuccess;
   const size_t n = size_t(c.N > 0 ? c.N : 1);
   cudaError_t e;
@@ -141,7 +147,16 @@ cudaError_t ensure_history(Context& c, const otfem_solver_params& p) {
       (e = cudaMalloc(&c.warm_bacc, sizeof(double) * (otfem::kMaxWarmSums * size_t(c.num_meshes) + 8))) !=
           cudaSuccess)
     return e;
+  if ((e = cudaMalloc(&c.hist_fill, sizeof(int))) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(c.hist_fill, 0, sizeof(int), c.stream)) != cudaSuccess) return e;
   return cudaMemsetAsync(c.warm_hist, 0, sizeof(float4) * 2 * otfem::kMaxHistory * n, c.stream);
+}
+
+// A step that records no velocity change (the reference and FP64 solvers,
+// the reference's stages) leaves the history without the newest change:
+// the extrapolated start starts over.
+cudaError_t history_gap(Context& c) {
+  return c.hist_fill ? cudaMemsetAsync(c.hist_fill, 0, sizeof(int), c.stream) : cudaSuccess;
 }
 
 // After the orientation phase of a matrix-free step: the network inputs of
@@ -162,6 +177,10 @@ cudaError_t enqueue_orient(Context& c, double dt, bool warp, const otfem_solver_
   return e != cudaSuccess ? e : launch_warm_start(c, p);
 }
 cudaError_t enqueue_solve(Context& c, double dt, const otfem_solver_params& p) {
+  if (p.solver == OTFEM_SOLVER_FP64) {
+    cudaError_t e = history_gap(c);
+    if (e != cudaSuccess) return e;
+  }
   return c.num_meshes > 1 ? otfem::launch_batch_solve(c, dt, p) : otfem::launch_mixed_solve(c, dt, p);
 }
 
@@ -177,6 +196,7 @@ cudaError_t enqueue_step(Context& c, double dt, bool warp, const otfem_solver_pa
         cudaSuccess)
       return e;
     if ((e = otfem::launch_position_update(c, dt)) != cudaSuccess) return e;
+    if ((e = history_gap(c)) != cudaSuccess) return e;
   } else {
     if ((e = enqueue_orient(c, dt, warp, p)) != cudaSuccess) return e;
     if ((e = enqueue_solve(c, dt, p)) != cudaSuccess) return e;
@@ -490,6 +510,7 @@ static int init_impl(Context& c, double young, double poisson, double density, d
   OT_CUDA(cudaMemsetAsync(c.warm_dv, 0, sizeof(float4) * size_t(c.N), c.stream));
   if (c.warm_hist)
     OT_CUDA(cudaMemsetAsync(c.warm_hist, 0, sizeof(float4) * 2 * otfem::kMaxHistory * size_t(c.N), c.stream));
+  if (c.hist_fill) OT_CUDA(cudaMemsetAsync(c.hist_fill, 0, sizeof(int), c.stream));
   // choose the element-apply variant for this mesh
   if ((e = otfem::autotune_apply(c)) != cudaSuccess) return cuda_fail(e, "autotune");
   std::vector<double> vol(size_t(c.T));
@@ -803,7 +824,7 @@ int otfem_simulate_phase(otfem_handle h, double dt, int warp, const otfem_solver
     if (p.warm_start == OTFEM_WARM_START_LEARNED || c.collect) c.launches += 1;
     if (p.warm_start == OTFEM_WARM_START_LEARNED) c.launches += c.warm_smoothing;
   } else if (phase == OTFEM_PHASE_SOLVE) {
-    e = c.num_meshes > 1 ? otfem::launch_batch_solve(c, dt, p) : otfem::launch_mixed_solve(c, dt, p);
+    e = enqueue_solve(c, dt, p);
     if (e != cudaSuccess) return cuda_fail(e, "solve phase");
     OT_CUDA(cudaMemcpyAsync(c.stats_host, c.stats, sizeof(otfem::DeviceStats), cudaMemcpyDeviceToHost, c.stream));
     c.launches += 2;
@@ -966,6 +987,7 @@ int otfem_reference_stage(otfem_handle h, int stage, double dt, double mass_damp
     default:
       return fail(OTFEM_ERR_INVALID_ARGUMENT, "unknown stage");
   }
+  if (e == cudaSuccess) e = history_gap(c);  // the reference's steps record no velocity change
   if (e != cudaSuccess) return cuda_fail(e, "reference stage");
   OT_CUDA(cudaStreamSynchronize(c.stream));
   return OTFEM_OK;

@@ -178,6 +178,9 @@ struct Context {
   // directions with A, the network's correction as a direction, and per-CTA
   // partial sums of the Gram system
   float4* warm_hist = nullptr;    // 2 kMaxHistory x N: hi parts, then lo parts
+  // the number of history levels that hold backward differences of the last
+  // steps' velocity changes (device; the extrapolated start's degree limit)
+  int* hist_fill = nullptr;
   float4* warm_prod = nullptr;    // (kMaxWarmDirs + 1) x N: products, then the correction
   double* warm_part = nullptr;    // kMaxWarmSums x max grid
   double* warm_bacc = nullptr;    // batch: num_meshes x kMaxWarmSums (+ 8) per-mesh Gram totals

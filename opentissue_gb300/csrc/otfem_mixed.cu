@@ -147,6 +147,8 @@ struct MixedArgs {
   int hist_k;                           // basis vectors searched this step
   int hist_rec;                         // basis vectors the step records
   int nwarm;                            // search directions this step (0: start from v)
+  int extrap_k;                         // extrapolated start: the polynomial degree (0: none)
+  int* hist_fill;                       // history levels holding the last steps' differences
   float4* v_keep;                       // kept iterates: copy k at v_keep[2kN + i] (hi), [(2k+1)N + i] (lo)
   // batched solve (see Context)
   int num_meshes;
@@ -1950,6 +1952,45 @@ __device__ __forceinline__ void record_velocity_change(const MixedArgs& a, long 
   }
 }
 
+// Extrapolated start: v + D_0 + ... + D_{deg-1}, the polynomial of degree deg
+// through the last deg + 1 velocities evaluated at the next step (Newton's
+// backward-difference form: the next change is the sum of the newest
+// change's backward differences), in (hi, lo) pairs from the stored levels.
+__device__ __forceinline__ void extrapolate(const MixedArgs& a, long i, int deg, DF (&v)[3]) {
+  const long N = a.N;
+  for (int j0 = 0; j0 < deg; j0 += 4) {
+    float4 h[4], l[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k < deg) {
+        h[k] = a.hist[size_t(j0 + k) * N + i];
+        l[k] = a.hist[size_t(kMaxHistory + j0 + k) * N + i];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (j0 + k >= deg) break;
+      v[0] = df_add(v[0], DF{h[k].x, l[k].x});
+      v[1] = df_add(v[1], DF{h[k].y, l[k].y});
+      v[2] = df_add(v[2], DF{h[k].z, l[k].z});
+    }
+  }
+}
+// The degree the extrapolated start uses: at most the levels that hold
+// differences of recorded steps.
+__device__ __forceinline__ int extrap_degree(const MixedArgs& a) {
+  if (a.extrap_k <= 0 || !a.hist_fill) return 0;
+  const int fill = *a.hist_fill;
+  return fill < a.extrap_k ? fill : a.extrap_k;
+}
+// One thread, after every CTA read the count: a step that recorded R levels
+// leaves min(fill + 1, R) of them holding differences of recorded steps.
+__device__ __forceinline__ void advance_fill(const MixedArgs& a) {
+  if (!a.hist_fill || a.hist_rec <= 0) return;
+  const int f = *a.hist_fill + 1;
+  *a.hist_fill = f < a.hist_rec ? f : a.hist_rec;
+}
+
 __device__ __forceinline__ void finish_stats(const MixedArgs& a, int it, int applies, bool converged, double rho,
                                              double rho0, double bnorm2) {
   int st = ld_status(&a.sync->status);
@@ -1995,6 +2036,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(MixedArgs a) {
   // ascending tet order and summed as (hi, lo) pairs; the diagonal
   // M(1 + dt*alpha) of fem_dynamics_assembly.h:84-85; v split into (hi, lo).
   DF bbsum[1] = {{0.f, 0.f}};
+  const int deg = extrap_degree(a);
   for (long i = n0; i < N; i += gstride) {
     DF g[3];
     gather_forces(a, i, g);
@@ -2027,9 +2069,12 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(MixedArgs a) {
     a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);
     // fixed columns keep their velocity in the initial residual (the reference
     // multiplies A_ij by the fixed node's m_velocity); rows of fixed nodes are
-    // never accumulated (w = 0).
-    a.v_f[i] = make_float4(vi[0].hi, vi[1].hi, vi[2].hi, fx ? 0.f : 1.f);
-    a.v_lo[i] = make_float4(vi[0].lo, vi[1].lo, vi[2].lo, 0.f);
+    // never accumulated (w = 0).  The extrapolated start moves free nodes'
+    // iterates (b above keeps m v).
+    DF v0[3] = {vi[0], vi[1], vi[2]};
+    if (deg > 0 && !fx) extrapolate(a, i, deg, v0);
+    a.v_f[i] = make_float4(v0[0].hi, v0[1].hi, v0[2].hi, fx ? 0.f : 1.f);
+    a.v_lo[i] = make_float4(v0[0].lo, v0[1].lo, v0[2].lo, 0.f);
     a.q_f[i] = zero4;
     if (a.nwarm) {
       // learned start: the network's correction c = its dv - dv_prev is the
@@ -2305,7 +2350,10 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_mixed(MixedArgs a) {
     if (a.hist) record_velocity_change(a, i, dv);
   }
   if (tracer) phase_stamp(a, 4, t_start);
-  if (blockIdx.x == 0 && threadIdx.x == 0) finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    finish_stats(a, it, applies, converged, rho, rho0, bnorm2);
+    advance_fill(a);
+  }
 }
 
 // K2, FP64 solver: every vector and reduction in FP64.
@@ -2903,7 +2951,9 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
   const long long t_start = tracer ? cycles_now() : 0ll;
   if (tracer) clear_phase_stamps(a);
 
-  // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess), q = 0
+  // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess or
+  // extrapolation), q = 0
+  const int deg = extrap_degree(a);
   {
     SegSum<1> ss;
     ss.start(first_mesh);
@@ -2942,8 +2992,10 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
           a.diag_lo[i] = 0.f;
         }
         a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
-        a.v_f[i] = make_float4(vi[0].hi, vi[1].hi, vi[2].hi, fx ? 0.f : 1.f);
-        a.v_lo[i] = make_float4(vi[0].lo, vi[1].lo, vi[2].lo, 0.f);
+        DF v0[3] = {vi[0], vi[1], vi[2]};
+        if (deg > 0 && !fx) extrapolate(a, i, deg, v0);  // extrapolated start (as k_cg_mixed)
+        a.v_f[i] = make_float4(v0[0].hi, v0[1].hi, v0[2].hi, fx ? 0.f : 1.f);
+        a.v_lo[i] = make_float4(v0[0].lo, v0[1].lo, v0[2].lo, 0.f);
         a.q_f[i] = zero4;
         if (a.nwarm) {
           // learned start: the network's correction is the last search direction
@@ -3215,6 +3267,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
     a.stats->rr = rel;
     a.stats->rr0 = rel0;
     a.stats->bb = 1.0;
+    advance_fill(a);
   }
 }
 
@@ -4000,8 +4053,10 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   if (a.hist && prm.warm_start == OTFEM_WARM_START_PROJECTED) a.hist_k = prm.warm_history;
   if (a.hist && learned) a.hist_k = std::max(prm.warm_history, 1);
   a.nwarm = a.hist_k + (learned ? 1 : 0);
-  // a step records the levels it searches (all of them when it searches none)
-  a.hist_rec = a.hist ? (a.hist_k > 0 ? a.hist_k : kMaxHistory) : 0;
+  a.extrap_k = a.hist && prm.warm_start == OTFEM_WARM_START_EXTRAPOLATED ? prm.warm_history : 0;
+  a.hist_fill = c.hist_fill;
+  // a step records the levels it searches or sums (all of them when it uses none)
+  a.hist_rec = a.hist ? (a.hist_k > 0 ? a.hist_k : (a.extrap_k > 0 ? a.extrap_k : kMaxHistory)) : 0;
   a.num_meshes = c.num_meshes;
   a.mesh_of_node = c.mesh_of_node;
   a.mesh_of_tet = c.mesh_of_tet;

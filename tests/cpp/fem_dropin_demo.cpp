@@ -58,6 +58,7 @@ int main(int argc, char** argv) {
     if (std::strcmp(solver, "sequential") == 0) params.sequential_dots = 1;
     if (std::strcmp(solver, "mixed") == 0) params = OpenTissue::fem::mixed_solver(1e-6);
     if (std::strcmp(solver, "projected") == 0) params = OpenTissue::fem::projected_solver(1e-6, 4);
+    if (std::strcmp(solver, "extrapolated") == 0) params = OpenTissue::fem::extrapolated_solver(1e-6, 4);
     FILE* out = std::fopen(argv[6], "wb");
     if (!out) return 3;
     std::vector<double> buf(3 * mesh.size_nodes());

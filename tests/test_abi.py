@@ -39,7 +39,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_defaults(lib):
-    assert lib.otfem_abi_version() == 7
+    assert lib.otfem_abi_version() == 8
     p = capi.default_params()
     assert p.solver == capi.SOLVER_REFERENCE
     assert p.mass_damping == 2.0 and p.min_iterations == 20 and p.max_iterations == 20

@@ -191,6 +191,28 @@ def test_batch_projected_start_per_mesh(gpu):
     b1.close()
 
 
+def test_batch_extrapolated_start_per_mesh(gpu):
+    """Each mesh of a batch starts from its own extrapolated velocity: the
+    same answer as the plain start, fewer iterations once the history has
+    filled."""
+    beams = random_beams(5, seed=36, nx=(10, 16), nyz=(3, 5))
+    steps = 12
+    b0, out0 = run_batch(beams, steps)
+    b1, out1 = run_batch(beams, steps, warm_start=capi.WARM_START_EXTRAPOLATED, warm_history=4)
+    for s in range(steps):
+        for k, bm in enumerate(beams):
+            disp = np.abs(out0[s][0][k] - bm["coord"]).max()
+            assert np.abs(out1[s][0][k] - out0[s][0][k]).max() <= 1e-5 * disp, (s, k)
+        its, st, rel, _ = out1[s][1]
+        assert np.all(st == capi.OK) and np.all(rel <= 1e-6)
+    late0 = np.sum([o[1][0] for o in out0[6:]])
+    late1 = np.sum([o[1][0] for o in out1[6:]])
+    print("batch iterations, steps 7-12: plain start", late0, "extrapolated", late1)
+    assert late1 < 0.75 * late0, (late0, late1)
+    b0.close()
+    b1.close()
+
+
 def test_batch_learned_start_per_mesh(gpu):
     """A network attached to a batch: each mesh starts from its least-energy
     point over the network's correction and its own history.  The network is

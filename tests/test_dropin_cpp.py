@@ -117,7 +117,7 @@ def test_dropin_cpp_default_and_mixed_solvers(gpu, oracle, tmp_path):
     from helpers import run_oracle
     _, ref = run_oracle(oracle, g["tets"], g["coord"], g["fixed"], 10, converged=True)
     x_ref = ref[-1][0]
-    for solver in ("mixed", "projected"):
+    for solver in ("mixed", "projected", "extrapolated"):
         data = _run_demo(exe, str(tmp_path), (10, 4, 4), 10, solver)
         assert np.abs(data[-1, 0] - x_ref).max() <= 1e-5 * np.abs(x_ref - g["coord"]).max(), solver
 

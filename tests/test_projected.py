@@ -169,7 +169,7 @@ def test_projected_start_parameter_checks(gpu):
     assert rc == capi.ERR_INVALID_ARGUMENT
     rc, _ = m.step(0.01, True, params(solver=capi.SOLVER_FP64, warm_start=capi.WARM_START_PROJECTED), check=False)
     assert rc == capi.ERR_UNSUPPORTED
-    rc, _ = m.step(0.01, True, params(warm_start=3), check=False)
+    rc, _ = m.step(0.01, True, params(warm_start=4), check=False)
     assert rc == capi.ERR_INVALID_ARGUMENT
     m.close()
 

@@ -32,8 +32,9 @@ measured up to 1.9x in x and 5.1x in v.)
     under a sinusoidal tip force, 40 steps (steps 1, 20, 40; 256 sampled
     nodes per beam)
 Arms: plain CG (the reference's method: no preconditioner, previous-velocity
-start), Jacobi PCG, the projected start and the learned start (a network
-trained here on other beams of the same family).
+start), Jacobi PCG, the projected start, the extrapolated start (degree 4)
+and the learned start (a network trained here on other beams of the same
+family).
 """
 import ctypes
 
@@ -53,6 +54,7 @@ ARMS = {
     "plain_cg": dict(preconditioner=capi.PRECONDITIONER_NONE),
     "jacobi": dict(),
     "projected": dict(warm_start=capi.WARM_START_PROJECTED),
+    "extrapolated": dict(warm_start=capi.WARM_START_EXTRAPOLATED, warm_history=4),
     "learned": dict(warm_start=capi.WARM_START_LEARNED),
 }
 
