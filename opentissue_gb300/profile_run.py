@@ -29,6 +29,10 @@ from opentissue_gb300 import build, capi  # noqa: E402
 from opentissue_gb300.fem import generate_blocks  # noqa: E402
 
 
+WARM_STARTS = {"previous": capi.WARM_START_PREVIOUS, "projected": capi.WARM_START_PROJECTED,
+               "extrapolated": capi.WARM_START_EXTRAPOLATED}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--dims", type=int, nargs=3, default=[128, 32, 32])
@@ -36,7 +40,7 @@ def main():
     ap.add_argument("--sweeps", type=int, default=4)
     ap.add_argument("--variant", type=int, default=-1, help="force an element-apply variant (0..3)")
     ap.add_argument("--solver", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--warm-start", default="previous", choices=["previous", "projected"])
+    ap.add_argument("--warm-start", default="previous", choices=["previous", "projected", "extrapolated"])
     ap.add_argument("--trace", action="store_true",
                     help="print the last step's phases and per-iteration breakdown (SM clock stamps)")
     ap.add_argument("--batch", type=int, default=0, help="a batch of the first M beams of the batch workload")
@@ -67,7 +71,7 @@ def main():
     f[fixed == 0, 1] = -9.81 * mass[fixed == 0]
     capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
     solver = capi.SOLVER_MIXED if args.solver == "mixed" else capi.SOLVER_FP64
-    warm = capi.WARM_START_PROJECTED if args.warm_start == "projected" else capi.WARM_START_PREVIOUS
+    warm = WARM_STARTS[args.warm_start]
     p = capi.default_params(solver=solver, max_iterations=5000, rtol=1e-6, graph=0, warm_start=warm)
     st = capi.StepStats()
     for _ in range(args.steps):
@@ -111,7 +115,7 @@ def run_batch(lib, args):
     capi.check(lib.otfem_get_nodes(h, capi.MASS, mass.ctypes.data_as(dp), N))
     f = wl.batch_forces(beams, mass, 0, 0.005, False)
     capi.check(lib.otfem_set_nodes(h, capi.F_EXTERNAL, f.ctypes.data_as(dp), f.size))
-    warm = capi.WARM_START_PROJECTED if args.warm_start == "projected" else capi.WARM_START_PREVIOUS
+    warm = WARM_STARTS[args.warm_start]
     p = capi.default_params(solver=capi.SOLVER_MIXED, max_iterations=5000, rtol=1e-6, graph=0, warm_start=warm)
     st = capi.StepStats()
     for k in range(args.steps):
