@@ -54,7 +54,8 @@ def _run(params, pinned, steps=6, dims=(12, 5, 4)):
 
 
 @pytest.mark.parametrize("pinned", [True, False])
-@pytest.mark.parametrize("warm", [capi.WARM_START_PREVIOUS, capi.WARM_START_PROJECTED])
+@pytest.mark.parametrize("warm", [capi.WARM_START_PREVIOUS, capi.WARM_START_PROJECTED,
+                                  capi.WARM_START_EXTRAPOLATED])
 def test_host_step_matches_the_copy_sequence(gpu, pinned, warm):
     """The matrix-free solver: positions and velocities as the copy sequence's
     (the apply's unordered float reductions make two runs differ in the last

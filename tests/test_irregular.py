@@ -110,7 +110,7 @@ def test_irregular_matrix_free_vs_oracle(gpu, oracle, variant):
         o.simulate_converged(0.01, True, 2.0, 1e-11, 100000)
         ref.append(o.get(oracle.COORD))
     o.close()
-    for warm in (capi.WARM_START_PREVIOUS, capi.WARM_START_PROJECTED):
+    for warm in (capi.WARM_START_PREVIOUS, capi.WARM_START_PROJECTED, capi.WARM_START_EXTRAPOLATED):
         m = GpuMesh(tets, coord, fixed)
         m.init()
         capi.check(m.lib.otfem_set_apply_variant(m.h, variant))
