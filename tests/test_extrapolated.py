@@ -99,3 +99,36 @@ def test_extrapolated_start_parameter_checks(gpu):
     rc, _ = m.step(0.01, True, params(solver=capi.SOLVER_FP64, warm_start=EXTRAP), check=False)
     assert rc == capi.ERR_UNSUPPORTED
     m.close()
+
+
+def test_extrapolated_start_after_a_velocity_reset(gpu):
+    """An abrupt change of the motion (the velocities set to zero by hand)
+    leaves the history predicting the old motion: the start is poor, and the
+    step still ends at the answer a mesh without history gives from the
+    same state."""
+    tets, coord, fixed = beam(*DIMS, jitter_seed=11)
+    m = GpuMesh(tets, coord, fixed)
+    m.init()
+    p4 = params(warm_start=EXTRAP, warm_history=4)
+    f = gravity_force(m.get(capi.MASS), fixed)
+    for _ in range(10):
+        m.set(capi.F_EXTERNAL, f)
+        m.step(0.01, True, p4)
+    x = m.get(capi.COORD)
+    zero = np.zeros_like(x)
+    m.set(capi.VELOCITY, zero)
+    _, st = m.step(0.01, True, p4)
+    assert st.status == capi.OK and st.rel_residual <= 1e-6
+    fresh = GpuMesh(tets, coord, fixed)
+    fresh.init()
+    fresh.set(capi.COORD, x)
+    fresh.set(capi.VELOCITY, zero)
+    fresh.set(capi.F_EXTERNAL, f)
+    _, st0 = fresh.step(0.01, True, params())
+    v, v0 = m.get(capi.VELOCITY), fresh.get(capi.VELOCITY)
+    assert np.abs(v - v0).max() <= 1e-5 * np.abs(v0).max(), np.abs(v - v0).max() / np.abs(v0).max()
+    print(f"after the reset: extrapolated start {st.iterations} iterations "
+          f"(start rel. residual {st.initial_rel_residual:.2e}), previous velocity {st0.iterations} "
+          f"({st0.initial_rel_residual:.2e})")
+    m.close()
+    fresh.close()
