@@ -93,7 +93,10 @@ enum {
    * since a step that recorded none).  No extra element-apply.  A smooth
    * trajectory's next velocity is predicted well; after an abrupt change of
    * the motion (a velocity set by hand, a jump of the load) the start can be
-   * poor for a few steps, and CG still stops at the same residual. */
+   * poor for a few steps, and CG still stops at the same residual.  In a
+   * batch of at most 512 meshes, a mesh whose previous solve took at least
+   * half the batch's largest iteration count starts from its projected start
+   * instead (larger batches: every mesh). */
   OTFEM_WARM_START_EXTRAPOLATED = 3
 };
 

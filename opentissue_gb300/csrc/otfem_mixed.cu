@@ -1551,13 +1551,16 @@ __device__ void apply_staged_dirs(const MixedArgs& a, float scale, unsigned char
       tet_apply(e.Re, e.b, e.c0, e.c1, e.c2, scale, e.nn, warm_dir(a, j), nullptr, a.wprod + size_t(j) * a.N);
   });
 }
-__device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
+// dir_mask (batches; null: every mesh): the meshes whose tets also apply A
+// to the search directions.
+__device__ void apply_tets_dirs(const MixedArgs& a, float scale, const unsigned char* dir_mask) {
   const int T = a.T, TT = a.tile_tets, stride = gridDim.x * blockDim.x;
   int t = int(sweep_first());
   int4 ids = tile_node_ids(a, t);
   for (; t < T; t += stride) {
     const int4 cur = ids;
     ids = tile_node_ids(a, t + stride);
+    const int nw = !dir_mask || dir_mask[a.mesh_of_tet[t]] ? a.nwarm : 0;
     const int tile = tile_of(t, a.tile_magic);
     const float* w = a.tile_f + size_t(tile) * kTileWords * TT + (t - tile * TT);
     const float4 quat = make_float4(w[4 * TT], w[5 * TT], w[6 * TT], w[7 * TT]);
@@ -1566,7 +1569,7 @@ __device__ void apply_tets_dirs(const MixedArgs& a, float scale) {
     for (int k = 0; k < 9; ++k) b[k] = w[(8 + k) * TT];
     const float c0 = w[17 * TT], c1 = w[18 * TT], c2 = w[19 * TT];
     const int nn[4] = {cur.x, cur.y, cur.z, cur.w};
-    for (int j = -1; j < a.nwarm; ++j) {
+    for (int j = -1; j < nw; ++j) {
       float Re[9];
       quaternion_to_rotation(quat, Re);
       if (j < 0) tet_apply(Re, b, c0, c1, c2, scale, nn, a.v_f, a.v_lo, a.q_f);
@@ -1601,15 +1604,18 @@ __device__ __forceinline__ void apply_sweep(const MixedArgs& a, const typename A
 
 // Projected start: A v (into q) and A W_j for every search direction
 // (products into a.wprod).  Tets and staged variants do all operands in one
-// pass; the patch variants sweep once per operand.
+// pass; the patch variants sweep once per operand.  dir_mask (batches, tets
+// variant): only the meshes it marks apply the directions (the staged
+// variant applies them for every mesh).
 template <bool AllowStream>
-__device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round) {
+__device__ bool apply_start_operands(const MixedArgs& a, float scale, unsigned char* smem, unsigned& round,
+                                     const unsigned char* dir_mask = nullptr) {
   if (a.apply_variant == kApplyStaged) {
     apply_staged_dirs(a, scale, smem);
     return true;
   }
   if (a.apply_variant == kApplyTets) {
-    apply_tets_dirs(a, scale);
+    apply_tets_dirs(a, scale, dir_mask);
     return true;
   }
   apply_sweep<float, AllowStream>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
@@ -2951,9 +2957,29 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
   const long long t_start = tracer ? cycles_now() : 0ll;
   if (tracer) clear_phase_stamps(a);
 
+  // The extrapolated start in a batch: a mesh whose previous solve took at
+  // least half the batch's largest iteration count (the meshes the lock-step
+  // waits for) starts from its projected start instead; the others
+  // extrapolate, and their tets skip the search directions in the start
+  // sweep.  Batches of at most kLocalMeshes meshes; larger ones project every
+  // mesh.  proj: null when every mesh projects.
+  __shared__ unsigned char s_proj[kLocalMeshes];
+  __shared__ int s_maxits;
+  const bool hybrid = a.extrap_k > 0 && a.nwarm > 0 && a.nwarm == a.hist_k && M <= kLocalMeshes &&
+                      blockDim.x == kBlock;
+  if (hybrid) {
+    if (threadIdx.x == 0) s_maxits = 0;
+    __syncthreads();
+    const int its = threadIdx.x < M ? __ldcg(&a.bm[threadIdx.x].iterations) : 0;
+    atomicMax(&s_maxits, its);
+    __syncthreads();
+    if (threadIdx.x < M) s_proj[threadIdx.x] = 2 * its >= s_maxits ? 1 : 0;
+    __syncthreads();
+  }
+  const unsigned char* proj = hybrid ? s_proj : nullptr;
   // Phase 0 (as k_cg_mixed): b, diagonal, operand v (+ learned guess or
   // extrapolation), q = 0
-  const int deg = extrap_degree(a);
+  const int deg = hybrid ? extrap_degree(a) : 0;
   {
     SegSum<1> ss;
     ss.start(first_mesh);
@@ -2993,7 +3019,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
         }
         a.r_f[i] = make_float4(0.f, 0.f, 0.f, sp);  // r.w: the node's preconditioner scalar
         DF v0[3] = {vi[0], vi[1], vi[2]};
-        if (deg > 0 && !fx) extrapolate(a, i, deg, v0);  // extrapolated start (as k_cg_mixed)
+        if (deg > 0 && !fx && !proj[m]) extrapolate(a, i, deg, v0);  // extrapolated start (as k_cg_mixed)
         a.v_f[i] = make_float4(v0[0].hi, v0[1].hi, v0[2].hi, fx ? 0.f : 1.f);
         a.v_lo[i] = make_float4(v0[0].lo, v0[1].lo, v0[2].lo, 0.f);
         a.q_f[i] = zero4;
@@ -3016,7 +3042,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
   // initial residual r = b - A v (FP64), p = S r, for every mesh; with the
   // projected or learned start also A W_j and each mesh's start (k_cg_mixed)
   if (a.nwarm) {
-    if (!apply_start_operands<true>(a, scale, smem, round)) return;
+    if (!apply_start_operands<true>(a, scale, smem, round, proj)) return;
     sweeps += 1 + a.nwarm;
   } else {
     apply_sweep<float>(a, a.v_f, a.v_lo, a.q_f, a.re_f, a.b_f, a.c_f, scale, smem);
@@ -3055,7 +3081,7 @@ __global__ void __launch_bounds__(kBlock, 1) k_cg_batch(MixedArgs a) {
         float v8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (valid) {
           m = a.mesh_of_node[i];
-          if (!a.fixed[i]) {
+          if (!a.fixed[i] && (!proj || proj[m])) {  // extrapolating meshes: no Gram system (no move)
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
               if (c0 + k >= nv) break;
@@ -4052,6 +4078,9 @@ static void fill_args(MixedArgs& a, Context& c, double dt, const otfem_solver_pa
   a.hist_k = 0;
   if (a.hist && prm.warm_start == OTFEM_WARM_START_PROJECTED) a.hist_k = prm.warm_history;
   if (a.hist && learned) a.hist_k = std::max(prm.warm_history, 1);
+  // batches: the extrapolated start projects the meshes that iterate longest
+  // (k_cg_batch), so their search directions are set up as for the projected start
+  if (a.hist && prm.warm_start == OTFEM_WARM_START_EXTRAPOLATED && c.num_meshes > 1) a.hist_k = prm.warm_history;
   a.nwarm = a.hist_k + (learned ? 1 : 0);
   a.extrap_k = a.hist && prm.warm_start == OTFEM_WARM_START_EXTRAPOLATED ? prm.warm_history : 0;
   a.hist_fill = c.hist_fill;
