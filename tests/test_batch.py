@@ -116,18 +116,21 @@ def test_batch_against_the_fp64_oracle(gpu, oracle):
     b.close()
 
 
-def test_batch_beyond_the_local_mesh_limit(gpu):
+@pytest.mark.parametrize("warm", [capi.WARM_START_PREVIOUS, capi.WARM_START_EXTRAPOLATED])
+def test_batch_beyond_the_local_mesh_limit(gpu, warm):
     """Up to 512 meshes every CTA runs the iterations' scalar steps on its own
     copy of the meshes' state; beyond that the last CTA of each reduction runs
     them for all.  520 copies of six beams step as the six beams do alone.
     The iteration counts may differ by one refresh period (4): a mesh near
     the tolerance at a refresh point converges there or 4 iterations later,
     depending on the last bits of its sums (FP64 atomics in no fixed order
-    already flip it from run to run)."""
+    already flip it from run to run).  With the extrapolated start the large
+    batch projects every mesh (the per-mesh choice needs the shared copy), so
+    only the answers are compared."""
     beams = random_beams(6, seed=35, nx=(4, 7), nyz=(2, 3))
     many = [beams[k % len(beams)] for k in range(520)]
-    small_b, small = run_batch(beams, 3)
-    big_b, big = run_batch(many, 3)
+    small_b, small = run_batch(beams, 3, warm_start=warm)
+    big_b, big = run_batch(many, 3, warm_start=warm)
     for s in range(3):
         xs_small, (its_small, _, _, _), _ = small[s]
         xs_big, (its_big, st_big, rel_big, _), agg = big[s]
@@ -137,7 +140,8 @@ def test_batch_beyond_the_local_mesh_limit(gpu):
             j = k % len(beams)
             disp = np.abs(xs_small[j] - beams[j]["coord"]).max()
             assert np.abs(xs_big[k] - xs_small[j]).max() <= 1e-5 * disp, (s, k)
-            assert abs(int(its_big[k]) - int(its_small[j])) <= 4, (s, k)
+            if warm == capi.WARM_START_PREVIOUS:
+                assert abs(int(its_big[k]) - int(its_small[j])) <= 4, (s, k)
     small_b.close()
     big_b.close()
 
